@@ -1,0 +1,362 @@
+"""Benchmark: particle-updates/s of the WCSPH time step on the 3-D dam break
+(524,288 fluid + 430,572 wall particles, h = 1.3 dx, Tait, alpha = 0.01).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+                  [--workload dambreak3d|peristalsis|poiseuille]
+
+Own arm: the CUDA solver through its C ABI.  `value` is fluid particles x steps /
+device seconds with the state resident in HBM (the step is replayed as a CUDA
+graph; the working set exceeds the 126 MB L2, so no flush is needed); `e2e` is
+the same metric through the public API with host buffers: every step uploads
+position/velocity/leap-frog velocity from pinned host memory, runs update() and
+reads the three arrays back.  The dominant kernel's roofline uses its algorithmic
+bytes per launch over its CUDA-event duration inside timed steps.
+
+Reference arm (--impl reference): the reference's CPU restatement (oracle port;
+the reference itself is CUDA-only and its host code needs OpenGL) on all host
+cores, same workload and metric.
+
+N > 1 (torchrun): independent replicas, one per GPU (the step has no exchange),
+barrier + max-over-ranks timing, value summed over ranks.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "particle-updates/s"
+
+# Algorithmic bytes per particle and stage (float4 arrays read or written once,
+# neighbour re-reads counted once, P = radix passes).
+STAGE_BYTES = {
+    "hash": 24, "reorder": 72, "density": 32,
+    "force": {0: 68, 1: 68, 2: 120}, "integrate": {0: 112, 1: 112, 2: 128},
+}
+
+
+def sort_bytes(passes):
+    return 4 + 16 * passes
+
+
+def load_peaks():
+    path = os.path.join(HERE, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_id=None):
+        self.proc = None
+        self.lines = []
+        cmd = ["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits", "-lms", "100"]
+        if gpu_id is not None:
+            cmd[1:1] = ["-i", str(gpu_id)]
+        try:
+            self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out = ""
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def gpu_selector():
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+    if vis:
+        return vis.split(",")[int(os.environ.get("LOCAL_RANK", "0")) % len(vis.split(","))]
+    try:
+        import torch
+        props = torch.cuda.get_device_properties(int(os.environ.get("LOCAL_RANK", "0")))
+        return "GPU-" + str(props.uuid)
+    except Exception:
+        return None
+
+
+def make_workload(name):
+    import cmag_gb300 as cm
+    from cmag_gb300 import presets
+    if name == "dambreak3d":
+        p, n, tank, L = presets.dambreak3d()
+        s = cm.DamBreakSystem(params=p, num_particles=n)
+        s.scene3d(tank, L, 0.01, 1973)
+        cfg = {"workload": "dambreak3d", "fluid": [64, 128, 64], "tank_cells": list(tank),
+               "wall_layers": L, "particles": n, "h_over_dx": 1.3, "kernel": "wendland-3d",
+               "alpha": 0.01, "dt": float(p.delta_time), "grid": list(p.grid_size)}
+        fluid = 64 * 128 * 64
+    elif name == "peristalsis":
+        p = presets.peristalsis_c3()
+        s = cm.PeristalsisSystem(params=p)
+        s.reset()
+        n = s.getNumParticles()
+        fluid = p.fluid_size[0] * p.fluid_size[1]
+        cfg = {"workload": "peristalsis2d", "fluid": [int(p.fluid_size[0]), int(p.fluid_size[1])],
+               "particles": n, "waves": 4, "grid": list(p.grid_size)}
+    else:
+        p = presets.poiseuille_c1()
+        s = cm.PoiseuilleFlowSystem(params=p)
+        s.reset()
+        n = s.getNumParticles()
+        fluid = 64 * 64
+        cfg = {"workload": "poiseuille2d", "fluid": [64, 64], "particles": n, "grid": list(p.grid_size)}
+    return s, p, n, fluid, cfg
+
+
+def oracle_state_for(name, p, n):
+    from oracle import oracle as O
+    from cmag_gb300 import presets
+    st = O.OracleState(p, n)
+    if name == "dambreak3d":
+        _, _, tank, L = presets.dambreak3d()
+        st.pos[:] = O.dambreak3d_scene(p, tank, L, 0.01, 1973)
+        st.meas[:, 0] = p.rest_density
+    else:
+        st.reset_reference()
+    return st
+
+
+def cpu_run(name, p, n, fluid, steps, threads):
+    """Oracle port on `threads` host threads: seconds for `steps` full steps."""
+    st = oracle_state_for(name, p, n)
+    st.step(threads=threads)  # warm (page-in, allocation)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        st.step(threads=threads)
+    dt = time.perf_counter() - t0
+    return fluid * steps / dt, dt
+
+
+def dist_init(n_gpus):
+    if n_gpus <= 1 and "RANK" not in os.environ:
+        return None
+    import torch
+    import torch.distributed as dist
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist.init_process_group("nccl")
+    return dist
+
+
+def barrier_max(dist, value):
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    dist.barrier()
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import cmag_gb300  # noqa: F401  (parameter derivation uses the host part of the ABI)
+    from oracle import oracle as O
+    O.build()
+    _, p, n, fluid, cfg = make_workload_cpu(args.workload)
+    threads = os.cpu_count() or 1
+    st = oracle_state_for(args.workload, p, n)
+    for _ in range(args.warmup):
+        st.step(threads=threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        st.step(threads=threads)
+    secs = time.perf_counter() - t0
+    value = fluid * args.steps / secs
+    line = {"metric": METRIC, "value": value, "unit": "particle-updates/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": secs * 1e3 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": cfg, "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": "particle-updates/s", "cores": threads,
+                             "kind": "port",
+                             "sample": "%d full steps of the %d-particle scene (oracle restatement "
+                                       "of the reference kernels; the reference itself is CUDA-only "
+                                       "and its host classes need OpenGL)" % (args.steps, n)},
+            "e2e": {"value": value, "unit": "particle-updates/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def make_workload_cpu(name):
+    """Parameter block and sizes without creating a device solver."""
+    from cmag_gb300 import presets
+    if name == "dambreak3d":
+        p, n, tank, L = presets.dambreak3d()
+        cfg = {"workload": "dambreak3d", "fluid": [64, 128, 64], "tank_cells": list(tank),
+               "wall_layers": L, "particles": n, "h_over_dx": 1.3, "kernel": "wendland-3d",
+               "alpha": 0.01, "dt": float(p.delta_time), "grid": list(p.grid_size)}
+        return None, p, n, 64 * 128 * 64, cfg
+    if name == "peristalsis":
+        p = presets.peristalsis_c3()
+        n = presets.reference_count(p)
+        return None, p, n, int(p.fluid_size[0] * p.fluid_size[1]), {
+            "workload": "peristalsis2d", "particles": n, "grid": list(p.grid_size)}
+    p = presets.poiseuille_c1()
+    n = presets.reference_count(p)
+    return None, p, n, 4096, {"workload": "poiseuille2d", "particles": n, "grid": list(p.grid_size)}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="own", choices=["own", "reference"])
+    ap.add_argument("--workload", default="dambreak3d", choices=["dambreak3d", "peristalsis", "poiseuille"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-steps", type=int, default=1)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    from cmag_gb300 import build as B
+    if not os.path.exists(B.LIB):
+        B.build()
+    dist = dist_init(args.gpus)
+    rank = int(os.environ.get("RANK", "0"))
+    world = dist.get_world_size() if dist else 1
+    import torch
+    torch.cuda.init()
+
+    s, p, n, fluid, cfg = make_workload(args.workload)
+    cfg["parallelism"] = "replicas%d" % world
+    cfg["l2"] = "inputs larger than L2 (working set %.0f MB)" % (
+        (n * (7 * 16 + 4 * 4) + 8 * p.num_grid_cells) / 1e6)
+
+    # warm-up (graph capture happens on the first step)
+    s.update_n(args.warmup)
+    s.synchronize()
+
+    # ---- device-resident timed region ----
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(gpu_selector())
+    time.sleep(0.3)
+    ms = s.timed_update(args.steps)
+    time.sleep(0.3)
+    clocks = sampler.stop()
+    torch.cuda.synchronize()
+    ms = barrier_max(dist, ms)
+    secs = ms / 1e3
+    value = fluid * args.steps * world / secs
+    s.synchronize()
+
+    # ---- per-stage times (plain launches, events around each stage) ----
+    s.set_stage_timing(True)
+    s.update_n(args.steps)
+    stage_ms, tsteps = s.stage_times()
+    s.set_stage_timing(False)
+    names = ["hash", "sort", "reorder", "density", "force", "integrate"]
+    per_stage = {nm: stage_ms[k] / max(tsteps, 1) for k, nm in enumerate(names)}
+    dom = max(per_stage, key=per_stage.get)
+    passes = max(1, (int(np.ceil(np.log2(max(p.num_grid_cells, 2)))) + 7) // 8)
+    bytes_pp = {"hash": STAGE_BYTES["hash"], "sort": sort_bytes(passes), "reorder": STAGE_BYTES["reorder"],
+                "density": STAGE_BYTES["density"], "force": STAGE_BYTES["force"][p.system],
+                "integrate": STAGE_BYTES["integrate"][p.system]}
+    peak, peak_kind = load_peaks()
+    achieved = bytes_pp[dom] * n / (per_stage[dom] / 1e3) / 1e9
+    traffic = None
+    tpath = os.path.join(HERE, "profiles", "traffic_%s.json" % cfg["workload"])
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            traffic = json.load(f).get(dom)
+
+    # ---- end-to-end through the public API with host buffers ----
+    import cmag_gb300 as cm
+    arrays = [cm.POSITION, cm.VELOCITY, cm.VELOCITYLEAPFROG]
+    host = {a: torch.empty((n, 4), dtype=torch.float32, pin_memory=True).numpy() for a in arrays}
+    for a in arrays:
+        host[a][:] = s.getArray(a)
+    e2e_steps = max(1, min(args.steps, 50))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        for a in arrays:
+            s.setArray(a, host[a])
+        s.update()
+        for a in arrays:
+            host[a][:] = s.getArray(a)
+    e2e_secs = barrier_max(dist, time.perf_counter() - t0)
+    e2e_value = fluid * e2e_steps * world / e2e_secs
+    io_bytes = 3 * 16 * n
+
+    launches_per_step = {0: 4 + passes + 3, 1: 4 + passes + 3, 2: 6 + passes + 3}[p.system]
+    line = {
+        "metric": METRIC, "value": value, "unit": "particle-updates/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded lattice + jitter, seed 1973)", "config": cfg,
+        "e2e": {"value": e2e_value, "unit": "particle-updates/s", "h2d_bytes_per_step": io_bytes,
+                "d2h_bytes_per_step": io_bytes, "steps": e2e_steps},
+        "gpu_launches": launches_per_step * args.steps,
+        "stage_ms": {k: round(v, 5) for k, v in per_stage.items()},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "bytes_per_particle": bytes_pp[dom]},
+        "clocks": clocks,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        from oracle import oracle as O
+        O.build()
+        v, dt = cpu_run(args.workload, p, n, fluid, args.cpu_steps, threads)
+        line["cpu_baseline"] = {"value": v, "unit": "particle-updates/s", "cores": threads,
+                                "kind": "port", "seconds": dt,
+                                "sample": "%d full step(s) of the same %d-particle scene"
+                                          % (args.cpu_steps, n)}
+    s.close()
+    if rank == 0:
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

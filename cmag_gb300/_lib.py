@@ -1,0 +1,97 @@
+"""ctypes binding of libcmag_sph.so (the C ABI of include/cmag_sph.h).
+
+The library is the only compute path: if it is missing this module raises on
+first use instead of falling back to anything else."""
+import ctypes
+import os
+
+from ._abi import SphParams
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libcmag_sph.so")
+
+_lib = None
+
+P = ctypes.POINTER
+c_u32p = P(ctypes.c_uint32)
+c_f32p = P(ctypes.c_float)
+c_sys = ctypes.c_void_p
+
+# every symbol the header declares, with its ctypes signature
+SIGNATURES = {
+    "cmag_version": ([], ctypes.c_char_p),
+    "cmag_last_error": ([], ctypes.c_char_p),
+    "cmag_system_last_error": ([c_sys], ctypes.c_char_p),
+    "cmag_dambreak_default_params": ([c_u32p, ctypes.c_int32, c_u32p, ctypes.c_float, P(SphParams)], ctypes.c_int),
+    "cmag_poiseuille_default_params": ([c_u32p, ctypes.c_int32, c_u32p, ctypes.c_float, P(SphParams)], ctypes.c_int),
+    "cmag_peristalsis_default_params": ([ctypes.c_float, c_u32p, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                         c_f32p, ctypes.c_int32, c_u32p, ctypes.c_float, P(SphParams)], ctypes.c_int),
+    "cmag_reference_particle_count": ([P(SphParams), c_u32p], ctypes.c_int),
+    "cmag_dambreak3d_particle_count": ([c_u32p, c_u32p, ctypes.c_uint32, c_u32p], ctypes.c_int),
+    "cmag_reference_scene": ([P(SphParams), c_f32p, ctypes.c_uint32], ctypes.c_int),
+    "cmag_peristalsis_mass_sum": ([P(SphParams), c_f32p, ctypes.c_uint32, c_f32p], ctypes.c_int),
+    "cmag_dambreak3d_scene_host": ([P(SphParams), c_u32p, ctypes.c_uint32, ctypes.c_float,
+                                    ctypes.c_uint64, c_f32p, ctypes.c_uint32], ctypes.c_int),
+    "cmag_system_create": ([P(SphParams), ctypes.c_uint32, P(c_sys)], ctypes.c_int),
+    "cmag_system_destroy": ([c_sys], ctypes.c_int),
+    "cmag_system_reset": ([c_sys], ctypes.c_int),
+    "cmag_dambreak3d_scene": ([c_sys, c_u32p, ctypes.c_uint32, ctypes.c_float, ctypes.c_uint64], ctypes.c_int),
+    "cmag_system_update": ([c_sys], ctypes.c_int),
+    "cmag_system_update_n": ([c_sys, ctypes.c_uint32], ctypes.c_int),
+    "cmag_system_timed_update": ([c_sys, ctypes.c_uint32, c_f32p], ctypes.c_int),
+    "cmag_system_run_stages": ([c_sys, ctypes.c_int32], ctypes.c_int),
+    "cmag_system_set_array": ([c_sys, ctypes.c_int32, c_f32p, ctypes.c_uint32, ctypes.c_uint32], ctypes.c_int),
+    "cmag_system_get_array": ([c_sys, ctypes.c_int32, c_f32p, ctypes.c_uint32, ctypes.c_uint32], ctypes.c_int),
+    "cmag_system_get_uint_array": ([c_sys, ctypes.c_int32, c_u32p, ctypes.c_uint32, ctypes.c_uint32], ctypes.c_int),
+    "cmag_system_device_array": ([c_sys, ctypes.c_int32], ctypes.c_void_p),
+    "cmag_system_num_particles": ([c_sys, c_u32p], ctypes.c_int),
+    "cmag_system_num_grid_cells": ([c_sys, P(ctypes.c_uint64)], ctypes.c_int),
+    "cmag_system_elapsed_time": ([c_sys, c_f32p], ctypes.c_int),
+    "cmag_system_get_params": ([c_sys, P(SphParams)], ctypes.c_int),
+    "cmag_system_set_params": ([c_sys, P(SphParams)], ctypes.c_int),
+    "cmag_dambreak_change_right_boundary": ([c_sys], ctypes.c_int),
+    "cmag_dambreak_remove_right_boundary": ([c_sys], ctypes.c_int),
+    "cmag_poiseuille_change_gravity": ([c_sys], ctypes.c_int),
+    "cmag_peristalsis_phase": ([c_sys, c_f32p, c_f32p, c_f32p, P(ctypes.c_int32)], ctypes.c_int),
+    "cmag_system_set_elapsed_time": ([c_sys, ctypes.c_float], ctypes.c_int),
+    "cmag_peristalsis_set_phase": ([c_sys, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                    ctypes.c_int32], ctypes.c_int),
+    "cmag_system_set_stream": ([c_sys, ctypes.c_void_p], ctypes.c_int),
+    "cmag_system_stream": ([c_sys], ctypes.c_void_p),
+    "cmag_system_set_graphs": ([c_sys, ctypes.c_int32], ctypes.c_int),
+    "cmag_system_synchronize": ([c_sys], ctypes.c_int),
+    "cmag_system_device_error_bits": ([c_sys, c_u32p], ctypes.c_int),
+    "cmag_system_set_stage_timing": ([c_sys, ctypes.c_int32], ctypes.c_int),
+    "cmag_system_stage_times": ([c_sys, c_f32p, c_u32p], ctypes.c_int),
+    "cmag_sort_particles": ([c_u32p, c_u32p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_void_p], ctypes.c_int),
+}
+
+
+class CmagError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("cmag status %d: %s" % (code, msg))
+        self.code = code
+
+
+def lib():
+    """Load the in-tree library (built by cmag_gb300.build / __graft_entry__.build)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("libcmag_sph.so is not built (%s); run "
+                              "`python -c 'import __graft_entry__ as g; g.build()'`" % LIB_PATH)
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (args, res) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+        _lib = L
+    return _lib
+
+
+def check(rc, handle=None):
+    if rc != 0:
+        L = lib()
+        msg = (L.cmag_system_last_error(handle) if handle else L.cmag_last_error()) or b""
+        raise CmagError(rc, msg.decode(errors="replace"))
+    return rc

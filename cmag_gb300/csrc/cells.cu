@@ -1,0 +1,246 @@
+// cells.cu -- grid hash, per-cell counts and dense cell offsets, sorted gather.
+//
+// The reference finds cell ranges after the sort: it clears cellStart for the
+// whole grid (cudaMemset, fluidSystem.cu:161) and writes cellStart/cellEnd where
+// the sorted hash changes (reorderDataAndFindCellStartD, fluid_kernel.cu:50-97).
+// Here the hash kernel also counts particles per cell (warp-aggregated atomics),
+// and one chained-scan pass turns the counts into a dense offset table
+//     off[c] = number of particles with hash < c,   c = 0 .. scan_cells,
+// so the particles of any run of consecutive cells [a, b] are the sorted range
+// [off[a], off[b+1]).  A row of neighbour cells costs two loads instead of one
+// or two per cell, and no full-grid clear is needed: the scan re-zeroes exactly
+// the counters it consumed.  The reference's cellStart/cellEnd arrays are
+// derived from the table on request (launch_cell_view).
+#include <cuda_runtime.h>
+
+#include "kernels.h"
+
+namespace cmag {
+
+namespace {
+
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 16;
+constexpr uint32_t kScanTile = kScanThreads * kScanItems;
+constexpr uint32_t kFlagAgg = 1u << 30;
+constexpr uint32_t kFlagPrefix = 2u << 30;
+constexpr uint32_t kCountMask = (1u << 30) - 1u;
+constexpr int kSpinLimit = 1 << 22;
+
+// calcHashD (fluid_kernel.cu:34-48) + per-cell counts + radix digit histograms
+__global__ void __launch_bounds__(256)
+    k_hash(DevParams p, const float4 *__restrict__ pos, uint32_t *__restrict__ hash,
+           uint32_t *__restrict__ cnt, uint32_t *__restrict__ hist, int passes,
+           uint32_t *err)
+{
+    __shared__ uint32_t s_hist[kMaxPasses * kRadix];
+    if (hist)
+        for (int b = threadIdx.x; b < passes * kRadix; b += blockDim.x) s_hist[b] = 0;
+    __syncthreads();
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t n = p.n;
+    // every lane runs the same trip count so the warp-collective calls stay converged
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+        uint32_t i = base + threadIdx.x;
+        bool valid = i < n;
+        uint32_t h = 0xffffffffu;
+        if (valid) {
+            float4 q = pos[i];
+            int3 g = grid_pos(p, q.x, q.y, q.z);
+            h = grid_hash(p, g.x, g.y, g.z);
+            hash[i] = h;
+        }
+        uint32_t peers = __match_any_sync(0xffffffffu, h);
+        bool leader = (threadIdx.x & 31) == (uint32_t)(__ffs(peers) - 1);
+        if (valid && leader) {
+            const uint32_t rel = h - p.scan_base;  // wraps for h < scan_base
+            if (rel < p.scan_cells) atomicAdd(&cnt[rel], (uint32_t)__popc(peers));
+            else set_error(err, CMAG_DEVERR_RANGE);
+        }
+        if (hist) {
+            for (int ps = 0; ps < passes; ++ps) {
+                uint32_t dg = valid ? ((h >> (8 * ps)) & 255u) : 0xffffffffu;
+                uint32_t dp = __match_any_sync(0xffffffffu, dg);
+                if (valid && (threadIdx.x & 31) == (uint32_t)(__ffs(dp) - 1))
+                    atomicAdd(&s_hist[ps * kRadix + dg], (uint32_t)__popc(dp));
+            }
+        }
+    }
+    __syncthreads();
+    if (hist)
+        for (int b = threadIdx.x; b < passes * kRadix; b += blockDim.x)
+            if (s_hist[b]) atomicAdd(&hist[b], s_hist[b]);
+}
+
+__global__ void __launch_bounds__(kScanThreads)
+    k_cell_scan(uint32_t *__restrict__ cnt, uint32_t *__restrict__ off, uint32_t m,
+                uint32_t *tile_ctr, uint32_t *status, uint32_t *err)
+{
+    __shared__ uint32_t s_warp[kScanThreads / 32];
+    __shared__ uint32_t s_tile, s_prefix;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) s_tile = atomicAdd(tile_ctr, 1u);
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const uint32_t first = tile * kScanTile + threadIdx.x * kScanItems;
+    uint32_t v[kScanItems];
+    uint32_t sum = 0;
+    if (first + kScanItems <= m) {
+        const uint4 *src = reinterpret_cast<const uint4 *>(cnt + first);
+#pragma unroll
+        for (int k = 0; k < kScanItems / 4; ++k) {
+            uint4 q = src[k];
+            v[4 * k] = q.x; v[4 * k + 1] = q.y; v[4 * k + 2] = q.z; v[4 * k + 3] = q.w;
+            if (q.x | q.y | q.z | q.w)
+                reinterpret_cast<uint4 *>(cnt + first)[k] = make_uint4(0, 0, 0, 0);
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k) {
+            uint32_t c = first + k;
+            v[k] = (c < m) ? cnt[c] : 0u;
+            if (c < m && v[k]) cnt[c] = 0;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) sum += v[k];
+
+    // block exclusive scan of the thread sums
+    uint32_t x = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    uint32_t wbase = 0, total = 0;
+#pragma unroll
+    for (int w = 0; w < kScanThreads / 32; ++w) {
+        uint32_t t = s_warp[w];
+        wbase += (w < warp) ? t : 0u;
+        total += t;
+    }
+    uint32_t texcl = wbase + x - sum;
+
+    if (threadIdx.x == 0) {
+        volatile uint32_t *st = status;
+        uint32_t exclusive = 0;
+        if (tile == 0) {
+            st[0] = kFlagPrefix | total;
+        } else {
+            st[tile] = kFlagAgg | total;
+            int t = (int)tile - 1;
+            while (t >= 0) {
+                uint32_t s;
+                int spins = 0;
+                while (true) {
+                    s = st[t];
+                    if (s & (kFlagAgg | kFlagPrefix)) break;
+                    if (++spins > kSpinLimit) {
+                        set_error(err, CMAG_DEVERR_LOOKBACK_TIMEOUT);
+                        s = kFlagPrefix;
+                        break;
+                    }
+                    if (spins > 8) __nanosleep(64);
+                }
+                exclusive += s & kCountMask;
+                if (s & kFlagPrefix) break;
+                --t;
+            }
+            st[tile] = kFlagPrefix | (exclusive + total);
+        }
+        s_prefix = exclusive;
+    }
+    __syncthreads();
+    uint32_t run = s_prefix + texcl;
+    if (first + kScanItems <= m) {
+        uint4 *dst = reinterpret_cast<uint4 *>(off + first);
+#pragma unroll
+        for (int k = 0; k < kScanItems / 4; ++k) {
+            uint4 q;
+            q.x = run; run += v[4 * k];
+            q.y = run; run += v[4 * k + 1];
+            q.z = run; run += v[4 * k + 2];
+            q.w = run; run += v[4 * k + 3];
+            dst[k] = q;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k) {
+            uint32_t c = first + k;
+            if (c < m) off[c] = run;
+            run += v[k];
+        }
+    }
+}
+
+// the copy half of reorderDataAndFindCellStartD (fluid_kernel.cu:91-96)
+__global__ void __launch_bounds__(256)
+    k_reorder(const uint32_t *__restrict__ idx, const float4 *__restrict__ pos,
+              const float4 *__restrict__ vlf, float4 *__restrict__ spos,
+              float4 *__restrict__ svel, uint32_t n)
+{
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t j = idx[i];
+    if (j >= n) j = i;  // only after a failed sort (reported by the sort itself)
+    spos[i] = __ldg(pos + j);
+    svel[i] = __ldg(vlf + j);
+}
+
+__global__ void k_cell_view(const uint32_t *__restrict__ off, uint32_t scan_base,
+                            uint32_t scan_cells, uint64_t ncells, uint32_t *__restrict__ cs,
+                            uint32_t *__restrict__ ce)
+{
+    for (uint64_t c = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; c < ncells;
+         c += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t a = 0, b = 0;
+        if (c >= scan_base && c - scan_base < scan_cells) {
+            a = off[c - scan_base];
+            b = off[c - scan_base + 1];
+        }
+        bool occupied = b > a;
+        cs[c] = occupied ? a : kEmptyCell;
+        ce[c] = occupied ? b : 0u;
+    }
+}
+
+}  // namespace
+
+void launch_hash(const DevParams &p, const float4 *pos, uint32_t *hash, uint32_t *cnt,
+                 uint32_t *hist, int passes, uint32_t *err, cudaStream_t st)
+{
+    if (p.n == 0) return;
+    uint32_t blocks = (p.n + 256 * 8 - 1) / (256 * 8);
+    if (blocks < 1) blocks = 1;
+    k_hash<<<blocks, 256, 0, st>>>(p, pos, hash, cnt, hist, passes, err);
+}
+
+size_t cell_scan_workspace_words(uint32_t m) { return 1 + (m + kScanTile - 1) / kScanTile; }
+
+void launch_cell_scan(uint32_t *cnt, uint32_t *off, uint32_t m, uint32_t *ws, uint32_t *err,
+                      cudaStream_t st)
+{
+    uint32_t tiles = (m + kScanTile - 1) / kScanTile;
+    k_cell_scan<<<tiles, kScanThreads, 0, st>>>(cnt, off, m, ws, ws + 1, err);
+}
+
+void launch_reorder(const uint32_t *idx, const float4 *pos, const float4 *vlf, float4 *spos,
+                    float4 *svel, uint32_t n, cudaStream_t st)
+{
+    if (n == 0) return;
+    k_reorder<<<(n + 255) / 256, 256, 0, st>>>(idx, pos, vlf, spos, svel, n);
+}
+
+void launch_cell_view(const uint32_t *off, uint32_t scan_base, uint32_t scan_cells,
+                      uint64_t ncells, uint32_t *cell_start, uint32_t *cell_end, cudaStream_t st)
+{
+    uint64_t blocks = (ncells + 255) / 256;
+    if (blocks > 4096) blocks = 4096;
+    if (blocks == 0) return;
+    k_cell_view<<<(uint32_t)blocks, 256, 0, st>>>(off, scan_base, scan_cells, ncells, cell_start,
+                                                  cell_end);
+}
+
+}  // namespace cmag

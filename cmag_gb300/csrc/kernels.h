@@ -1,0 +1,77 @@
+// kernels.h -- host-side launchers of the device kernels (internal interface
+// between the C ABI in system.cu and the kernel translation units).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "sph_common.cuh"
+
+namespace cmag {
+
+// ---- onesweep radix sort (sort.cu) ----------------------------------------
+constexpr int kSortThreads = 256;
+constexpr int kSortItems = 16;
+constexpr uint32_t kSortTile = kSortThreads * kSortItems;  // keys per tile
+constexpr int kRadixBits = 8;
+constexpr int kRadix = 256;
+constexpr int kMaxPasses = 4;
+
+inline int sort_passes(uint32_t key_bits) { return (int)((key_bits + kRadixBits - 1) / kRadixBits); }
+inline uint32_t sort_tiles(uint32_t n) { return (n + kSortTile - 1) / kSortTile; }
+
+// Workspace of one sort, in 32-bit words: digit histograms [4][256], tile
+// counters [4], then one look-back status array of tiles*256 words per pass.
+// Must be zero when a sort starts (sort_workspace_clear or a memset).
+size_t sort_workspace_words(uint32_t n, int passes);
+struct SortWorkspace {
+    uint32_t *hist;       // [kMaxPasses][256]
+    uint32_t *tile_ctr;   // [kMaxPasses]
+    uint32_t *status;     // [passes][tiles][256]
+};
+SortWorkspace sort_workspace_view(uint32_t *base, uint32_t n);
+
+// Digit histograms of all passes (used when the hash kernel did not fill them).
+void launch_digit_hist(const uint32_t *keys, uint32_t n, int passes, uint32_t *hist,
+                       cudaStream_t st);
+// One LSD pass on digit `pass`; identity_values: value = input position.
+void launch_onesweep_pass(const uint32_t *kin, const uint32_t *vin, uint32_t *kout,
+                          uint32_t *vout, uint32_t n, int pass, bool identity_values,
+                          const SortWorkspace &ws, uint32_t *err, cudaStream_t st);
+
+// ---- cells (cells.cu) --------------------------------------------------------
+// Hash every particle, count particles per cell and accumulate the sort's digit
+// histograms.  hist may be null.
+void launch_hash(const DevParams &p, const float4 *pos, uint32_t *hash, uint32_t *cnt,
+                 uint32_t *hist, int passes, uint32_t *err, cudaStream_t st);
+// Exclusive scan of cnt[0..m) into off[0..m) (single pass, chained look-back),
+// clearing cnt for the next step.  ws must hold cell_scan_workspace_words(m), zeroed.
+size_t cell_scan_workspace_words(uint32_t m);
+void launch_cell_scan(uint32_t *cnt, uint32_t *off, uint32_t m, uint32_t *ws, uint32_t *err,
+                      cudaStream_t st);
+// sortedPos/sortedVel gather (reorderDataAndFindCellStartD's copy half).
+void launch_reorder(const uint32_t *idx, const float4 *pos, const float4 *vlf, float4 *spos,
+                    float4 *svel, uint32_t n, cudaStream_t st);
+// Reference cellStart/cellEnd view of the dense offsets.
+void launch_cell_view(const uint32_t *off, uint32_t scan_base, uint32_t scan_cells,
+                      uint64_t ncells, uint32_t *cell_start, uint32_t *cell_end, cudaStream_t st);
+
+// ---- neighbour loops (neighbors.cu) ----------------------------------------
+void launch_density(const DevParams &p, int group, const float4 *spos, const uint32_t *off,
+                    float4 *meas, cudaStream_t st);
+void launch_force(const DevParams &p, int group, const float4 *spos, const float4 *svel,
+                  const float4 *meas, const uint32_t *idx, const uint32_t *off, float4 *out_a,
+                  float4 *out_b, cudaStream_t st);
+
+// ---- integration and wall motion (integrate.cu) ------------------------------
+void launch_phase(const DevParams &p, PhaseState *ph, float k_milli, cudaStream_t st);
+void launch_configure_boundary(const DevParams &p, float4 *pos, const PhaseState *ph,
+                               cudaStream_t st);
+void launch_integrate(const DevParams &p, float4 *pos, float4 *vel, float4 *vlf,
+                      const float4 *acc, const float4 *vforce, const float4 *pforce,
+                      const PhaseState *ph, cudaStream_t st);
+void launch_gate(const DevParams &p, float4 *pos, int remove, float dx, float fx, float fy,
+                 cudaStream_t st);
+
+}  // namespace cmag

@@ -1,0 +1,225 @@
+// sort.cu -- stable LSD radix sort of (cell hash, particle index) pairs.
+//
+// Replaces thrust::sort_by_key in sortParticles (DamBreak.Core/fluidSystem.cu:94-99,
+// Poiseuille.Core/poiseuilleFlowSystem.cu:103-108, PeristalsisSystem.cu:116-121).
+// One kernel launch per 8-bit digit, following the single-pass "onesweep" scheme
+// of Adinets & Merrill (2022):
+//   * the digit histograms of every pass come from one read of the keys (fused
+//     into the hash kernel, or launch_digit_hist);
+//   * each CTA takes the next tile from an atomic counter, ranks its keys with a
+//     warp-level multisplit (__match_any_sync), publishes its per-digit counts and
+//     resolves its global offsets by decoupled look-back over earlier tiles;
+//   * ranks follow input order inside a warp, warps follow each other inside a
+//     tile and tiles follow tile order, so the sort is stable and equals a stable
+//     sort by key -- bit-identical to the reference's thrust result.
+// Every look-back wait is bounded: after kSpinLimit polls the CTA records
+// CMAG_DEVERR_LOOKBACK_TIMEOUT, treats the missing count as zero and finishes.
+#include <cuda_runtime.h>
+
+#include "kernels.h"
+
+namespace cmag {
+
+namespace {
+
+constexpr uint32_t kFlagAgg = 1u << 30;     // tile aggregate published
+constexpr uint32_t kFlagPrefix = 2u << 30;  // inclusive prefix published
+constexpr uint32_t kCountMask = (1u << 30) - 1u;
+constexpr int kSpinLimit = 1 << 22;
+constexpr int kWarps = kSortThreads / 32;
+constexpr uint32_t kInvalidDigit = 256;
+
+__device__ __forceinline__ uint32_t lanemask_lt()
+{
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// exclusive scan of one value per thread over a 256-thread block
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t *s_warp,
+                                                         uint32_t *total)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    uint32_t wbase = 0, all = 0;
+#pragma unroll
+    for (int w = 0; w < kWarps; ++w) {
+        uint32_t t = s_warp[w];
+        wbase += (w < warp) ? t : 0u;
+        all += t;
+    }
+    __syncthreads();
+    if (total) *total = all;
+    return wbase + x - v;
+}
+
+__global__ void __launch_bounds__(256) k_digit_hist(const uint32_t *__restrict__ keys, uint32_t n,
+                                                    int passes, uint32_t *__restrict__ hist)
+{
+    __shared__ uint32_t s_hist[kMaxPasses * kRadix];
+    for (int b = threadIdx.x; b < passes * kRadix; b += blockDim.x) s_hist[b] = 0;
+    __syncthreads();
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint32_t k = keys[i];
+        for (int ps = 0; ps < passes; ++ps) atomicAdd(&s_hist[ps * kRadix + ((k >> (8 * ps)) & 255u)], 1u);
+    }
+    __syncthreads();
+    for (int b = threadIdx.x; b < passes * kRadix; b += blockDim.x)
+        if (s_hist[b]) atomicAdd(&hist[b], s_hist[b]);
+}
+
+template <bool kIdentity>
+__global__ void __launch_bounds__(kSortThreads)
+    k_onesweep(const uint32_t *__restrict__ kin, const uint32_t *__restrict__ vin,
+               uint32_t *__restrict__ kout, uint32_t *__restrict__ vout, uint32_t n, int shift,
+               const uint32_t *__restrict__ hist, uint32_t *tile_ctr, uint32_t *status,
+               uint32_t *err)
+{
+    __shared__ uint32_t s_whist[kWarps][kRadix];  // per-warp digit counts -> offsets
+    __shared__ uint32_t s_base[kRadix];           // global start of each digit in this tile
+    __shared__ uint32_t s_scan[kWarps];
+    __shared__ uint32_t s_tile;
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) s_tile = atomicAdd(tile_ctr, 1u);
+    for (int b = threadIdx.x; b < kWarps * kRadix; b += kSortThreads) (&s_whist[0][0])[b] = 0;
+    // digit offsets of this pass: exclusive scan of the global histogram
+    uint32_t digit_start = block_exclusive_scan(hist[threadIdx.x], s_scan, nullptr);
+    const uint32_t tile = s_tile;  // visible: block_exclusive_scan synchronised
+
+    const uint32_t chunk = tile * kSortTile + (uint32_t)warp * (32u * kSortItems);
+    uint32_t key[kSortItems], val[kSortItems], off[kSortItems];
+#pragma unroll
+    for (int it = 0; it < kSortItems; ++it) {
+        uint32_t i = chunk + (uint32_t)it * 32u + (uint32_t)lane;
+        if (i < n) {
+            key[it] = kin[i];
+            val[it] = kIdentity ? i : vin[i];
+        } else {
+            key[it] = 0xffffffffu;
+            val[it] = 0;
+        }
+    }
+    const uint32_t lt = lanemask_lt();
+#pragma unroll
+    for (int it = 0; it < kSortItems; ++it) {
+        uint32_t i = chunk + (uint32_t)it * 32u + (uint32_t)lane;
+        uint32_t d = (i < n) ? ((key[it] >> shift) & 255u) : kInvalidDigit;
+        uint32_t peers = __match_any_sync(0xffffffffu, d);
+        uint32_t before = 0;
+        if (d != kInvalidDigit) before = s_whist[warp][d];
+        __syncwarp();
+        if (d != kInvalidDigit && lane == __ffs(peers) - 1) s_whist[warp][d] = before + __popc(peers);
+        __syncwarp();
+        off[it] = before + __popc(peers & lt);
+    }
+    __syncthreads();
+
+    // thread d owns digit d: warp-exclusive offsets and the tile total
+    const uint32_t d = threadIdx.x;
+    uint32_t run = 0;
+#pragma unroll
+    for (int w = 0; w < kWarps; ++w) {
+        uint32_t c = s_whist[w][d];
+        s_whist[w][d] = run;
+        run += c;
+    }
+    // decoupled look-back over the tiles before this one
+    volatile uint32_t *st = status;
+    uint32_t exclusive = 0;
+    if (tile == 0) {
+        st[d] = kFlagPrefix | run;
+    } else {
+        st[(size_t)tile * kRadix + d] = kFlagAgg | run;
+        int t = (int)tile - 1;
+        while (t >= 0) {
+            uint32_t v;
+            int spins = 0;
+            while (true) {
+                v = st[(size_t)t * kRadix + d];
+                if (v & (kFlagAgg | kFlagPrefix)) break;
+                if (++spins > kSpinLimit) {
+                    set_error(err, CMAG_DEVERR_LOOKBACK_TIMEOUT);
+                    v = kFlagPrefix;  // give up: count as zero and stop
+                    break;
+                }
+                if (spins > 8) __nanosleep(64);
+            }
+            exclusive += v & kCountMask;
+            if (v & kFlagPrefix) break;
+            --t;
+        }
+        st[(size_t)tile * kRadix + d] = kFlagPrefix | (exclusive + run);
+    }
+    s_base[d] = digit_start + exclusive;
+    __syncthreads();
+
+#pragma unroll
+    for (int it = 0; it < kSortItems; ++it) {
+        uint32_t i = chunk + (uint32_t)it * 32u + (uint32_t)lane;
+        if (i < n) {
+            uint32_t dd = (key[it] >> shift) & 255u;
+            uint32_t o = s_base[dd] + s_whist[warp][dd] + off[it];
+            if (o < n) {  // always true unless a look-back gave up
+                kout[o] = key[it];
+                vout[o] = val[it];
+            } else {
+                set_error(err, CMAG_DEVERR_RANGE);
+            }
+        }
+    }
+}
+
+}  // namespace
+
+size_t sort_workspace_words(uint32_t n, int passes)
+{
+    return (size_t)kMaxPasses * kRadix + kMaxPasses +
+           (size_t)(passes > 0 ? passes : 1) * sort_tiles(n) * kRadix;
+}
+
+SortWorkspace sort_workspace_view(uint32_t *base, uint32_t n)
+{
+    SortWorkspace ws;
+    ws.hist = base;
+    ws.tile_ctr = base + kMaxPasses * kRadix;
+    ws.status = ws.tile_ctr + kMaxPasses;
+    (void)n;
+    return ws;
+}
+
+void launch_digit_hist(const uint32_t *keys, uint32_t n, int passes, uint32_t *hist,
+                       cudaStream_t st)
+{
+    if (n == 0 || passes == 0) return;
+    uint32_t blocks = (n + 2047) / 2048;
+    if (blocks > 1216) blocks = 1216;  // 8 waves of 152 SMs
+    k_digit_hist<<<blocks, 256, 0, st>>>(keys, n, passes, hist);
+}
+
+void launch_onesweep_pass(const uint32_t *kin, const uint32_t *vin, uint32_t *kout,
+                          uint32_t *vout, uint32_t n, int pass, bool identity_values,
+                          const SortWorkspace &ws, uint32_t *err, cudaStream_t st)
+{
+    if (n == 0) return;
+    uint32_t tiles = sort_tiles(n);
+    uint32_t *status = ws.status + (size_t)pass * tiles * kRadix;
+    if (identity_values)
+        k_onesweep<true><<<tiles, kSortThreads, 0, st>>>(kin, vin, kout, vout, n, 8 * pass,
+                                                         ws.hist + pass * kRadix,
+                                                         ws.tile_ctr + pass, status, err);
+    else
+        k_onesweep<false><<<tiles, kSortThreads, 0, st>>>(kin, vin, kout, vout, n, 8 * pass,
+                                                          ws.hist + pass * kRadix,
+                                                          ws.tile_ctr + pass, status, err);
+}
+
+}  // namespace cmag

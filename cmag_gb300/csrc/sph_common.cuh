@@ -1,0 +1,149 @@
+// sph_common.cuh -- device parameter block and per-pair helpers shared by the
+// hash, neighbour-loop and integration kernels.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/cmag_sph.h"
+
+namespace cmag {
+
+constexpr uint32_t kEmptyCell = 0xffffffffu;
+
+// Launch-time parameter block: the cmag_sph_params fields the kernels read,
+// plus coefficients the host derives once (kernel normalisation, clamps).
+struct DevParams {
+    int32_t system, dims, kernel, eos;
+    uint32_t gx, gy, gz;          // grid cells per axis (powers of two)
+    uint32_t n;                   // particles
+    uint32_t scan_base;           // first cell covered by the dense offset table
+    uint32_t scan_cells;          // cells covered (one z layer for planar scenes)
+    float ox, oy, oz;             // world origin
+    float csx, csy, csz;          // cell size (DamBreak hash divides by it)
+    float r;                      // particle radius (other families' hash)
+    float h, inv_h, support2;     // smoothing length, 1/h, (2h)^2
+    float mass, rho0, c0, B, gamma, dt, damping, mu;
+    float gvx, gvy, gvz;          // gravity
+    int32_t cell_count;
+    int32_t planar;               // 1: search only the particle's own z layer
+    int32_t trim;                 // 1: trim rows/columns to the support sphere
+    float wsx, wsy, wsz;          // periodic image shift per axis
+    float right_boundary, left_border, bottom_border;
+    int32_t clamp_z;
+    float z_min_border, z_max_border;
+    float lj_D, lj_a;
+    int32_t lj_cutoff;
+    float av_alpha, av_eps2;      // artificial viscosity alpha, 0.001 h^2
+    float w_norm, dw_norm;        // kernel normalisations (see kernel_w/kernel_dw)
+    float wall_bottom, wall_top;  // Poiseuille extrapolation lines
+    float amplitude, wave_k, wave_speed, half_fluid_h;  // Peristalsis wall law
+    float half_world_x;
+    float p_wall;                 // Poiseuille wall pressure (EOS at rho0)
+};
+
+// Device-resident per-step scalars of the Peristalsis phase machine
+// (PeristalsisSystem.cpp:330-343), advanced on the device so that a captured
+// step can be replayed without host involvement.
+struct PhaseState {
+    float elapsed, time_shift, time_relax, wave_height;
+    int32_t is_bc;            // boundary-configuration flag seen by this step
+    int32_t configure;        // 1: configureBoundary runs this step
+    float configure_height;   // height passed to configureBoundary
+    float t;                  // time passed to the force/integrate kernels
+};
+
+// ---------------------------------------------------------------- hashing ---
+
+// calcGridPos: DamBreak divides by the cell size (fluid_kernel.cu:19-25); the
+// Poiseuille and Peristalsis copies multiply by 0.5f and divide by the radius
+// (poiseuilleFlowKernel.cu:18-24, PeristalsisKernel.cu:18-24).  The _rn
+// intrinsics keep every operation separately rounded so the result is the
+// reference's bit for bit; float->int truncation saturates like cvt.rzi.
+__device__ __forceinline__ int3 grid_pos(const DevParams &p, float x, float y, float z)
+{
+    int3 g;
+    if (p.system == CMAG_DAMBREAK) {
+        g.x = __float2int_rz(floorf(__fdiv_rn(__fsub_rn(x, p.ox), p.csx)));
+        g.y = __float2int_rz(floorf(__fdiv_rn(__fsub_rn(y, p.oy), p.csy)));
+        g.z = __float2int_rz(floorf(__fdiv_rn(__fsub_rn(z, p.oz), p.csz)));
+    } else {
+        g.x = __float2int_rz(floorf(__fdiv_rn(__fmul_rn(__fsub_rn(x, p.ox), 0.5f), p.r)));
+        g.y = __float2int_rz(floorf(__fdiv_rn(__fmul_rn(__fsub_rn(y, p.oy), 0.5f), p.r)));
+        g.z = __float2int_rz(floorf(__fdiv_rn(__fmul_rn(__fsub_rn(z, p.oz), 0.5f), p.r)));
+    }
+    return g;
+}
+
+// calcGridHash (fluid_kernel.cu:27-32): power-of-two wrap, z*Y*X + y*X + x.
+// The host checks that every product stays below 2^24 per operand, where the
+// reference's __umul24 equals a plain multiply.
+__device__ __forceinline__ uint32_t grid_hash(const DevParams &p, int gx, int gy, int gz)
+{
+    uint32_t x = (uint32_t)gx & (p.gx - 1u), y = (uint32_t)gy & (p.gy - 1u),
+             z = (uint32_t)gz & (p.gz - 1u);
+    return (z * p.gy) * p.gx + y * p.gx + x;
+}
+
+// EvaluateShift, PeristalsisUtil.cu:4-11
+__device__ __forceinline__ int eval_shift(int pos, uint32_t size)
+{
+    return pos < 0 ? -1 : (pos > (int)size - 1 ? 1 : 0);
+}
+
+// ----------------------------------------------------------- kernel W, dW ---
+
+// W(q) for q < 2.  Wendland C2: w_norm (1-q/2)^4 (2q+1) with w_norm = 7/(4 pi h^2)
+// in 2-D (fluid_kernel.cu:121-124) or 21/(16 pi h^3) in 3-D.  Cubic spline (M4):
+// w_norm = 10/(7 pi h^2) or 1/(pi h^3).
+__device__ __forceinline__ float kernel_w(const DevParams &p, float q)
+{
+    if (p.kernel == CMAG_KERNEL_WENDLAND) {
+        float t = 1.0f - 0.5f * q;
+        float t2 = t * t;
+        return p.w_norm * (t2 * t2) * (2.0f * q + 1.0f);
+    }
+    if (q < 1.0f) return p.w_norm * (1.0f - 1.5f * q * q + 0.75f * q * q * q);
+    float t = 2.0f - q;
+    return p.w_norm * 0.25f * t * t * t;
+}
+
+// dW/dr for q < 2.  Wendland: the reference's dw_norm (-(1-q/2)^3 (2q+1) + (1-q/2)^4)
+// with dw_norm = 7/(2 pi h^3) (fluid_kernel.cu:222-224) simplifies to
+// -2.5 dw_norm q (1-q/2)^3.  Cubic spline: dw_norm = w_norm / h.
+__device__ __forceinline__ float kernel_dw(const DevParams &p, float q)
+{
+    if (p.kernel == CMAG_KERNEL_WENDLAND) {
+        float t = 1.0f - 0.5f * q;
+        return -2.5f * p.dw_norm * q * (t * t * t);
+    }
+    if (q < 1.0f) return p.dw_norm * (-3.0f * q + 2.25f * q * q);
+    float t = 2.0f - q;
+    return p.dw_norm * (-0.75f * t * t);
+}
+
+// Equation of state (fluid_kernel.cu:168, poiseuilleFlowKernel.cu:181,
+// PeristalsisDensity.cu:75).
+__device__ __forceinline__ float eos_pressure(const DevParams &p, float rho)
+{
+    if (p.eos == CMAG_EOS_TAIT || p.system == CMAG_DAMBREAK) {
+        float x = rho / p.rho0;
+        float xg;
+        if (p.gamma == 7.0f) {
+            float x2 = x * x;
+            xg = x2 * x2 * x2 * x;
+        } else {
+            xg = powf(x, p.gamma);
+        }
+        return p.B * (xg - 1.0f);
+    }
+    if (p.system == CMAG_POISEUILLE) return (p.c0 * p.c0) * rho;
+    return 50.0f * p.c0 * rho;
+}
+
+__device__ __forceinline__ void set_error(uint32_t *err, uint32_t bits)
+{
+    if (err) atomicOr(err, bits);
+}
+
+}  // namespace cmag

@@ -1,0 +1,1042 @@
+// system.cu -- solver instances and the C ABI of include/cmag_sph.h.
+//
+// One cmag_system replaces one reference system object (DamBreakSystem,
+// PoiseuilleFlowSystem, PeristalsisSystem): it owns the device arrays the
+// reference allocates in _initialize (fluidSystem.cpp:116-190), a per-instance
+// parameter block (the reference keeps one global __constant__ block per library,
+// fluidSystem.cu:17-19) and a CUDA stream.  A step is the reference update()
+// stage sequence; it is captured once as a CUDA graph and replayed.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "host_scenes.h"
+#include "kernels.h"
+
+using namespace cmag;
+
+struct cmag_system {
+    cmag_sph_params p{};
+    uint32_t n = 0;
+    uint64_t ncells = 0;
+    int passes = 1;
+    int device = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    bool user_stream = false;
+
+    float4 *pos = nullptr, *vel = nullptr, *vlf = nullptr, *meas = nullptr, *acc = nullptr,
+           *vforce = nullptr, *pforce = nullptr, *pred = nullptr, *spos = nullptr,
+           *svel = nullptr;
+    uint32_t *hash[2] = {nullptr, nullptr}, *idx[2] = {nullptr, nullptr};
+    uint32_t *cnt = nullptr, *off = nullptr;
+    uint32_t *ws = nullptr;  // sort + scan workspace, cleared every step
+    size_t ws_words = 0, sort_words = 0;
+    uint32_t *err = nullptr;
+    PhaseState *phase = nullptr;
+    uint32_t *view_cs = nullptr, *view_ce = nullptr;
+
+    // host mirrors of device-side scalars
+    float elapsed = 0.0f;
+    PhaseState host_phase{};
+    float k_milli = 0.0f;  // powf(10, -3): configuration ramp rate factor
+
+    // layout
+    bool planar = false;
+    uint32_t scan_base = 0, scan_cells = 0;
+    bool z_uniform = false;
+    float z_value = 0.0f;
+    bool vz_nonzero = false;
+    int last_stage = CMAG_STAGE_INTEGRATE;
+
+    int g_density = 8, g_force = 8;
+
+    bool use_graphs = true;
+    cudaGraphExec_t gexec = nullptr;
+    bool gvalid = false;
+
+    bool timing = false;
+    std::vector<cudaEvent_t> events;  // 7 per timed step
+    size_t events_used = 0;
+    double stage_ms[6] = {0, 0, 0, 0, 0, 0};
+    uint32_t timed_steps = 0;
+
+    std::string last_error;
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(cmag_system *s, int code, const std::string &msg)
+{
+    if (s) s->last_error = msg;
+    g_last_error = msg;
+    return code;
+}
+
+#define CM_CUDA(s, call)                                                                    \
+    do {                                                                                    \
+        cudaError_t e_ = (call);                                                            \
+        if (e_ != cudaSuccess)                                                              \
+            return fail((s), e_ == cudaErrorMemoryAllocation ? CMAG_ERR_NOMEM : CMAG_ERR_CUDA, \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                \
+    } while (0)
+
+bool is_pow2(uint32_t v) { return v && !(v & (v - 1)); }
+
+uint32_t log2u(uint64_t v)
+{
+    uint32_t b = 0;
+    while ((1ull << b) < v) ++b;
+    return b;
+}
+
+int validate(const cmag_sph_params &p, uint32_t n, std::string &why)
+{
+    if (p.system < CMAG_DAMBREAK || p.system > CMAG_PERISTALSIS) return why = "unknown system", 1;
+    for (int k = 0; k < 3; ++k)
+        if (!is_pow2(p.grid_size[k])) return why = "grid_size must be powers of two", 1;
+    const uint64_t cells = (uint64_t)p.grid_size[0] * p.grid_size[1] * p.grid_size[2];
+    if (cells > (1ull << 31)) return why = "more than 2^31 grid cells", 1;
+    // the reference hashes with __umul24: equal to a plain product below 2^24
+    if ((uint64_t)p.grid_size[2] * p.grid_size[1] > (1u << 24) || p.grid_size[0] > (1u << 24))
+        return why = "grid too large for the 24-bit hash products", 1;
+    if (p.cell_count < 0 || p.cell_count > 64) return why = "cell_count out of range", 1;
+    // a run of 2c+1 cells must wrap at most once along x
+    if (p.grid_size[0] < (uint32_t)(2 * p.cell_count + 1))
+        return why = "grid_size[0] must be at least 2*cell_count+1", 1;
+    if (!(p.smoothing_radius > 0.0f) || !(p.particle_radius > 0.0f))
+        return why = "smoothing_radius and particle_radius must be positive", 1;
+    if (p.kernel != CMAG_KERNEL_WENDLAND && p.kernel != CMAG_KERNEL_CUBIC_SPLINE)
+        return why = "unknown kernel", 1;
+    if (p.dims != 2 && p.dims != 3) return why = "dims must be 2 or 3", 1;
+    if (n == 0 || n >= (1u << 30)) return why = "particle count must be in [1, 2^30)", 1;
+    return 0;
+}
+
+const double kPi = 3.14159265358979323846;
+
+DevParams make_dev(const cmag_system *s)
+{
+    const cmag_sph_params &p = s->p;
+    DevParams d;
+    std::memset(&d, 0, sizeof(d));
+    d.system = p.system; d.dims = p.dims; d.kernel = p.kernel; d.eos = p.eos;
+    d.gx = p.grid_size[0]; d.gy = p.grid_size[1]; d.gz = p.grid_size[2];
+    d.n = s->n;
+    d.scan_base = s->scan_base;
+    d.scan_cells = s->scan_cells;
+    d.ox = p.world_origin[0]; d.oy = p.world_origin[1]; d.oz = p.world_origin[2];
+    d.csx = p.cell_size[0]; d.csy = p.cell_size[1]; d.csz = p.cell_size[2];
+    d.r = p.particle_radius;
+    const double h = p.smoothing_radius;
+    d.h = p.smoothing_radius;
+    d.inv_h = (float)(1.0 / h);
+    d.support2 = (float)(4.0 * h * h);
+    d.mass = p.particle_mass; d.rho0 = p.rest_density; d.c0 = p.soundspeed;
+    d.B = p.B; d.gamma = p.gamma; d.dt = p.delta_time; d.damping = p.boundary_damping;
+    d.mu = p.mu;
+    d.gvx = p.gravity[0]; d.gvy = p.gravity[1]; d.gvz = p.gravity[2];
+    d.cell_count = p.cell_count;
+    d.planar = s->planar ? 1 : 0;
+    // rows can be trimmed to the support sphere unless some interaction reaches
+    // past q = 2 (the reference DamBreak wall force has no cut-off)
+    d.trim = (p.system != CMAG_DAMBREAK || p.lj_cutoff) ? 1 : 0;
+    if (p.system == CMAG_POISEUILLE) {
+        d.wsx = p.grid_size[0] * 2.0f * p.particle_radius;  // poiseuilleFlowKernel.cu:120
+    } else if (p.system == CMAG_PERISTALSIS) {
+        d.wsx = p.world_size[0]; d.wsy = p.world_size[1]; d.wsz = p.world_size[2];
+    }
+    d.right_boundary = p.right_boundary;
+    d.left_border = p.world_origin[0] + p.boundary_offset * 2 * p.particle_radius;
+    d.bottom_border = p.world_origin[1] + p.boundary_offset * 2 * p.particle_radius;
+    d.clamp_z = p.clamp_z;
+    d.z_min_border = p.z_min_border;
+    d.z_max_border = p.z_max_border;
+    d.lj_D = p.lj_D; d.lj_a = p.lj_a; d.lj_cutoff = p.lj_cutoff;
+    d.av_alpha = p.av_alpha;
+    d.av_eps2 = 0.001f * std::pow(p.smoothing_radius, 2.0f);
+    double wn, dwn;
+    if (p.kernel == CMAG_KERNEL_WENDLAND) {
+        wn = (p.dims == 2) ? 7.0 / (4.0 * kPi * h * h) : 21.0 / (16.0 * kPi * h * h * h);
+        dwn = 2.0 * wn / h;
+    } else {
+        wn = (p.dims == 2) ? 10.0 / (7.0 * kPi * h * h) : 1.0 / (kPi * h * h * h);
+        dwn = wn / h;
+    }
+    d.w_norm = (float)wn;
+    d.dw_norm = (float)dwn;
+    d.wall_bottom = p.world_origin[1] + p.boundary_offset * 2.0f * p.particle_radius;
+    d.wall_top = d.wall_bottom + p.fluid_size[1] * 2.0f * p.particle_radius;
+    d.amplitude = p.amplitude;
+    d.wave_k = 3.141592654f * p.wave_count / (p.fluid_size[0] * p.particle_radius);
+    d.wave_speed = p.wave_speed;
+    d.half_fluid_h = p.fluid_size[1] * p.particle_radius;
+    d.half_world_x = p.grid_size[0] * p.particle_radius;
+    if (p.eos == CMAG_EOS_TAIT) d.p_wall = 0.0f;
+    else d.p_wall = std::pow(p.soundspeed, 2.0f) * p.rest_density;  // poiseuilleFlowKernel.cu:156
+    return d;
+}
+
+// z cell of a position, as the hash computes it
+int z_cell(const cmag_sph_params &p, float z)
+{
+    float c = (p.system == CMAG_DAMBREAK) ? std::floor((z - p.world_origin[2]) / p.cell_size[2])
+                                          : std::floor((z - p.world_origin[2]) * 0.5f / p.particle_radius);
+    if (!(c == c)) return 0;
+    if (c >= 2147483648.0f) return 2147483647;
+    if (c <= -2147483648.0f) return -2147483647 - 1;
+    return (int)c;
+}
+
+void invalidate_graph(cmag_system *s)
+{
+    if (s->gexec) cudaGraphExecDestroy(s->gexec);
+    s->gexec = nullptr;
+    s->gvalid = false;
+}
+
+// Planar 2-D scenes (every particle at one z, no z motion) search and scan only
+// their own z layer; the result equals the full search whenever the grid has
+// more than cell_count layers (the layer is then reached only with dz = 0 and
+// every other layer is empty).
+void refresh_layout(cmag_system *s)
+{
+    const cmag_sph_params &p = s->p;
+    bool planar = p.dims == 2 && s->z_uniform && !s->vz_nonzero && p.gravity[2] == 0.0f &&
+                  (int)p.grid_size[2] > p.cell_count;
+    uint32_t base = 0, cells = (uint32_t)s->ncells;
+    if (planar) {
+        const uint32_t layer = (uint32_t)z_cell(p, s->z_value) & (p.grid_size[2] - 1u);
+        cells = p.grid_size[0] * p.grid_size[1];
+        base = layer * cells;
+    }
+    if (planar != s->planar || base != s->scan_base || cells != s->scan_cells) invalidate_graph(s);
+    s->planar = planar;
+    s->scan_base = base;
+    s->scan_cells = cells;
+}
+
+cudaStream_t st_of(cmag_system *s) { return s->stream; }
+
+uint32_t *sorted_hash(cmag_system *s) { return s->hash[s->passes & 1]; }
+uint32_t *sorted_idx(cmag_system *s) { return s->idx[s->passes & 1]; }
+
+int ensure_events(cmag_system *s, size_t count)
+{
+    while (s->events.size() < count) {
+        cudaEvent_t e;
+        CM_CUDA(s, cudaEventCreate(&e));
+        s->events.push_back(e);
+    }
+    return CMAG_OK;
+}
+
+// Enqueue the stages of one step up to and including `last` on the stream.
+int record_step(cmag_system *s, int last, bool timed)
+{
+    const DevParams d = make_dev(s);
+    cudaStream_t st = st_of(s);
+    const cmag_sph_params &p = s->p;
+    cudaEvent_t *ev = nullptr;
+    if (timed) {
+        if (ensure_events(s, s->events_used + 7) != CMAG_OK) return CMAG_ERR_CUDA;
+        ev = &s->events[s->events_used];
+        s->events_used += 7;
+    }
+    auto mark = [&](int k) { if (ev) cudaEventRecord(ev[k], st); };
+
+    if (p.system == CMAG_PERISTALSIS) {
+        launch_phase(d, s->phase, s->k_milli, st);
+        launch_configure_boundary(d, s->pos, s->phase, st);
+    }
+    mark(0);
+    CM_CUDA(s, cudaMemsetAsync(s->ws, 0, s->ws_words * sizeof(uint32_t), st));
+    SortWorkspace sw = sort_workspace_view(s->ws, s->n);
+    launch_hash(d, s->pos, s->hash[0], s->cnt, sw.hist, s->passes, s->err, st);
+    launch_cell_scan(s->cnt, s->off, s->scan_cells + 1, s->ws + s->sort_words, s->err, st);
+    mark(1);
+    if (last >= CMAG_STAGE_SORT) {
+        for (int k = 0; k < s->passes; ++k) {
+            const int src = k & 1, dst = src ^ 1;
+            launch_onesweep_pass(s->hash[src], s->idx[src], s->hash[dst], s->idx[dst], s->n, k,
+                                 k == 0, sw, s->err, st);
+        }
+    }
+    mark(2);
+    if (last >= CMAG_STAGE_REORDER)
+        launch_reorder(sorted_idx(s), s->pos, s->vlf, s->spos, s->svel, s->n, st);
+    mark(3);
+    if (last >= CMAG_STAGE_DENSITY) launch_density(d, s->g_density, s->spos, s->off, s->meas, st);
+    mark(4);
+    if (last >= CMAG_STAGE_FORCE) {
+        if (p.system == CMAG_PERISTALSIS)
+            launch_force(d, s->g_force, s->spos, s->svel, s->meas, sorted_idx(s), s->off,
+                         s->vforce, s->pforce, st);
+        else
+            launch_force(d, s->g_force, s->spos, s->svel, s->meas, sorted_idx(s), s->off, s->acc,
+                         nullptr, st);
+    }
+    mark(5);
+    if (last >= CMAG_STAGE_INTEGRATE)
+        launch_integrate(d, s->pos, s->vel, s->vlf, s->acc, s->vforce, s->pforce, s->phase, st);
+    mark(6);
+    CM_CUDA(s, cudaGetLastError());
+    return CMAG_OK;
+}
+
+// host mirror of k_phase (PeristalsisSystem.cpp:330-343, 407)
+void advance_host_mirror(cmag_system *s)
+{
+    const float dt = s->p.delta_time;
+    if (s->p.system == CMAG_PERISTALSIS) {
+        PhaseState &h = s->host_phase;
+        h.configure = 0;
+        if (h.is_bc) {
+            h.time_shift = h.time_shift + dt;
+            if (h.wave_height < s->p.amplitude) {
+                h.configure = 1;
+                h.configure_height = h.wave_height;
+                h.wave_height = h.wave_height + dt * s->k_milli;
+            } else {
+                h.time_relax = h.time_relax - dt;
+                if (h.time_relax < 0.0f) h.is_bc = 0;
+            }
+        }
+        h.t = h.is_bc ? 0.0f : h.elapsed - h.time_shift;
+        h.elapsed = h.elapsed + dt;
+        s->p.is_boundary_configuration = h.is_bc;
+        s->elapsed = h.elapsed;
+    } else {
+        s->elapsed = s->elapsed + dt;
+    }
+}
+
+int upload_phase(cmag_system *s)
+{
+    CM_CUDA(s, cudaMemcpyAsync(s->phase, &s->host_phase, sizeof(PhaseState),
+                               cudaMemcpyHostToDevice, st_of(s)));
+    CM_CUDA(s, cudaStreamSynchronize(st_of(s)));
+    return CMAG_OK;
+}
+
+int capture_graph(cmag_system *s)
+{
+    invalidate_graph(s);
+    cudaStream_t st = st_of(s);
+    CM_CUDA(s, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    int rc = record_step(s, CMAG_STAGE_INTEGRATE, false);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(st, &g);
+    if (rc != CMAG_OK) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    if (e != cudaSuccess) return fail(s, CMAG_ERR_CUDA, std::string("stream capture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&s->gexec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(s, CMAG_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+    s->gvalid = true;
+    return CMAG_OK;
+}
+
+int do_step(cmag_system *s)
+{
+    if (s->use_graphs && !s->timing && s->stream != nullptr) {
+        if (!s->gvalid) {
+            int rc = capture_graph(s);
+            if (rc != CMAG_OK) return rc;
+        }
+        CM_CUDA(s, cudaGraphLaunch(s->gexec, st_of(s)));
+    } else {
+        int rc = record_step(s, CMAG_STAGE_INTEGRATE, s->timing);
+        if (rc != CMAG_OK) return rc;
+        if (s->timing) s->timed_steps++;
+    }
+    s->last_stage = CMAG_STAGE_INTEGRATE;
+    advance_host_mirror(s);
+    return CMAG_OK;
+}
+
+float4 *float_array(cmag_system *s, int a)
+{
+    switch (a) {
+    case CMAG_POSITION: return s->pos;
+    case CMAG_VELOCITY: return s->vel;
+    case CMAG_MEASURES: return s->meas;
+    case CMAG_ACCELERATION: return s->acc;
+    case CMAG_VELOCITYLEAPFROG: return s->vlf;
+    case CMAG_VISCOUSFORCE: return s->vforce;
+    case CMAG_PRESSUREFORCE: return s->pforce;
+    case CMAG_PREDICTEDPOSITION: return s->pred;
+    case CMAG_SORTEDPOSITION: return s->spos;
+    case CMAG_SORTEDVELOCITY: return s->svel;
+    default: return nullptr;
+    }
+}
+
+void free_all(cmag_system *s)
+{
+    invalidate_graph(s);
+    for (auto e : s->events) cudaEventDestroy(e);
+    s->events.clear();
+    void *ptrs[] = {s->pos, s->vel, s->vlf, s->meas, s->acc, s->vforce, s->pforce, s->pred,
+                    s->spos, s->svel, s->hash[0], s->hash[1], s->idx[0], s->idx[1], s->cnt,
+                    s->off, s->ws, s->err, s->phase, s->view_cs, s->view_ce};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    if (s->own_stream) cudaStreamDestroy(s->own_stream);
+}
+
+template <class T>
+int dalloc(cmag_system *s, T **ptr, size_t bytes)
+{
+    CM_CUDA(s, cudaMalloc((void **)ptr, bytes));
+    CM_CUDA(s, cudaMemset(*ptr, 0, bytes));
+    return CMAG_OK;
+}
+
+int check_range(cmag_system *s, uint32_t start, uint32_t count, uint64_t size)
+{
+    if ((uint64_t)start + count > size)
+        return fail(s, CMAG_ERR_INVALID, "array range [" + std::to_string(start) + ", " +
+                                             std::to_string((uint64_t)start + count) +
+                                             ") exceeds " + std::to_string(size));
+    return CMAG_OK;
+}
+
+}  // namespace
+
+// ============================================================================
+// C ABI
+// ============================================================================
+
+extern "C" {
+
+const char *cmag_version(void) { return "cmag_gb300 0.1 (sm_103a)"; }
+
+const char *cmag_last_error(void) { return g_last_error.c_str(); }
+
+const char *cmag_system_last_error(const cmag_system *s)
+{
+    return s ? s->last_error.c_str() : g_last_error.c_str();
+}
+
+int cmag_dambreak_default_params(const uint32_t fluid_size[3], int32_t boundary_offset,
+                                 const uint32_t grid_size[3], float particle_radius,
+                                 cmag_sph_params *out)
+{
+    if (!out || !fluid_size || !grid_size) return fail(nullptr, CMAG_ERR_INVALID, "null argument");
+    dambreak_params(fluid_size, boundary_offset, grid_size, particle_radius, *out);
+    return CMAG_OK;
+}
+
+int cmag_poiseuille_default_params(const uint32_t fluid_size[3], int32_t boundary_offset,
+                                   const uint32_t grid_size[3], float particle_radius,
+                                   cmag_sph_params *out)
+{
+    if (!out || !fluid_size || !grid_size) return fail(nullptr, CMAG_ERR_INVALID, "null argument");
+    poiseuille_params(fluid_size, boundary_offset, grid_size, particle_radius, *out);
+    return CMAG_OK;
+}
+
+int cmag_peristalsis_default_params(float delta_time, const uint32_t fluid_size[3],
+                                    float amplitude, float wave_speed, float soundspeed,
+                                    const float gravity[3], int32_t boundary_offset,
+                                    const uint32_t grid_size[3], float radius,
+                                    cmag_sph_params *out)
+{
+    if (!out || !fluid_size || !grid_size || !gravity)
+        return fail(nullptr, CMAG_ERR_INVALID, "null argument");
+    peristalsis_params(delta_time, fluid_size, amplitude, wave_speed, soundspeed, gravity,
+                       boundary_offset, grid_size, radius, *out);
+    return CMAG_OK;
+}
+
+int cmag_reference_particle_count(const cmag_sph_params *p, uint32_t *out)
+{
+    if (!p || !out) return fail(nullptr, CMAG_ERR_INVALID, "null argument");
+    *out = reference_particle_count(*p);
+    return CMAG_OK;
+}
+
+int cmag_reference_scene(const cmag_sph_params *p, float *pos, uint32_t n)
+{
+    if (!p || (!pos && n)) return fail(nullptr, CMAG_ERR_INVALID, "null argument");
+    reference_scene(*p, pos, n);
+    return CMAG_OK;
+}
+
+int cmag_peristalsis_mass_sum(const cmag_sph_params *p, const float *pos, uint32_t n, float *out)
+{
+    if (!p || !out || (!pos && n)) return fail(nullptr, CMAG_ERR_INVALID, "null argument");
+    if (n <= p->grid_size[0] / 2) return fail(nullptr, CMAG_ERR_INVALID, "probe particle out of range");
+    *out = peristalsis_mass_sum(*p, pos, n);
+    return CMAG_OK;
+}
+
+int cmag_dambreak3d_scene_host(const cmag_sph_params *p, const uint32_t tank_cells[3],
+                               uint32_t layers, float jitter_frac, uint64_t seed, float *pos,
+                               uint32_t n)
+{
+    if (!p || !tank_cells || (!pos && n)) return fail(nullptr, CMAG_ERR_INVALID, "null argument");
+    std::memset(pos, 0, sizeof(float) * 4 * (size_t)n);
+    dambreak3d_scene(*p, tank_cells, layers, jitter_frac, seed, pos, n);
+    return CMAG_OK;
+}
+
+int cmag_dambreak3d_particle_count(const uint32_t fluid_size[3], const uint32_t tank_cells[3],
+                                   uint32_t layers, uint32_t *out)
+{
+    if (!fluid_size || !tank_cells || !out) return fail(nullptr, CMAG_ERR_INVALID, "null argument");
+    *out = dambreak3d_count(fluid_size, tank_cells, layers);
+    return CMAG_OK;
+}
+
+int cmag_system_create(const cmag_sph_params *params, uint32_t n, cmag_system **out)
+{
+    if (!params || !out) return fail(nullptr, CMAG_ERR_INVALID, "null argument");
+    *out = nullptr;
+    std::string why;
+    if (validate(*params, n, why)) return fail(nullptr, CMAG_ERR_INVALID, why);
+    cmag_system *s = new (std::nothrow) cmag_system();
+    if (!s) return fail(nullptr, CMAG_ERR_NOMEM, "host allocation failed");
+    s->p = *params;
+    s->n = n;
+    s->ncells = (uint64_t)params->grid_size[0] * params->grid_size[1] * params->grid_size[2];
+    const uint32_t bits = log2u(s->ncells);
+    s->passes = sort_passes(bits);
+    if (s->passes < 1) s->passes = 1;
+    s->k_milli = std::pow(10.0f, -3.0f);
+    s->scan_base = 0;
+    s->scan_cells = (uint32_t)s->ncells;
+    // 3-D searches need every axis wide enough for one wrap per run
+    if (params->dims == 3) {
+        s->g_density = 4;
+        s->g_force = 4;
+    }
+    int rc = CMAG_OK;
+    auto step = [&](int r) { if (rc == CMAG_OK) rc = r; };
+    cudaError_t e = cudaGetDevice(&s->device);
+    if (e != cudaSuccess) {
+        fail(nullptr, CMAG_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+        delete s;
+        return CMAG_ERR_CUDA;
+    }
+    e = cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        fail(nullptr, CMAG_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
+        delete s;
+        return CMAG_ERR_CUDA;
+    }
+    s->stream = s->own_stream;
+    const size_t f4 = sizeof(float4) * (size_t)n, u4 = sizeof(uint32_t) * (size_t)n;
+    step(dalloc(s, &s->pos, f4));
+    step(dalloc(s, &s->vel, f4));
+    step(dalloc(s, &s->vlf, f4));
+    step(dalloc(s, &s->meas, f4));
+    step(dalloc(s, &s->acc, f4));
+    step(dalloc(s, &s->spos, f4));
+    step(dalloc(s, &s->svel, f4));
+    if (params->system == CMAG_PERISTALSIS) {
+        step(dalloc(s, &s->vforce, f4));
+        step(dalloc(s, &s->pforce, f4));
+        step(dalloc(s, &s->pred, f4));
+    }
+    for (int k = 0; k < 2; ++k) {
+        step(dalloc(s, &s->hash[k], u4));
+        step(dalloc(s, &s->idx[k], u4));
+    }
+    // per-cell counters and offsets for the whole grid (+1 sentinel entry)
+    step(dalloc(s, &s->cnt, sizeof(uint32_t) * (s->ncells + 1)));
+    step(dalloc(s, &s->off, sizeof(uint32_t) * (s->ncells + 1)));
+    s->sort_words = sort_workspace_words(n, s->passes);
+    s->ws_words = s->sort_words + cell_scan_workspace_words((uint32_t)(s->ncells + 1));
+    step(dalloc(s, &s->ws, sizeof(uint32_t) * s->ws_words));
+    step(dalloc(s, &s->err, sizeof(uint32_t)));
+    step(dalloc(s, &s->phase, sizeof(PhaseState)));
+    if (rc != CMAG_OK) {
+        std::string msg = s->last_error;
+        free_all(s);
+        delete s;
+        g_last_error = msg;
+        return rc;
+    }
+    s->host_phase.is_bc = params->is_boundary_configuration;
+    s->host_phase.time_relax = 1000 * params->delta_time;
+    upload_phase(s);
+    refresh_layout(s);
+    *out = s;
+    return CMAG_OK;
+}
+
+int cmag_system_destroy(cmag_system *s)
+{
+    if (!s) return CMAG_OK;
+    cudaStreamSynchronize(s->stream);
+    free_all(s);
+    delete s;
+    return CMAG_OK;
+}
+
+int cmag_system_set_array(cmag_system *s, int32_t array, const float *host, uint32_t start,
+                          uint32_t count)
+{
+    if (!s || (!host && count)) return fail(s, CMAG_ERR_INVALID, "null argument");
+    float4 *d = float_array(s, array);
+    if (!d) return fail(s, CMAG_ERR_INVALID, "not a settable float4 array: " + std::to_string(array));
+    if (check_range(s, start, count, s->n) != CMAG_OK) return CMAG_ERR_INVALID;
+    if (count == 0) return CMAG_OK;
+    CM_CUDA(s, cudaMemcpyAsync(d + start, host, sizeof(float4) * (size_t)count,
+                               cudaMemcpyHostToDevice, st_of(s)));
+    CM_CUDA(s, cudaStreamSynchronize(st_of(s)));
+    if (array == CMAG_POSITION) {
+        bool uniform = true;
+        const float z0 = host[2];
+        for (uint32_t i = 0; i < count && uniform; ++i) uniform = host[4 * (size_t)i + 2] == z0;
+        if (start == 0 && count == s->n) {
+            s->z_uniform = uniform;
+            s->z_value = z0;
+        } else if (!uniform || z0 != s->z_value) {
+            s->z_uniform = false;
+        }
+    } else if (array == CMAG_VELOCITY || array == CMAG_VELOCITYLEAPFROG) {
+        bool nz = false;
+        for (uint32_t i = 0; i < count && !nz; ++i) nz = host[4 * (size_t)i + 2] != 0.0f;
+        if (nz) s->vz_nonzero = true;
+        else if (start == 0 && count == s->n && array == CMAG_VELOCITY) s->vz_nonzero = false;
+    }
+    refresh_layout(s);
+    return CMAG_OK;
+}
+
+int cmag_system_get_array(cmag_system *s, int32_t array, float *host, uint32_t start,
+                          uint32_t count)
+{
+    if (!s || (!host && count)) return fail(s, CMAG_ERR_INVALID, "null argument");
+    float4 *d = float_array(s, array);
+    if (!d) return fail(s, CMAG_ERR_INVALID, "not a float4 array: " + std::to_string(array));
+    if (check_range(s, start, count, s->n) != CMAG_OK) return CMAG_ERR_INVALID;
+    if (count == 0) return CMAG_OK;
+    CM_CUDA(s, cudaMemcpyAsync(host, d + start, sizeof(float4) * (size_t)count,
+                               cudaMemcpyDeviceToHost, st_of(s)));
+    CM_CUDA(s, cudaStreamSynchronize(st_of(s)));
+    return CMAG_OK;
+}
+
+int cmag_system_get_uint_array(cmag_system *s, int32_t array, uint32_t *host, uint32_t start,
+                               uint32_t count)
+{
+    if (!s || (!host && count)) return fail(s, CMAG_ERR_INVALID, "null argument");
+    const uint32_t *src = nullptr;
+    uint64_t size = s->n;
+    switch (array) {
+    case CMAG_HASH: src = (s->last_stage == CMAG_STAGE_HASH) ? s->hash[0] : sorted_hash(s); break;
+    case CMAG_INDEX:
+        if (s->last_stage == CMAG_STAGE_HASH) {  // before the sort: identity
+            if (check_range(s, start, count, s->n) != CMAG_OK) return CMAG_ERR_INVALID;
+            for (uint32_t i = 0; i < count; ++i) host[i] = start + i;
+            return CMAG_OK;
+        }
+        src = sorted_idx(s);
+        break;
+    case CMAG_CELLOFFSET: src = s->off; size = (uint64_t)s->scan_cells + 1; break;
+    case CMAG_CELLSTART:
+    case CMAG_CELLEND: {
+        size = s->ncells;
+        if (!s->view_cs) {
+            if (dalloc(s, &s->view_cs, sizeof(uint32_t) * s->ncells) != CMAG_OK) return CMAG_ERR_NOMEM;
+            if (dalloc(s, &s->view_ce, sizeof(uint32_t) * s->ncells) != CMAG_OK) return CMAG_ERR_NOMEM;
+        }
+        launch_cell_view(s->off, s->scan_base, s->scan_cells, s->ncells, s->view_cs, s->view_ce,
+                         st_of(s));
+        CM_CUDA(s, cudaGetLastError());
+        src = (array == CMAG_CELLSTART) ? s->view_cs : s->view_ce;
+        break;
+    }
+    default: return fail(s, CMAG_ERR_INVALID, "not a uint32 array: " + std::to_string(array));
+    }
+    if (check_range(s, start, count, size) != CMAG_OK) return CMAG_ERR_INVALID;
+    if (count == 0) return CMAG_OK;
+    CM_CUDA(s, cudaMemcpyAsync(host, src + start, sizeof(uint32_t) * (size_t)count,
+                               cudaMemcpyDeviceToHost, st_of(s)));
+    CM_CUDA(s, cudaStreamSynchronize(st_of(s)));
+    return CMAG_OK;
+}
+
+void *cmag_system_device_array(cmag_system *s, int32_t array)
+{
+    if (!s) return nullptr;
+    switch (array) {
+    case CMAG_HASH: return sorted_hash(s);
+    case CMAG_INDEX: return sorted_idx(s);
+    case CMAG_CELLOFFSET: return s->off;
+    default: return float_array(s, array);
+    }
+}
+
+int cmag_system_reset(cmag_system *s)
+{
+    if (!s) return fail(nullptr, CMAG_ERR_INVALID, "null handle");
+    const uint32_t want = reference_particle_count(s->p);
+    if (want != s->n)
+        return fail(s, CMAG_ERR_STATE, "instance holds " + std::to_string(s->n) +
+                                           " particles, the reference scene has " +
+                                           std::to_string(want));
+    std::vector<float> pos((size_t)s->n * 4, 0.0f), zero((size_t)s->n * 4, 0.0f),
+        meas((size_t)s->n * 4, 0.0f);
+    reference_scene(s->p, pos.data(), s->n);
+    if (s->p.system != CMAG_PERISTALSIS)  // fluidSystem.cpp:131-132
+        for (uint32_t i = 0; i < s->n; ++i) meas[4 * (size_t)i] = s->p.rest_density;
+    int rc;
+    if ((rc = cmag_system_set_array(s, CMAG_POSITION, pos.data(), 0, s->n))) return rc;
+    const int zero_arrays[] = {CMAG_VELOCITY, CMAG_ACCELERATION, CMAG_VELOCITYLEAPFROG};
+    for (int a : zero_arrays)
+        if ((rc = cmag_system_set_array(s, a, zero.data(), 0, s->n))) return rc;
+    if ((rc = cmag_system_set_array(s, CMAG_MEASURES, meas.data(), 0, s->n))) return rc;
+    s->elapsed = 0.0f;
+    if (s->p.system == CMAG_DAMBREAK) {  // fluidSystem.cpp:378-379
+        const uint32_t gate_cells = (uint32_t)(s->p.boundary_offset + (int32_t)s->p.fluid_size[0]) * 2u;
+        s->p.right_boundary = s->p.world_origin[0] + gate_cells * s->p.particle_radius;
+    }
+    if (s->p.system == CMAG_PERISTALSIS) {  // PeristalsisSystem.cpp:213-236
+        for (int a : {CMAG_VISCOUSFORCE, CMAG_PRESSUREFORCE, CMAG_PREDICTEDPOSITION})
+            if ((rc = cmag_system_set_array(s, a, zero.data(), 0, s->n))) return rc;
+        s->host_phase = PhaseState{};
+        s->host_phase.time_relax = 1000 * s->p.delta_time;
+        s->host_phase.is_bc = 1;
+        s->p.is_boundary_configuration = 1;
+        s->p.particle_mass = s->p.rest_density / peristalsis_mass_sum(s->p, pos.data(), s->n);
+        if ((rc = upload_phase(s))) return rc;
+    }
+    invalidate_graph(s);
+    return CMAG_OK;
+}
+
+int cmag_dambreak3d_scene(cmag_system *s, const uint32_t tank_cells[3], uint32_t layers,
+                          float jitter_frac, uint64_t seed)
+{
+    if (!s || !tank_cells) return fail(s, CMAG_ERR_INVALID, "null argument");
+    if (s->p.system != CMAG_DAMBREAK) return fail(s, CMAG_ERR_STATE, "not a dam-break system");
+    const uint32_t want = dambreak3d_count(s->p.fluid_size, tank_cells, layers);
+    if (want != s->n)
+        return fail(s, CMAG_ERR_STATE, "instance holds " + std::to_string(s->n) +
+                                           " particles, the 3-D scene has " + std::to_string(want));
+    std::vector<float> pos((size_t)s->n * 4, 0.0f), zero((size_t)s->n * 4, 0.0f),
+        meas((size_t)s->n * 4, 0.0f);
+    dambreak3d_scene(s->p, tank_cells, layers, jitter_frac, seed, pos.data(), s->n);
+    for (uint32_t i = 0; i < s->n; ++i) meas[4 * (size_t)i] = s->p.rest_density;
+    int rc;
+    if ((rc = cmag_system_set_array(s, CMAG_POSITION, pos.data(), 0, s->n))) return rc;
+    for (int a : {CMAG_VELOCITY, CMAG_ACCELERATION, CMAG_VELOCITYLEAPFROG})
+        if ((rc = cmag_system_set_array(s, a, zero.data(), 0, s->n))) return rc;
+    if ((rc = cmag_system_set_array(s, CMAG_MEASURES, meas.data(), 0, s->n))) return rc;
+    s->elapsed = 0.0f;
+    invalidate_graph(s);
+    return CMAG_OK;
+}
+
+int cmag_system_update(cmag_system *s)
+{
+    if (!s) return fail(nullptr, CMAG_ERR_INVALID, "null handle");
+    return do_step(s);
+}
+
+int cmag_system_update_n(cmag_system *s, uint32_t steps)
+{
+    if (!s) return fail(nullptr, CMAG_ERR_INVALID, "null handle");
+    for (uint32_t k = 0; k < steps; ++k) {
+        int rc = do_step(s);
+        if (rc != CMAG_OK) return rc;
+    }
+    return CMAG_OK;
+}
+
+int cmag_system_timed_update(cmag_system *s, uint32_t steps, float *ms_out)
+{
+    if (!s || !ms_out) return fail(s, CMAG_ERR_INVALID, "null argument");
+    cudaEvent_t a, b;
+    CM_CUDA(s, cudaEventCreate(&a));
+    CM_CUDA(s, cudaEventCreate(&b));
+    cudaEventRecord(a, st_of(s));
+    int rc = CMAG_OK;
+    for (uint32_t k = 0; k < steps && rc == CMAG_OK; ++k) rc = do_step(s);
+    cudaEventRecord(b, st_of(s));
+    cudaError_t e = cudaEventSynchronize(b);
+    float ms = 0.0f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (rc != CMAG_OK) return rc;
+    if (e != cudaSuccess) return fail(s, CMAG_ERR_CUDA, std::string("timed update: ") + cudaGetErrorString(e));
+    *ms_out = ms;
+    return CMAG_OK;
+}
+
+int cmag_system_run_stages(cmag_system *s, int32_t last_stage)
+{
+    if (!s) return fail(nullptr, CMAG_ERR_INVALID, "null handle");
+    if (last_stage < CMAG_STAGE_HASH || last_stage > CMAG_STAGE_INTEGRATE)
+        return fail(s, CMAG_ERR_INVALID, "unknown stage");
+    int rc = record_step(s, last_stage, false);
+    if (rc != CMAG_OK) return rc;
+    s->last_stage = last_stage;
+    if (last_stage == CMAG_STAGE_INTEGRATE) {
+        advance_host_mirror(s);
+    } else if (s->p.system == CMAG_PERISTALSIS) {
+        // the stages ran with this step's phase; time does not advance
+        if ((rc = upload_phase(s))) return rc;
+    }
+    CM_CUDA(s, cudaStreamSynchronize(st_of(s)));
+    return CMAG_OK;
+}
+
+int cmag_system_num_particles(const cmag_system *s, uint32_t *out)
+{
+    if (!s || !out) return fail(nullptr, CMAG_ERR_INVALID, "null argument");
+    *out = s->n;
+    return CMAG_OK;
+}
+
+int cmag_system_num_grid_cells(const cmag_system *s, uint64_t *out)
+{
+    if (!s || !out) return fail(nullptr, CMAG_ERR_INVALID, "null argument");
+    *out = s->ncells;
+    return CMAG_OK;
+}
+
+int cmag_system_elapsed_time(const cmag_system *s, float *out)
+{
+    if (!s || !out) return fail(nullptr, CMAG_ERR_INVALID, "null argument");
+    *out = s->elapsed;
+    return CMAG_OK;
+}
+
+int cmag_system_get_params(const cmag_system *s, cmag_sph_params *out)
+{
+    if (!s || !out) return fail(nullptr, CMAG_ERR_INVALID, "null argument");
+    *out = s->p;
+    return CMAG_OK;
+}
+
+int cmag_system_set_params(cmag_system *s, const cmag_sph_params *p)
+{
+    if (!s || !p) return fail(s, CMAG_ERR_INVALID, "null argument");
+    if (p->system != s->p.system || std::memcmp(p->grid_size, s->p.grid_size, sizeof(p->grid_size)))
+        return fail(s, CMAG_ERR_INVALID, "system kind and grid size are fixed at creation");
+    std::string why;
+    if (validate(*p, s->n, why)) return fail(s, CMAG_ERR_INVALID, why);
+    s->p = *p;
+    if (s->p.system == CMAG_PERISTALSIS && s->host_phase.is_bc != p->is_boundary_configuration) {
+        s->host_phase.is_bc = p->is_boundary_configuration;
+        int rc = upload_phase(s);
+        if (rc) return rc;
+    }
+    refresh_layout(s);
+    invalidate_graph(s);
+    return CMAG_OK;
+}
+
+int cmag_dambreak_change_right_boundary(cmag_system *s)
+{
+    if (!s) return fail(nullptr, CMAG_ERR_INVALID, "null handle");
+    if (s->p.system != CMAG_DAMBREAK) return fail(s, CMAG_ERR_STATE, "not a dam-break system");
+    const float width = s->p.fluid_size[0] * 2 * s->p.particle_radius;
+    s->p.right_boundary += width;  // fluidSystem.cpp:240
+    launch_gate(make_dev(s), s->pos, 0, width, 0.0f, 0.0f, st_of(s));
+    CM_CUDA(s, cudaGetLastError());
+    invalidate_graph(s);
+    return CMAG_OK;
+}
+
+int cmag_dambreak_remove_right_boundary(cmag_system *s)
+{
+    if (!s) return fail(nullptr, CMAG_ERR_INVALID, "null handle");
+    if (s->p.system != CMAG_DAMBREAK) return fail(s, CMAG_ERR_STATE, "not a dam-break system");
+    s->p.right_boundary = (float)0xffffffffu;  // fluidSystem.cpp:223
+    const float fw = s->p.fluid_size[0] * 2 * s->p.particle_radius;
+    const float fh = s->p.grid_size[1] * 2 * s->p.particle_radius;
+    launch_gate(make_dev(s), s->pos, 1, 0.0f, fw, fh, st_of(s));
+    CM_CUDA(s, cudaGetLastError());
+    s->elapsed = 0.0f;
+    invalidate_graph(s);
+    return CMAG_OK;
+}
+
+int cmag_poiseuille_change_gravity(cmag_system *s)
+{
+    if (!s) return fail(nullptr, CMAG_ERR_INVALID, "null handle");
+    if (s->p.system != CMAG_POISEUILLE) return fail(s, CMAG_ERR_STATE, "not a Poiseuille system");
+    s->p.gravity[1] *= -1.0f;
+    invalidate_graph(s);
+    return CMAG_OK;
+}
+
+int cmag_peristalsis_phase(const cmag_system *s, float *wave_height, float *time_relax,
+                           float *time_shift, int32_t *is_bc)
+{
+    if (!s) return fail(nullptr, CMAG_ERR_INVALID, "null handle");
+    if (wave_height) *wave_height = s->host_phase.wave_height;
+    if (time_relax) *time_relax = s->host_phase.time_relax;
+    if (time_shift) *time_shift = s->host_phase.time_shift;
+    if (is_bc) *is_bc = s->host_phase.is_bc;
+    return CMAG_OK;
+}
+
+int cmag_system_set_elapsed_time(cmag_system *s, float elapsed)
+{
+    if (!s) return fail(nullptr, CMAG_ERR_INVALID, "null handle");
+    s->elapsed = elapsed;
+    if (s->p.system == CMAG_PERISTALSIS) {
+        s->host_phase.elapsed = elapsed;
+        return upload_phase(s);
+    }
+    return CMAG_OK;
+}
+
+int cmag_peristalsis_set_phase(cmag_system *s, float wave_height, float time_relax,
+                               float time_shift, int32_t is_bc)
+{
+    if (!s) return fail(nullptr, CMAG_ERR_INVALID, "null handle");
+    if (s->p.system != CMAG_PERISTALSIS) return fail(s, CMAG_ERR_STATE, "not a Peristalsis system");
+    s->host_phase.wave_height = wave_height;
+    s->host_phase.time_relax = time_relax;
+    s->host_phase.time_shift = time_shift;
+    s->host_phase.is_bc = is_bc;
+    s->p.is_boundary_configuration = is_bc;
+    return upload_phase(s);
+}
+
+int cmag_system_set_stream(cmag_system *s, void *cuda_stream)
+{
+    if (!s) return fail(nullptr, CMAG_ERR_INVALID, "null handle");
+    cudaStreamSynchronize(s->stream);
+    s->stream = cuda_stream ? (cudaStream_t)cuda_stream : s->own_stream;
+    s->user_stream = cuda_stream != nullptr;
+    invalidate_graph(s);
+    return CMAG_OK;
+}
+
+void *cmag_system_stream(const cmag_system *s) { return s ? (void *)s->stream : nullptr; }
+
+int cmag_system_set_graphs(cmag_system *s, int32_t enable)
+{
+    if (!s) return fail(nullptr, CMAG_ERR_INVALID, "null handle");
+    s->use_graphs = enable != 0;
+    invalidate_graph(s);
+    return CMAG_OK;
+}
+
+int cmag_system_device_error_bits(cmag_system *s, uint32_t *bits)
+{
+    if (!s || !bits) return fail(s, CMAG_ERR_INVALID, "null argument");
+    CM_CUDA(s, cudaStreamSynchronize(s->stream));
+    CM_CUDA(s, cudaMemcpy(bits, s->err, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    return CMAG_OK;
+}
+
+int cmag_system_synchronize(cmag_system *s)
+{
+    if (!s) return fail(nullptr, CMAG_ERR_INVALID, "null handle");
+    uint32_t bits = 0;
+    int rc = cmag_system_device_error_bits(s, &bits);
+    if (rc) return rc;
+    if (bits) {
+        std::string m = "device check failed:";
+        if (bits & CMAG_DEVERR_LOOKBACK_TIMEOUT) m += " look-back spin limit reached;";
+        if (bits & CMAG_DEVERR_RANGE) m += " particle hash outside the scanned cell range;";
+        return fail(s, CMAG_ERR_DEVICE, m);
+    }
+    return CMAG_OK;
+}
+
+int cmag_system_set_stage_timing(cmag_system *s, int32_t enable)
+{
+    if (!s) return fail(nullptr, CMAG_ERR_INVALID, "null handle");
+    s->timing = enable != 0;
+    return CMAG_OK;
+}
+
+int cmag_system_stage_times(cmag_system *s, float ms_out[6], uint32_t *steps_out)
+{
+    if (!s) return fail(nullptr, CMAG_ERR_INVALID, "null handle");
+    CM_CUDA(s, cudaStreamSynchronize(s->stream));
+    for (size_t b = 0; b + 7 <= s->events_used; b += 7)
+        for (int k = 0; k < 6; ++k) {
+            float ms = 0.0f;
+            CM_CUDA(s, cudaEventElapsedTime(&ms, s->events[b + k], s->events[b + k + 1]));
+            s->stage_ms[k] += ms;
+        }
+    s->events_used = 0;
+    if (ms_out)
+        for (int k = 0; k < 6; ++k) ms_out[k] = (float)s->stage_ms[k];
+    if (steps_out) *steps_out = s->timed_steps;
+    for (int k = 0; k < 6; ++k) s->stage_ms[k] = 0;
+    s->timed_steps = 0;
+    return CMAG_OK;
+}
+
+// ---------------------------------------------------------------- sorting --
+
+namespace {
+struct SortCache {
+    uint32_t *ws = nullptr, *keys = nullptr, *vals = nullptr;
+    size_t ws_words = 0, cap = 0;
+};
+std::mutex g_sort_mu;
+std::map<int, SortCache> g_sort_cache;
+}  // namespace
+
+int cmag_sort_particles(uint32_t *d_hash, uint32_t *d_index, uint32_t n, uint32_t key_bits,
+                        void *cuda_stream)
+{
+    if (n == 0) return CMAG_OK;
+    if (!d_hash || !d_index) return fail(nullptr, CMAG_ERR_INVALID, "null argument");
+    if (key_bits > 32 || n >= (1u << 30)) return fail(nullptr, CMAG_ERR_INVALID, "key_bits or n out of range");
+    cudaStream_t st = (cudaStream_t)cuda_stream;
+    int passes = sort_passes(key_bits);
+    if (passes < 1) passes = 1;
+    int dev = 0;
+    CM_CUDA(nullptr, cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(g_sort_mu);
+    SortCache &c = g_sort_cache[dev];
+    const size_t words = sort_workspace_words(n, kMaxPasses) + 1;
+    if (c.cap < n || c.ws_words < words) {
+        if (c.ws) cudaFree(c.ws);
+        if (c.keys) cudaFree(c.keys);
+        if (c.vals) cudaFree(c.vals);
+        c = SortCache{};
+        CM_CUDA(nullptr, cudaMalloc((void **)&c.ws, words * sizeof(uint32_t)));
+        CM_CUDA(nullptr, cudaMalloc((void **)&c.keys, sizeof(uint32_t) * (size_t)n));
+        CM_CUDA(nullptr, cudaMalloc((void **)&c.vals, sizeof(uint32_t) * (size_t)n));
+        c.ws_words = words;
+        c.cap = n;
+    }
+    uint32_t *err = c.ws + (words - 1);
+    CM_CUDA(nullptr, cudaMemsetAsync(c.ws, 0, words * sizeof(uint32_t), st));
+    SortWorkspace sw = sort_workspace_view(c.ws, n);
+    launch_digit_hist(d_hash, n, passes, sw.hist, st);
+    uint32_t *kb[2] = {d_hash, c.keys}, *vb[2] = {d_index, c.vals};
+    for (int k = 0; k < passes; ++k) {
+        const int src = k & 1, dst = src ^ 1;
+        launch_onesweep_pass(kb[src], vb[src], kb[dst], vb[dst], n, k, false, sw, err, st);
+    }
+    if (passes & 1) {
+        CM_CUDA(nullptr, cudaMemcpyAsync(d_hash, c.keys, sizeof(uint32_t) * (size_t)n,
+                                         cudaMemcpyDeviceToDevice, st));
+        CM_CUDA(nullptr, cudaMemcpyAsync(d_index, c.vals, sizeof(uint32_t) * (size_t)n,
+                                         cudaMemcpyDeviceToDevice, st));
+    }
+    uint32_t bits = 0;
+    CM_CUDA(nullptr, cudaMemcpyAsync(&bits, err, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    CM_CUDA(nullptr, cudaStreamSynchronize(st));
+    if (bits) return fail(nullptr, CMAG_ERR_DEVICE, "sort look-back spin limit reached");
+    return CMAG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,313 @@
+/*
+ * cmag_sph.h -- C ABI of the GB300-native weakly-compressible SPH time step.
+ *
+ * This is the drop-in boundary for cmag's three 2-D particle solvers (DamBreak,
+ * Poiseuille, Peristalsis).  In the reference each solver is a C++ class over an
+ * extern "C" launcher layer that keeps its parameters in one global __constant__
+ * block per library:
+ *
+ *   DamBreak     DamBreak.Core/fluidSystem.h:6-113     launchers fluidSystem.cuh:4-71
+ *   Poiseuille   Poiseuille.Core/poiseuilleFlowSystem.h:6-112
+ *                                                      launchers poiseuilleFlowSystem.cuh:4-67
+ *   Peristalsis  Peristalsis.Core/PeristalsisSystem.h:6-132
+ *                                                      launchers PeristalsisSystem.cuh:4-95
+ *
+ * Here every solver instance is an opaque handle with its own parameter block,
+ * device buffers and CUDA stream, so any number of instances of any system can
+ * live in one process (the reference's three libraries export clashing names and
+ * one parameter block each).  All entry points take plain pointers and sizes,
+ * return an int status (CMAG_OK == 0) and never exit the process; the text of the
+ * last failure is available from cmag_system_last_error() / cmag_last_error().
+ *
+ * Array meaning and order follow the reference exactly: positions, velocities,
+ * leap-frog velocities, accelerations and forces are in ORIGINAL particle order;
+ * measures (x = density, y = pressure), the sorted hash/index pair and the
+ * sorted position/velocity copies are in SORTED (cell) order.
+ *
+ * The C++ classes in include/cmag/systems.hpp mirror the reference class API on
+ * top of these entry points.
+ */
+#ifndef CMAG_SPH_H
+#define CMAG_SPH_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------- */
+enum cmag_status {
+    CMAG_OK = 0,
+    CMAG_ERR_INVALID = 1,  /* bad argument or parameter block                  */
+    CMAG_ERR_CUDA = 2,     /* a CUDA runtime call failed (message has the name) */
+    CMAG_ERR_NOMEM = 3,    /* device or host allocation failed                  */
+    CMAG_ERR_DEVICE = 4,   /* a kernel reported a failed device-side check      */
+    CMAG_ERR_STATE = 5     /* call not valid in the current state               */
+};
+
+/* device-side check bits, reported by cmag_system_synchronize() */
+enum cmag_device_error {
+    CMAG_DEVERR_LOOKBACK_TIMEOUT = 1, /* a sort/scan look-back wait hit its spin limit */
+    CMAG_DEVERR_RANGE = 2             /* an index left its buffer; access skipped       */
+};
+
+/* ---- solver families ---------------------------------------------------- */
+enum cmag_system_kind {
+    CMAG_DAMBREAK = 0,    /* DamBreak.Core/fluid_kernel.cu                     */
+    CMAG_POISEUILLE = 1,  /* Poiseuille.Core/poiseuilleFlowKernel.cu           */
+    CMAG_PERISTALSIS = 2  /* Peristalsis.Core/Peristalsis{Density,...}.cu      */
+};
+
+/* smoothing kernel; the reference uses the Wendland C2 function everywhere
+ * (fluid_kernel.cu:121,222) with the 2-D normalisation 7/(4 pi h^2) */
+enum cmag_kernel_fn {
+    CMAG_KERNEL_WENDLAND = 0,
+    CMAG_KERNEL_CUBIC_SPLINE = 1
+};
+
+/* equation of state */
+enum cmag_eos {
+    CMAG_EOS_REFERENCE = 0, /* per family: DamBreak Tait (fluid_kernel.cu:168),
+                               Poiseuille p = c^2 rho (poiseuilleFlowKernel.cu:181),
+                               Peristalsis p = 50 c rho (PeristalsisDensity.cu:75)  */
+    CMAG_EOS_TAIT = 1       /* p = B((rho/rho0)^gamma - 1) for any family        */
+};
+
+/* DamBreak particle types, DamBreak.Core/fluid_kernel.cuh:16-23 */
+enum cmag_dambreak_type {
+    CMAG_RIGHT_FIRST_TYPE = 0,
+    CMAG_FIRST_TYPE = 1,
+    CMAG_RIGHT_SECOND_TYPE = 2,
+    CMAG_SECOND_TYPE = 3,
+    CMAG_FLUID = 4
+};
+
+/* ---- particle arrays (setArray / getArray selectors) -------------------- */
+enum cmag_array {
+    /* float4 arrays */
+    CMAG_POSITION = 0,          /* original order; .w = particle type           */
+    CMAG_VELOCITY = 1,          /* original order                               */
+    CMAG_MEASURES = 2,          /* SORTED order: x density, y pressure          */
+    CMAG_ACCELERATION = 3,      /* original order (DamBreak, Poiseuille)        */
+    CMAG_VELOCITYLEAPFROG = 4,  /* original order: 0.5 (v_n + v_n+1)            */
+    CMAG_VISCOUSFORCE = 5,      /* original order (Peristalsis)                 */
+    CMAG_PRESSUREFORCE = 6,     /* original order (Peristalsis)                 */
+    CMAG_PREDICTEDPOSITION = 7, /* Peristalsis; allocated, never advanced (the
+                                   reference's predictor is dead code)          */
+    CMAG_SORTEDPOSITION = 8,    /* sorted order                                 */
+    CMAG_SORTEDVELOCITY = 9,    /* sorted order (copy of leap-frog velocity)    */
+    /* uint32 arrays (cmag_system_get_uint_array only) */
+    CMAG_HASH = 16,             /* sorted cell hash                             */
+    CMAG_INDEX = 17,            /* sorted -> original particle index            */
+    CMAG_CELLSTART = 18,        /* numGridCells; 0xffffffff for empty cells     */
+    CMAG_CELLEND = 19,          /* numGridCells; defined for occupied cells     */
+    CMAG_CELLOFFSET = 20        /* numGridCells + 1: first sorted particle with
+                                   hash >= cell (dense form used by the kernels) */
+};
+
+/* ---- parameter block ---------------------------------------------------- */
+/* Superset of SimParams (DamBreak.Core/fluid_kernel.cuh:25-51), PoiseuilleParams
+ * (Poiseuille.Core/poiseuilleFlowKernel.cuh:16-35) and Peristalsiscfg
+ * (Peristalsis.Core/PeristalsisKernel.cuh:22-63), plus the options that the
+ * reference hard-codes.  The *_default_params() functions fill it exactly as the
+ * reference constructors do. */
+typedef struct cmag_sph_params {
+    int32_t system;              /* enum cmag_system_kind                           */
+    uint32_t grid_size[3];       /* cells per axis, each a power of two             */
+    float world_origin[3];
+    float cell_size[3];
+    uint32_t fluid_size[3];      /* fluid lattice dimensions                        */
+    int32_t cell_count;          /* neighbour cells searched each side (3)          */
+    float world_size[3];         /* periodic image shift (Peristalsis)              */
+
+    float gravity[3];
+    float particle_radius;
+    float smoothing_radius;      /* h */
+    float particle_mass;
+    float rest_density;
+    float soundspeed;
+    float B;                     /* Tait coefficient                                */
+    float gamma;                 /* Tait exponent                                   */
+    float delta_time;
+    float boundary_damping;
+    float mu;                    /* dynamic viscosity (Poiseuille, Peristalsis)     */
+    int32_t boundary_offset;
+    float right_boundary;        /* DamBreak gate clamp                             */
+    float lj_D;                  /* DamBreak wall force strength D                  */
+    float lj_a;                  /* DamBreak wall force length a                    */
+
+    float amplitude;             /* Peristalsis wall wave amplitude                 */
+    float wave_speed;
+    float wave_count;            /* wavelengths per domain length (reference: 1)    */
+    int32_t is_boundary_configuration;
+
+    /* options the reference hard-codes; defaults reproduce the reference */
+    int32_t dims;                /* 2: kernel normalised in 2-D (reference); 3: 3-D  */
+    int32_t kernel;              /* enum cmag_kernel_fn                              */
+    int32_t eos;                 /* enum cmag_eos                                    */
+    float av_alpha;              /* DamBreak artificial viscosity (reference 0.38)   */
+    int32_t lj_cutoff;           /* 0: wall force from every wall particle in the
+                                    searched cell box (reference); 1: only q < 2     */
+    int32_t clamp_z;             /* DamBreak: 1 also clamps z to [z_min_border,
+                                    z_max_border] like the x/y clamps (3-D tanks)   */
+    float z_min_border;
+    float z_max_border;
+    int32_t reserved[5];
+} cmag_sph_params;
+
+/* Reference-constructor parameter derivations.
+ * DamBreakSystem::DamBreakSystem        DamBreak.Core/fluidSystem.cpp:17-77
+ * PoiseuilleFlowSystem::PoiseuilleFlowSystem  Poiseuille.Core/poiseuilleFlowSystem.cpp:21-67
+ * PeristalsisSystem::PeristalsisSystem  Peristalsis.Core/PeristalsisSystem.cpp:17-80 */
+int cmag_dambreak_default_params(const uint32_t fluid_size[3], int32_t boundary_offset,
+                                 const uint32_t grid_size[3], float particle_radius,
+                                 cmag_sph_params *out);
+int cmag_poiseuille_default_params(const uint32_t fluid_size[3], int32_t boundary_offset,
+                                   const uint32_t grid_size[3], float particle_radius,
+                                   cmag_sph_params *out);
+int cmag_peristalsis_default_params(float delta_time, const uint32_t fluid_size[3],
+                                    float amplitude, float wave_speed, float soundspeed,
+                                    const float gravity[3], int32_t boundary_offset,
+                                    const uint32_t grid_size[3], float radius,
+                                    cmag_sph_params *out);
+
+/* Number of particles a family's reference scene generator creates
+ * (fluidSystem.cpp:34-37, poiseuilleFlowSystem.cpp:35-36, PeristalsisSystem.cpp:23-24). */
+int cmag_reference_particle_count(const cmag_sph_params *p, uint32_t *out);
+
+/* Host-side scene generators (no device needed): fill pos[4*n] with the
+ * reference scene of p (initFluid + initBoundaryParticles, fluidSystem.cpp:382-523,
+ * poiseuilleFlowSystem.cpp:325-383, PeristalsisSystem.cpp:255-317), and the
+ * Peristalsis lattice kernel sum whose inverse sets the particle mass
+ * (CalculateMass, PeristalsisSystem.cpp:238-253). */
+int cmag_reference_scene(const cmag_sph_params *p, float *pos, uint32_t n);
+int cmag_peristalsis_mass_sum(const cmag_sph_params *p, const float *pos, uint32_t n,
+                              float *out);
+int cmag_dambreak3d_scene_host(const cmag_sph_params *p, const uint32_t tank_cells[3],
+                               uint32_t layers, float jitter_frac, uint64_t seed, float *pos,
+                               uint32_t n);
+
+/* ---- solver instances --------------------------------------------------- */
+typedef struct cmag_system cmag_system;
+
+/* Allocate a solver for num_particles particles on the current CUDA device
+ * (replaces the constructors' _initialize, fluidSystem.cpp:116-190). */
+int cmag_system_create(const cmag_sph_params *params, uint32_t num_particles,
+                       cmag_system **out);
+int cmag_system_destroy(cmag_system *s);
+
+/* Fill the reference scene (reset/Reset: fluidSystem.cpp:361-380,
+ * poiseuilleFlowSystem.cpp:311-323, PeristalsisSystem.cpp:213-236).  For
+ * Peristalsis this also sets the particle mass from the lattice sum
+ * (PeristalsisSystem.cpp:238-253). */
+int cmag_system_reset(cmag_system *s);
+
+/* Build a 3-D dam break: fluid block fx*fy*fz on a lattice of spacing
+ * 2*particle_radius with uniform jitter of +-jitter_frac*spacing (seeded), in a
+ * tank of tank_cells[3] lattice cells with `layers` wall layers on the floor and
+ * the four sides.  Particle mass = rest_density * spacing^3.  Extension beyond the
+ * reference (which is 2-D only). */
+int cmag_dambreak3d_scene(cmag_system *s, const uint32_t tank_cells[3], uint32_t layers,
+                          float jitter_frac, uint64_t seed);
+/* particles cmag_dambreak3d_scene creates for the given sizes */
+int cmag_dambreak3d_particle_count(const uint32_t fluid_size[3], const uint32_t tank_cells[3],
+                                   uint32_t layers, uint32_t *out);
+
+/* One time step (update/Update: fluidSystem.cpp:257-319,
+ * poiseuilleFlowSystem.cpp:212-270, PeristalsisSystem.cpp:320-407). */
+int cmag_system_update(cmag_system *s);
+/* Run `steps` time steps back to back (replayed as one captured CUDA graph per
+ * step when graphs are enabled). */
+int cmag_system_update_n(cmag_system *s, uint32_t steps);
+
+/* Run `steps` steps between two CUDA events recorded on the instance's stream,
+ * synchronize, and return the elapsed device time in milliseconds (benchmarks). */
+int cmag_system_timed_update(cmag_system *s, uint32_t steps, float *ms_out);
+
+/* Stage-by-stage execution for parity tests: run the stages of one step up to
+ * and including `last_stage` without advancing time (CMAG_STAGE_INTEGRATE runs
+ * a full step and does advance time). */
+enum cmag_stage {
+    CMAG_STAGE_HASH = 0,
+    CMAG_STAGE_SORT = 1,
+    CMAG_STAGE_REORDER = 2,
+    CMAG_STAGE_DENSITY = 3,
+    CMAG_STAGE_FORCE = 4,
+    CMAG_STAGE_INTEGRATE = 5
+};
+int cmag_system_run_stages(cmag_system *s, int32_t last_stage);
+
+/* setArray (fluidSystem.cpp:321-355): copy `count` float4 elements starting at
+ * element `start` from host memory.  getArray is its inverse. */
+int cmag_system_set_array(cmag_system *s, int32_t array, const float *host, uint32_t start,
+                          uint32_t count);
+int cmag_system_get_array(cmag_system *s, int32_t array, float *host, uint32_t start,
+                          uint32_t count);
+int cmag_system_get_uint_array(cmag_system *s, int32_t array, uint32_t *host, uint32_t start,
+                               uint32_t count);
+/* Borrowed device pointer of an array (getCudaPosVBO, getCudaMeasures, ...);
+ * valid until destroy.  NULL for unknown arrays. */
+void *cmag_system_device_array(cmag_system *s, int32_t array);
+
+int cmag_system_num_particles(const cmag_system *s, uint32_t *out);
+int cmag_system_num_grid_cells(const cmag_system *s, uint64_t *out);
+int cmag_system_elapsed_time(const cmag_system *s, float *out);
+int cmag_system_get_params(const cmag_system *s, cmag_sph_params *out);
+/* Replace the parameter block (system kind and grid must not change). */
+int cmag_system_set_params(cmag_system *s, const cmag_sph_params *p);
+
+/* DamBreakSystem::changeRightBoundary / removeRightBoundary
+ * (fluidSystem.cpp:222-255). */
+int cmag_dambreak_change_right_boundary(cmag_system *s);
+int cmag_dambreak_remove_right_boundary(cmag_system *s);
+/* PoiseuilleFlowSystem::changeGravity (poiseuilleFlowSystem.cpp:207-210). */
+int cmag_poiseuille_change_gravity(cmag_system *s);
+/* Peristalsis host-side phase state: current wave height, relax time left,
+ * time shift and the boundary-configuration flag (PeristalsisSystem.cpp:330-343). */
+int cmag_peristalsis_phase(const cmag_system *s, float *current_wave_height,
+                           float *time_relax, float *time_shift, int32_t *is_boundary_configuration);
+/* Restore the host-side time state (checkpoint/resume; no reference counterpart:
+ * the reference keeps elapsedTime and the phase private). */
+int cmag_system_set_elapsed_time(cmag_system *s, float elapsed);
+int cmag_peristalsis_set_phase(cmag_system *s, float current_wave_height, float time_relax,
+                               float time_shift, int32_t is_boundary_configuration);
+
+/* Use a caller-owned cudaStream_t (NULL = the instance's own stream). */
+int cmag_system_set_stream(cmag_system *s, void *cuda_stream);
+void *cmag_system_stream(const cmag_system *s);
+/* 1: capture each step as a CUDA graph and replay it (default); 0: plain launches. */
+int cmag_system_set_graphs(cmag_system *s, int32_t enable);
+/* Wait for the instance's stream and report device-side check failures
+ * (CMAG_ERR_DEVICE with the cmag_device_error bits in the message). */
+int cmag_system_synchronize(cmag_system *s);
+int cmag_system_device_error_bits(cmag_system *s, uint32_t *bits);
+
+/* Per-stage timing: when enabled, every step records CUDA events around each
+ * stage on the instance's stream; read back the accumulated milliseconds per stage
+ * (6 entries, enum cmag_stage order) and the number of timed steps. */
+int cmag_system_set_stage_timing(cmag_system *s, int32_t enable);
+int cmag_system_stage_times(cmag_system *s, float ms_out[6], uint32_t *steps_out);
+
+const char *cmag_system_last_error(const cmag_system *s);
+/* thread-local message of the last failed call that had no handle */
+const char *cmag_last_error(void);
+
+/* ---- launcher-level entry points ---------------------------------------- */
+/* sortParticles (fluidSystem.cu:94-99, poiseuilleFlowSystem.cu:103-108,
+ * PeristalsisSystem.cu:116-121): stable ascending sort of the (hash, index) pairs
+ * in place on the device, keys below 2^key_bits.  Replaces thrust::sort_by_key
+ * with a onesweep LSD radix sort (8-bit digits).  Scratch memory is allocated on
+ * the first call and cached per device (grown when a larger n arrives). */
+int cmag_sort_particles(uint32_t *d_hash, uint32_t *d_index, uint32_t n, uint32_t key_bits,
+                        void *cuda_stream);
+
+/* Library version string. */
+const char *cmag_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CMAG_SPH_H */

@@ -1,0 +1,33 @@
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (sm_103a)")
+
+
+@pytest.fixture(scope="session")
+def built():
+    """Build the CUDA library and the oracle if they are missing."""
+    from cmag_gb300 import build as B
+    from oracle import oracle as O
+    if not os.path.exists(B.LIB):
+        B.build()
+    if not os.path.exists(O.LIB_PATH):
+        O.build()
+    return True
+
+
+@pytest.fixture(scope="session")
+def gpu(built):
+    import torch
+    if not torch.cuda.is_available():
+        pytest.fail("CUDA device required for -m gpu tests")
+    torch.cuda.init()
+    return True
