@@ -180,13 +180,8 @@ def dist_init(n_gpus):
 
 
 def barrier_max(dist, value):
-    if dist is None:
-        return value
-    import torch
-    t = torch.tensor([value], dtype=torch.float64, device="cuda")
-    dist.barrier()
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
+    from cmag_gb300.replicas import aggregate
+    return aggregate(dist, value, 0.0, device="cuda")[0]
 
 
 def run_reference(args):
@@ -199,22 +194,27 @@ def run_reference(args):
     _, p, n, fluid, cfg = make_workload_cpu(args.workload)
     threads = os.cpu_count() or 1
     st = oracle_state_for(args.workload, p, n)
+    t0 = time.perf_counter()
     for _ in range(args.warmup):
         st.step(threads=threads)
+    per_step = (time.perf_counter() - t0) / max(args.warmup, 1)
+    # bounded sample: at most ~150 s of timed CPU work
+    steps = max(1, min(args.steps, int(150.0 / max(per_step, 1e-6))))
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(steps):
         st.step(threads=threads)
     secs = time.perf_counter() - t0
-    value = fluid * args.steps / secs
+    value = fluid * steps / secs
     line = {"metric": METRIC, "value": value, "unit": "particle-updates/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": secs * 1e3 / args.steps,
+            "steps": steps, "warmup": args.warmup, "ms_per_step": secs * 1e3 / steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "config": cfg, "impl": "reference",
             "cpu_baseline": {"value": value, "unit": "particle-updates/s", "cores": threads,
                              "kind": "port",
-                             "sample": "%d full steps of the %d-particle scene (oracle restatement "
-                                       "of the reference kernels; the reference itself is CUDA-only "
-                                       "and its host classes need OpenGL)" % (args.steps, n)},
+                             "sample": "%d full steps of the %d-particle scene (of %d requested; "
+                                       "oracle restatement of the reference kernels; the reference "
+                                       "itself is CUDA-only and its host classes need OpenGL)"
+                                       % (steps, n, args.steps)},
             "e2e": {"value": value, "unit": "particle-updates/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line))

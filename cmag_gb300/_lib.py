@@ -20,6 +20,7 @@ c_sys = ctypes.c_void_p
 # every symbol the header declares, with its ctypes signature
 SIGNATURES = {
     "cmag_version": ([], ctypes.c_char_p),
+    "cmag_sph_params_size": ([], ctypes.c_size_t),
     "cmag_last_error": ([], ctypes.c_char_p),
     "cmag_system_last_error": ([c_sys], ctypes.c_char_p),
     "cmag_dambreak_default_params": ([c_u32p, ctypes.c_int32, c_u32p, ctypes.c_float, P(SphParams)], ctypes.c_int),

@@ -53,5 +53,19 @@ def build(verbose=False, extra=()):
     return LIB
 
 
+def stale():
+    """True when the library is missing or older than any source or header."""
+    if not os.path.exists(LIB):
+        return True
+    t = os.path.getmtime(LIB)
+    deps = [os.path.join(SRC, f) for f in os.listdir(SRC)]
+    deps.append(os.path.join(os.path.dirname(PKG), "include", "cmag_sph.h"))
+    return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
+
+
+def build_if_stale():
+    return build() if stale() else LIB
+
+
 if __name__ == "__main__":
     print(build(verbose="-v" in sys.argv, extra=["-Xptxas", "-v"] if "--ptxas" in sys.argv else ()))

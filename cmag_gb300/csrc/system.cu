@@ -420,6 +420,8 @@ extern "C" {
 
 const char *cmag_version(void) { return "cmag_gb300 0.1 (sm_103a)"; }
 
+size_t cmag_sph_params_size(void) { return sizeof(cmag_sph_params); }
+
 const char *cmag_last_error(void) { return g_last_error.c_str(); }
 
 const char *cmag_system_last_error(const cmag_system *s)

@@ -305,6 +305,8 @@ int cmag_sort_particles(uint32_t *d_hash, uint32_t *d_index, uint32_t n, uint32_
 
 /* Library version string. */
 const char *cmag_version(void);
+/* sizeof(cmag_sph_params) as compiled into the library (for FFI layout checks). */
+size_t cmag_sph_params_size(void);
 
 #ifdef __cplusplus
 }

@@ -617,10 +617,15 @@ static f3 poiseuille_vab(const cmag_sph_params *p, f3 vi, f3 pi, f3 vj, f3 pj, f
 
 /* Force on sorted particle i.  Returns 0 when the reference writes nothing for i
  * (DamBreak non-fluid particles, fluid_kernel.cu:258). */
+/* |t| summed component-wise over the pair terms: the scale of the rounding error
+ * of any summation order of those terms */
+static f3 abs3(f3 a) { return mk3(fabsf(a.x), fabsf(a.y), fabsf(a.z)); }
+
 static int force_one(const cmag_sph_params *p, const float *spos, const float *svel,
                      const float *meas, const uint32_t *cs, const uint32_t *ce, uint32_t i,
-                     f3 *fa, f3 *fb)
+                     f3 *fa, f3 *fb, f3 *sa, f3 *sb)
 {
+    f3 scA = mk3(0, 0, 0), scB = mk3(0, 0, 0);
     f3 pi = ld3(spos, i);
     float wi = spos[4 * (size_t)i + 3];
     if (p->system == CMAG_DAMBREAK && wi != (float)CMAG_FLUID) return 0;
@@ -650,7 +655,9 @@ static int force_one(const cmag_sph_params *p, const float *spos, const float *s
                             if (wj != (float)CMAG_FLUID) { /* Lennard-Jones wall, fluid_kernel.cu:199-207 */
                                 if (p->lj_cutoff && !(q < 2)) continue;
                                 float s = p->lj_D * (powf(p->lj_a / dist, 12) - powf(p->lj_a / dist, 6));
-                                tA = add3(tA, divs3(smul3(s, rp), powf(dist, 2)));
+                                f3 term = divs3(smul3(s, rp), powf(dist, 2));
+                                tA = add3(tA, term);
+                                scA = add3(scA, abs3(term));
                                 continue;
                             }
                             if (q < 2) { /* fluid_kernel.cu:221-237 */
@@ -664,7 +671,9 @@ static int force_one(const cmag_sph_params *p, const float *spos, const float *s
                                     art = -1.0f * nu * vij_pij / (dot3(rp, rp) + 0.001f * powf(h, 2));
                                 }
                                 float s = -1.0f * m * (pr / powf(rho, 2) + pr2 / powf(rho2, 2) + art);
-                                tA = add3(tA, muls3(smul3(s, normalize3(rp)), temp));
+                                f3 term = muls3(smul3(s, normalize3(rp)), temp);
+                                tA = add3(tA, term);
+                                scA = add3(scA, abs3(term));
                             }
                         } else if (p->system == CMAG_POISEUILLE) {
                             if (q < 2) { /* poiseuilleFlowKernel.cu:236-245 */
@@ -677,6 +686,7 @@ static int force_one(const cmag_sph_params *p, const float *spos, const float *s
                                 float s2 = m * (p->mu + p->mu);
                                 f3 t2 = muls3(divs3(muls3(divs3(smul3(s2, vab), rho * rho2), 1.0f), dist), temp);
                                 tA = add3(tA, add3(t1, t2));
+                                scA = add3(scA, add3(abs3(t1), abs3(t2)));
                             }
                         } else {
                             if (q < 2) {
@@ -686,10 +696,14 @@ static int force_one(const cmag_sph_params *p, const float *spos, const float *s
                                 /* viscous, PeristalsisViscousForce.cu:206-213 */
                                 f3 vab = sub3(vi, vj);
                                 float sv = m * temp * (p->mu + p->mu);
-                                tA = add3(tA, divs3(smul3(sv, vab), rho * rho2 * dist));
+                                f3 tv = divs3(smul3(sv, vab), rho * rho2 * dist);
+                                tA = add3(tA, tv);
+                                scA = add3(scA, abs3(tv));
                                 /* pressure, PeristalsisPressureForce.cu:39-43 */
                                 float sp = -1.0f * m * temp * (pr / powf(rho, 2) + pr2 / powf(rho2, 2));
-                                tB = add3(tB, smul3(sp, normalize3(rp)));
+                                f3 tp = smul3(sp, normalize3(rp));
+                                tB = add3(tB, tp);
+                                scB = add3(scB, abs3(tp));
                             }
                         }
                     }
@@ -699,6 +713,8 @@ static int force_one(const cmag_sph_params *p, const float *spos, const float *s
             }
     *fa = fA;
     *fb = fB;
+    if (sa) *sa = scA;
+    if (sb) *sb = scB;
     return 1;
 }
 
@@ -707,7 +723,7 @@ void orc_force_at(const cmag_sph_params *p, const float *spos, const float *svel
                   float out_a[3], float out_b[3], int32_t *written)
 {
     f3 a, b;
-    *written = force_one(p, spos, svel, meas, cs, ce, i, &a, &b);
+    *written = force_one(p, spos, svel, meas, cs, ce, i, &a, &b, NULL, NULL);
     if (!*written) { a = mk3(0, 0, 0); b = a; }
     out_a[0] = a.x; out_a[1] = a.y; out_a[2] = a.z;
     out_b[0] = b.x; out_b[1] = b.y; out_b[2] = b.z;
@@ -726,7 +742,7 @@ void orc_force(const cmag_sph_params *p, const float *spos, const float *svel, c
     for (long li = 0; li < (long)n; li++) {
         uint32_t i = (uint32_t)li;
         f3 a, b;
-        if (!force_one(p, spos, svel, meas, cs, ce, i, &a, &b)) continue;
+        if (!force_one(p, spos, svel, meas, cs, ce, i, &a, &b, NULL, NULL)) continue;
         size_t o = 4 * (size_t)idx[i];
         out_a[o] = a.x; out_a[o + 1] = a.y; out_a[o + 2] = a.z; out_a[o + 3] = 0.0f;
         if (p->system == CMAG_PERISTALSIS && out_b) {
@@ -880,4 +896,23 @@ void orc_step(cmag_sph_params *p, uint32_t n, uint64_t ncells, float *pos, float
     if (p->system == CMAG_PERISTALSIS) t = p->is_boundary_configuration ? 0 : phase[0] - phase[1];
     orc_integrate(p, pos, vel, vlf, acc, vforce, pforce, t, n);
     phase[0] += dt;
+}
+
+void orc_force_scale(const cmag_sph_params *p, const float *spos, const float *svel,
+                     const float *meas, const uint32_t *idx, const uint32_t *cs,
+                     const uint32_t *ce, float *scale_a, float *scale_b, uint32_t n, int threads)
+{
+    (void)threads;
+#pragma omp parallel for schedule(dynamic, 256) num_threads(threads > 0 ? threads : 1)
+    for (long li = 0; li < (long)n; li++) {
+        uint32_t i = (uint32_t)li;
+        f3 a, b, sa, sb;
+        size_t o = 4 * (size_t)idx[i];
+        if (!force_one(p, spos, svel, meas, cs, ce, i, &a, &b, &sa, &sb)) {
+            sa = mk3(0, 0, 0);
+            sb = sa;
+        }
+        scale_a[o] = sa.x; scale_a[o + 1] = sa.y; scale_a[o + 2] = sa.z; scale_a[o + 3] = 0;
+        if (scale_b) { scale_b[o] = sb.x; scale_b[o + 1] = sb.y; scale_b[o + 2] = sb.z; scale_b[o + 3] = 0; }
+    }
 }

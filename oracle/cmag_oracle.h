@@ -64,6 +64,12 @@ void orc_density(const cmag_sph_params *p, const float *spos, float *meas,
 void orc_force(const cmag_sph_params *p, const float *spos, const float *svel, const float *meas,
                const uint32_t *idx, const uint32_t *cell_start, const uint32_t *cell_end,
                float *out_a, float *out_b, uint32_t n, int threads);
+/* Per particle (original order), the component-wise sum of |pair term| of the
+ * force: the magnitude that bounds the rounding error of any summation order. */
+void orc_force_scale(const cmag_sph_params *p, const float *spos, const float *svel,
+                     const float *meas, const uint32_t *idx, const uint32_t *cell_start,
+                     const uint32_t *cell_end, float *scale_a, float *scale_b, uint32_t n,
+                     int threads);
 /* single-particle evaluations on given sorted arrays (spot checks at full size) */
 float orc_density_at(const cmag_sph_params *p, const float *spos, const uint32_t *cell_start,
                      const uint32_t *cell_end, uint32_t i);

@@ -78,6 +78,8 @@ def lib():
         L.orc_density.argtypes = [sp, c_f32p, c_f32p, c_u32p, c_u32p, ctypes.c_uint32, ctypes.c_int]
         L.orc_force.argtypes = [sp, c_f32p, c_f32p, c_f32p, c_u32p, c_u32p, c_u32p, c_f32p, c_f32p,
                                 ctypes.c_uint32, ctypes.c_int]
+        L.orc_force_scale.argtypes = [sp, c_f32p, c_f32p, c_f32p, c_u32p, c_u32p, c_u32p, c_f32p,
+                                      c_f32p, ctypes.c_uint32, ctypes.c_int]
         L.orc_density_at.argtypes = [sp, c_f32p, c_u32p, c_u32p, ctypes.c_uint32]
         L.orc_density_at.restype = ctypes.c_float
         L.orc_force_at.argtypes = [sp, c_f32p, c_f32p, c_f32p, c_u32p, c_u32p, ctypes.c_uint32,
@@ -215,6 +217,16 @@ class OracleState(_StateBase):
                        up(self.cell_start), up(self.cell_end), fp(self.phase), threads,
                        stop_after)
         return self
+
+    def force_scale(self, threads=1):
+        """Per particle (original order) sum of |pair term| of this step's forces,
+        evaluated on the current sorted arrays: (scale_a, scale_b) as (n, 4)."""
+        sa = np.zeros((self.n, 4), np.float32)
+        sb = np.zeros((self.n, 4), np.float32)
+        lib().orc_force_scale(ctypes.byref(self.p), fp(self.spos), fp(self.svel), fp(self.meas),
+                              up(self.idx), up(self.cell_start), up(self.cell_end), fp(sa), fp(sb),
+                              self.n, threads)
+        return sa, sb
 
     def density_at(self, i):
         return float(lib().orc_density_at(ctypes.byref(self.p), fp(self.spos),

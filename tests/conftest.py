@@ -17,10 +17,8 @@ def built():
     """Build the CUDA library and the oracle if they are missing."""
     from cmag_gb300 import build as B
     from oracle import oracle as O
-    if not os.path.exists(B.LIB):
-        B.build()
-    if not os.path.exists(O.LIB_PATH):
-        O.build()
+    B.build_if_stale()
+    O.build()  # make: rebuilds only when the sources changed
     return True
 
 
