@@ -269,8 +269,11 @@ def main():
     cfg["l2"] = "inputs larger than L2 (working set %.0f MB)" % (
         (n * (7 * 16 + 4 * 4) + 8 * p.num_grid_cells) / 1e6)
 
-    # warm-up (graph capture happens on the first step)
+    # warm-up (graph capture happens on the first step), then pick the lanes per
+    # particle of the neighbour loops on this workload
     s.update_n(args.warmup)
+    cfg["lanes_density_force"] = list(s.autotune(3))
+    s.update_n(2)
     s.synchronize()
 
     # ---- device-resident timed region ----

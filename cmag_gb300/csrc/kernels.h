@@ -58,10 +58,11 @@ void launch_cell_view(const uint32_t *off, uint32_t scan_base, uint32_t scan_cel
                       uint64_t ncells, uint32_t *cell_start, uint32_t *cell_end, cudaStream_t st);
 
 // ---- neighbour loops (neighbors.cu) ----------------------------------------
+// density also writes aux[i] = (p/rho^2, rho) (DamBreak) or (p/rho^2, 1/rho)
 void launch_density(const DevParams &p, int group, const float4 *spos, const uint32_t *off,
-                    float4 *meas, cudaStream_t st);
+                    float4 *meas, float2 *aux, cudaStream_t st);
 void launch_force(const DevParams &p, int group, const float4 *spos, const float4 *svel,
-                  const float4 *meas, const uint32_t *idx, const uint32_t *off, float4 *out_a,
+                  const float2 *aux, const uint32_t *idx, const uint32_t *off, float4 *out_a,
                   float4 *out_b, cudaStream_t st);
 
 // ---- integration and wall motion (integrate.cu) ------------------------------

@@ -40,6 +40,14 @@ struct DevParams {
     float amplitude, wave_k, wave_speed, half_fluid_h;  // Peristalsis wall law
     float half_world_x;
     float p_wall;                 // Poiseuille wall pressure (EOS at rho0)
+    // derived on the host for the neighbour loops
+    float inv_csx, inv_csy, inv_csz; // 1 / cell size (trimming only; not the hash)
+    float support2_cells;         // (2h / cell size)^2
+    uint32_t planar_layer;        // z layer of a planar scene
+    uint32_t pow2_grid;           // 1: every grid dimension is a power of two
+    float lj_a2;                  // a^2 of the wall force
+    float av_coeff;               // 2 alpha h c0 (fluid_kernel.cu:229-230)
+    float visc_coeff;             // m (mu + mu) (poiseuilleFlowKernel.cu:242-243)
 };
 
 // Device-resident per-step scalars of the Peristalsis phase machine
@@ -75,13 +83,24 @@ __device__ __forceinline__ int3 grid_pos(const DevParams &p, float x, float y, f
     return g;
 }
 
-// calcGridHash (fluid_kernel.cu:27-32): power-of-two wrap, z*Y*X + y*X + x.
+// Periodic wrap of a cell coordinate onto [0, n): the reference's mask
+// (fluid_kernel.cu:28-30) for power-of-two grids, the same residue for any other
+// size (an extension: the mask is only defined for powers of two).
+__device__ __forceinline__ uint32_t wrap_cell(int v, uint32_t n, uint32_t pow2)
+{
+    if (pow2) return (uint32_t)v & (n - 1u);
+    if ((uint32_t)v < n) return (uint32_t)v;
+    int m = v % (int)n;
+    return (uint32_t)(m < 0 ? m + (int)n : m);
+}
+
+// calcGridHash (fluid_kernel.cu:27-32): z*Y*X + y*X + x of the wrapped cell.
 // The host checks that every product stays below 2^24 per operand, where the
 // reference's __umul24 equals a plain multiply.
 __device__ __forceinline__ uint32_t grid_hash(const DevParams &p, int gx, int gy, int gz)
 {
-    uint32_t x = (uint32_t)gx & (p.gx - 1u), y = (uint32_t)gy & (p.gy - 1u),
-             z = (uint32_t)gz & (p.gz - 1u);
+    const uint32_t x = wrap_cell(gx, p.gx, p.pow2_grid), y = wrap_cell(gy, p.gy, p.pow2_grid),
+                   z = wrap_cell(gz, p.gz, p.pow2_grid);
     return (z * p.gy) * p.gx + y * p.gx + x;
 }
 

@@ -34,6 +34,7 @@ struct cmag_system {
            *svel = nullptr;
     uint32_t *hash[2] = {nullptr, nullptr}, *idx[2] = {nullptr, nullptr};
     uint32_t *cnt = nullptr, *off = nullptr;
+    float2 *aux = nullptr;   // per sorted particle: p/rho^2 and rho or 1/rho
     uint32_t *ws = nullptr;  // sort + scan workspace, cleared every step
     size_t ws_words = 0, sort_words = 0;
     uint32_t *err = nullptr;
@@ -47,13 +48,14 @@ struct cmag_system {
 
     // layout
     bool planar = false;
+    uint32_t planar_layer = 0;
     uint32_t scan_base = 0, scan_cells = 0;
     bool z_uniform = false;
     float z_value = 0.0f;
     bool vz_nonzero = false;
     int last_stage = CMAG_STAGE_INTEGRATE;
 
-    int g_density = 8, g_force = 8;
+    int g_density = 1, g_force = 1;  // lanes per particle (cmag_system_autotune)
 
     bool use_graphs = true;
     cudaGraphExec_t gexec = nullptr;
@@ -100,16 +102,21 @@ int validate(const cmag_sph_params &p, uint32_t n, std::string &why)
 {
     if (p.system < CMAG_DAMBREAK || p.system > CMAG_PERISTALSIS) return why = "unknown system", 1;
     for (int k = 0; k < 3; ++k)
-        if (!is_pow2(p.grid_size[k])) return why = "grid_size must be powers of two", 1;
+        if (p.grid_size[k] == 0 || p.grid_size[k] > (1u << 24)) return why = "grid_size out of range", 1;
     const uint64_t cells = (uint64_t)p.grid_size[0] * p.grid_size[1] * p.grid_size[2];
     if (cells > (1ull << 31)) return why = "more than 2^31 grid cells", 1;
     // the reference hashes with __umul24: equal to a plain product below 2^24
     if ((uint64_t)p.grid_size[2] * p.grid_size[1] > (1u << 24) || p.grid_size[0] > (1u << 24))
         return why = "grid too large for the 24-bit hash products", 1;
     if (p.cell_count < 0 || p.cell_count > 64) return why = "cell_count out of range", 1;
-    // a run of 2c+1 cells must wrap at most once along x
-    if (p.grid_size[0] < (uint32_t)(2 * p.cell_count + 1))
-        return why = "grid_size[0] must be at least 2*cell_count+1", 1;
+    // a run of 2c+1 cells must wrap at most once along x, and rows at most once in y
+    if (p.grid_size[0] < (uint32_t)(2 * p.cell_count + 1) || p.grid_size[1] < (uint32_t)(2 * p.cell_count + 1))
+        return why = "grid_size[0] and grid_size[1] must be at least 2*cell_count+1", 1;
+    // grids that are not powers of two wrap by residue; a 3-D search must then
+    // wrap z at most once too
+    const bool pow2 = is_pow2(p.grid_size[0]) && is_pow2(p.grid_size[1]) && is_pow2(p.grid_size[2]);
+    if (!pow2 && p.grid_size[2] < (uint32_t)(2 * p.cell_count + 1) && p.dims == 3)
+        return why = "grid_size[2] must be at least 2*cell_count+1", 1;
     if (!(p.smoothing_radius > 0.0f) || !(p.particle_radius > 0.0f))
         return why = "smoothing_radius and particle_radius must be positive", 1;
     if (p.kernel != CMAG_KERNEL_WENDLAND && p.kernel != CMAG_KERNEL_CUBIC_SPLINE)
@@ -180,6 +187,18 @@ DevParams make_dev(const cmag_system *s)
     d.half_world_x = p.grid_size[0] * p.particle_radius;
     if (p.eos == CMAG_EOS_TAIT) d.p_wall = 0.0f;
     else d.p_wall = std::pow(p.soundspeed, 2.0f) * p.rest_density;  // poiseuilleFlowKernel.cu:156
+    d.inv_csx = (float)(1.0 / p.cell_size[0]);
+    d.inv_csy = (float)(1.0 / p.cell_size[1]);
+    d.inv_csz = (float)(1.0 / p.cell_size[2]);
+    const double sc = 2.0 * h / p.cell_size[0];
+    d.support2_cells = (float)(sc * sc);
+    // trimming works in cell units: it needs cubic cells
+    if (!(p.cell_size[0] == p.cell_size[1] && p.cell_size[1] == p.cell_size[2])) d.trim = 0;
+    d.pow2_grid = (is_pow2(p.grid_size[0]) && is_pow2(p.grid_size[1]) && is_pow2(p.grid_size[2])) ? 1u : 0u;
+    d.planar_layer = s->planar_layer;
+    d.lj_a2 = p.lj_a * p.lj_a;
+    d.av_coeff = (float)(2.0 * p.av_alpha * h * p.soundspeed);
+    d.visc_coeff = (float)((double)p.particle_mass * (2.0 * p.mu));
     return d;
 }
 
@@ -210,14 +229,16 @@ void refresh_layout(cmag_system *s)
     const cmag_sph_params &p = s->p;
     bool planar = p.dims == 2 && s->z_uniform && !s->vz_nonzero && p.gravity[2] == 0.0f &&
                   (int)p.grid_size[2] > p.cell_count;
-    uint32_t base = 0, cells = (uint32_t)s->ncells;
+    uint32_t base = 0, cells = (uint32_t)s->ncells, layer = 0;
     if (planar) {
-        const uint32_t layer = (uint32_t)z_cell(p, s->z_value) & (p.grid_size[2] - 1u);
+        const int64_t zc = z_cell(p, s->z_value), nz = p.grid_size[2];
+        layer = (uint32_t)(((zc % nz) + nz) % nz);
         cells = p.grid_size[0] * p.grid_size[1];
         base = layer * cells;
     }
     if (planar != s->planar || base != s->scan_base || cells != s->scan_cells) invalidate_graph(s);
     s->planar = planar;
+    s->planar_layer = layer;
     s->scan_base = base;
     s->scan_cells = cells;
 }
@@ -272,14 +293,15 @@ int record_step(cmag_system *s, int last, bool timed)
     if (last >= CMAG_STAGE_REORDER)
         launch_reorder(sorted_idx(s), s->pos, s->vlf, s->spos, s->svel, s->n, st);
     mark(3);
-    if (last >= CMAG_STAGE_DENSITY) launch_density(d, s->g_density, s->spos, s->off, s->meas, st);
+    if (last >= CMAG_STAGE_DENSITY)
+        launch_density(d, s->g_density, s->spos, s->off, s->meas, s->aux, st);
     mark(4);
     if (last >= CMAG_STAGE_FORCE) {
         if (p.system == CMAG_PERISTALSIS)
-            launch_force(d, s->g_force, s->spos, s->svel, s->meas, sorted_idx(s), s->off,
+            launch_force(d, s->g_force, s->spos, s->svel, s->aux, sorted_idx(s), s->off,
                          s->vforce, s->pforce, st);
         else
-            launch_force(d, s->g_force, s->spos, s->svel, s->meas, sorted_idx(s), s->off, s->acc,
+            launch_force(d, s->g_force, s->spos, s->svel, s->aux, sorted_idx(s), s->off, s->acc,
                          nullptr, st);
     }
     mark(5);
@@ -387,7 +409,7 @@ void free_all(cmag_system *s)
     s->events.clear();
     void *ptrs[] = {s->pos, s->vel, s->vlf, s->meas, s->acc, s->vforce, s->pforce, s->pred,
                     s->spos, s->svel, s->hash[0], s->hash[1], s->idx[0], s->idx[1], s->cnt,
-                    s->off, s->ws, s->err, s->phase, s->view_cs, s->view_ce};
+                    s->off, s->aux, s->ws, s->err, s->phase, s->view_cs, s->view_ce};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (s->own_stream) cudaStreamDestroy(s->own_stream);
@@ -518,9 +540,9 @@ int cmag_system_create(const cmag_sph_params *params, uint32_t n, cmag_system **
     s->scan_base = 0;
     s->scan_cells = (uint32_t)s->ncells;
     // 3-D searches need every axis wide enough for one wrap per run
-    if (params->dims == 3) {
-        s->g_density = 4;
-        s->g_force = 4;
+    if (params->dims == 3) {  // 49 rows per particle: split them over 2 lanes
+        s->g_density = 2;
+        s->g_force = 2;
     }
     int rc = CMAG_OK;
     auto step = [&](int r) { if (rc == CMAG_OK) rc = r; };
@@ -545,6 +567,7 @@ int cmag_system_create(const cmag_sph_params *params, uint32_t n, cmag_system **
     step(dalloc(s, &s->acc, f4));
     step(dalloc(s, &s->spos, f4));
     step(dalloc(s, &s->svel, f4));
+    step(dalloc(s, &s->aux, sizeof(float2) * (size_t)n));
     if (params->system == CMAG_PERISTALSIS) {
         step(dalloc(s, &s->vforce, f4));
         step(dalloc(s, &s->pforce, f4));
@@ -954,6 +977,79 @@ int cmag_system_synchronize(cmag_system *s)
         if (bits & CMAG_DEVERR_RANGE) m += " particle hash outside the scanned cell range;";
         return fail(s, CMAG_ERR_DEVICE, m);
     }
+    return CMAG_OK;
+}
+
+int cmag_system_set_groups(cmag_system *s, int32_t gd, int32_t gf)
+{
+    if (!s) return fail(nullptr, CMAG_ERR_INVALID, "null handle");
+    auto ok = [](int32_t g) { return g == 1 || g == 2 || g == 4; };
+    if (!ok(gd) || !ok(gf)) return fail(s, CMAG_ERR_INVALID, "lanes per particle must be 1, 2 or 4");
+    s->g_density = gd;
+    s->g_force = gf;
+    invalidate_graph(s);
+    return CMAG_OK;
+}
+
+int cmag_system_get_groups(const cmag_system *s, int32_t *gd, int32_t *gf)
+{
+    if (!s) return fail(nullptr, CMAG_ERR_INVALID, "null handle");
+    if (gd) *gd = s->g_density;
+    if (gf) *gf = s->g_force;
+    return CMAG_OK;
+}
+
+int cmag_system_autotune(cmag_system *s, int32_t reps)
+{
+    if (!s) return fail(nullptr, CMAG_ERR_INVALID, "null handle");
+    if (reps < 1) reps = 1;
+    // hash, sort and gather of the current state, then time each variant
+    PhaseState saved = s->host_phase;
+    int rc = record_step(s, CMAG_STAGE_REORDER, false);
+    if (rc != CMAG_OK) return rc;
+    if (s->p.system == CMAG_PERISTALSIS) {
+        s->host_phase = saved;
+        if ((rc = upload_phase(s))) return rc;
+    }
+    const DevParams d = make_dev(s);
+    cudaStream_t st = st_of(s);
+    cudaEvent_t a, b;
+    CM_CUDA(s, cudaEventCreate(&a));
+    CM_CUDA(s, cudaEventCreate(&b));
+    const int groups[3] = {1, 2, 4};
+    float best_d = 1e30f, best_f = 1e30f;
+    int gd = s->g_density, gf = s->g_force;
+    float4 *fa = s->p.system == CMAG_PERISTALSIS ? s->vforce : s->acc;
+    float4 *fb = s->p.system == CMAG_PERISTALSIS ? s->pforce : nullptr;
+    for (int k = 0; k < 3; ++k) {
+        launch_density(d, groups[k], s->spos, s->off, s->meas, s->aux, st);  // warm
+        cudaEventRecord(a, st);
+        for (int r = 0; r < reps; ++r) launch_density(d, groups[k], s->spos, s->off, s->meas, s->aux, st);
+        cudaEventRecord(b, st);
+        cudaEventSynchronize(b);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, a, b);
+        if (ms < best_d) { best_d = ms; gd = groups[k]; }
+    }
+    launch_density(d, gd, s->spos, s->off, s->meas, s->aux, st);
+    for (int k = 0; k < 3; ++k) {
+        launch_force(d, groups[k], s->spos, s->svel, s->aux, sorted_idx(s), s->off, fa, fb, st);
+        cudaEventRecord(a, st);
+        for (int r = 0; r < reps; ++r)
+            launch_force(d, groups[k], s->spos, s->svel, s->aux, sorted_idx(s), s->off, fa, fb, st);
+        cudaEventRecord(b, st);
+        cudaEventSynchronize(b);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, a, b);
+        if (ms < best_f) { best_f = ms; gf = groups[k]; }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    CM_CUDA(s, cudaGetLastError());
+    s->g_density = gd;
+    s->g_force = gf;
+    s->last_stage = CMAG_STAGE_FORCE;
+    invalidate_graph(s);
     return CMAG_OK;
 }
 

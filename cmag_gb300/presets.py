@@ -122,9 +122,11 @@ def dambreak3d(fluid=(64, 128, 64), tank=(256, 192, 64), layers=3, h_over_dx=1.3
     dx = column_width / fluid[0]
     r = dx / 2
     L = int(layers)
-    gx = _next_pow2(tank[0] + 2 * L + 2)
-    gy = _next_pow2(tank[1] + L + 2 + tank[1] // 4)
-    gz = _next_pow2(tank[2] + 2 * L + 2)
+    # a tight grid around the tank (+1 cell each side, a quarter tank height of
+    # headroom); sizes need not be powers of two (cells wrap by residue)
+    gx = tank[0] + 2 * L + 2
+    gy = tank[1] + L + 2 + tank[1] // 4
+    gz = tank[2] + 2 * L + 2
     p = dambreak_params(fluid, L + 1, (gx, gy, gz), r)
     o = -(L + 1) * dx
     p.world_origin[0] = p.world_origin[1] = p.world_origin[2] = F32(o)

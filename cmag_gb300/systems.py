@@ -191,6 +191,18 @@ class _System:
     def set_graphs(self, enable):
         self._chk(lib().cmag_system_set_graphs(self._h, int(bool(enable))))
 
+    def set_groups(self, density_lanes, force_lanes):
+        self._chk(lib().cmag_system_set_groups(self._h, int(density_lanes), int(force_lanes)))
+
+    def groups(self):
+        a, b = ctypes.c_int32(), ctypes.c_int32()
+        self._chk(lib().cmag_system_get_groups(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    def autotune(self, reps=3):
+        self._chk(lib().cmag_system_autotune(self._h, int(reps)))
+        return self.groups()
+
     def set_stage_timing(self, enable):
         self._chk(lib().cmag_system_set_stage_timing(self._h, int(bool(enable))))
 

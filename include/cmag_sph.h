@@ -284,6 +284,15 @@ int cmag_system_set_graphs(cmag_system *s, int32_t enable);
 int cmag_system_synchronize(cmag_system *s);
 int cmag_system_device_error_bits(cmag_system *s, uint32_t *bits);
 
+/* Lanes per particle in the density and force loops (1, 2 or 4; the rows of a
+ * particle's cell box are split between its lanes). */
+int cmag_system_set_groups(cmag_system *s, int32_t density_lanes, int32_t force_lanes);
+int cmag_system_get_groups(const cmag_system *s, int32_t *density_lanes, int32_t *force_lanes);
+/* Autotune: on the current state, time the density and force kernels for every
+ * lane count (`reps` launches each) and keep the fastest.  Both kernels are
+ * recomputed from scratch every step, so tuning leaves the trajectory unchanged. */
+int cmag_system_autotune(cmag_system *s, int32_t reps);
+
 /* Per-stage timing: when enabled, every step records CUDA events around each
  * stage on the instance's stream; read back the accumulated milliseconds per stage
  * (6 entries, enum cmag_stage order) and the number of timed steps. */

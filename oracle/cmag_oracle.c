@@ -392,11 +392,23 @@ static i3 grid_pos(const cmag_sph_params *p, float x, float y, float z)
     return g;
 }
 
-/* calcGridHash, fluid_kernel.cu:27-32: power-of-two wrap, z*Y*X + y*X + x */
+static int is_pow2(uint32_t v) { return v && !(v & (v - 1)); }
+
+/* periodic wrap onto [0, n): the reference's mask (fluid_kernel.cu:28-30) for
+ * power-of-two grids; the same residue for other sizes (extension) */
+static uint32_t wrap_cell(int v, uint32_t n, int pow2)
+{
+    if (pow2) return (uint32_t)v & (n - 1);
+    long long m = (long long)v % (long long)n;
+    return (uint32_t)(m < 0 ? m + (long long)n : m);
+}
+
+/* calcGridHash, fluid_kernel.cu:27-32: z*Y*X + y*X + x of the wrapped cell */
 static uint32_t grid_hash(const cmag_sph_params *p, i3 g)
 {
     uint32_t X = p->grid_size[0], Y = p->grid_size[1], Z = p->grid_size[2];
-    uint32_t x = (uint32_t)g.x & (X - 1), y = (uint32_t)g.y & (Y - 1), z = (uint32_t)g.z & (Z - 1);
+    int pow2 = is_pow2(X) && is_pow2(Y) && is_pow2(Z);
+    uint32_t x = wrap_cell(g.x, X, pow2), y = wrap_cell(g.y, Y, pow2), z = wrap_cell(g.z, Z, pow2);
     return umul24(umul24(z, Y), X) + umul24(y, X) + x;
 }
 
@@ -657,7 +669,8 @@ static int force_one(const cmag_sph_params *p, const float *spos, const float *s
                                 float s = p->lj_D * (powf(p->lj_a / dist, 12) - powf(p->lj_a / dist, 6));
                                 f3 term = divs3(smul3(s, rp), powf(dist, 2));
                                 tA = add3(tA, term);
-                                scA = add3(scA, abs3(term));
+                                float smag = fabsf(p->lj_D) * (powf(p->lj_a / dist, 12) + powf(p->lj_a / dist, 6));
+                                scA = add3(scA, divs3(smul3(smag, abs3(rp)), powf(dist, 2)));
                                 continue;
                             }
                             if (q < 2) { /* fluid_kernel.cu:221-237 */
@@ -673,7 +686,17 @@ static int force_one(const cmag_sph_params *p, const float *spos, const float *s
                                 float s = -1.0f * m * (pr / powf(rho, 2) + pr2 / powf(rho2, 2) + art);
                                 f3 term = muls3(smul3(s, normalize3(rp)), temp);
                                 tA = add3(tA, term);
-                                scA = add3(scA, abs3(term));
+                                /* conditioning: the sizes of the factors, with every
+                                 * difference (v_i - v_j, p_i + p_j terms) taken as a sum
+                                 * of magnitudes */
+                                float art_mag = 0.0f;
+                                if (vij_pij < 0) {
+                                    f3 vs = add3(abs3(vi), abs3(vj));
+                                    art_mag = 2.0f * p->av_alpha * h * p->soundspeed / (rho + rho2) *
+                                              dot3(vs, abs3(rp)) / (dot3(rp, rp) + 0.001f * powf(h, 2));
+                                }
+                                float smag = m * (fabsf(pr) / powf(rho, 2) + fabsf(pr2) / powf(rho2, 2) + art_mag);
+                                scA = add3(scA, muls3(abs3(rp), smag * fabsf(temp) / dist));
                             }
                         } else if (p->system == CMAG_POISEUILLE) {
                             if (q < 2) { /* poiseuilleFlowKernel.cu:236-245 */
@@ -686,7 +709,13 @@ static int force_one(const cmag_sph_params *p, const float *spos, const float *s
                                 float s2 = m * (p->mu + p->mu);
                                 f3 t2 = muls3(divs3(muls3(divs3(smul3(s2, vab), rho * rho2), 1.0f), dist), temp);
                                 tA = add3(tA, add3(t1, t2));
-                                scA = add3(scA, add3(abs3(t1), abs3(t2)));
+                                float m1 = m * (fabsf(pr) / powf(rho, 2) + fabsf(pr2) / powf(rho2, 2));
+                                f3 vin = (wj == 1.0f && (pj.y > p->world_origin[1] + p->boundary_offset * 2.0f * p->particle_radius +
+                                                                   p->fluid_size[1] * 2.0f * p->particle_radius ||
+                                                         pj.y < p->world_origin[1] + p->boundary_offset * 2.0f * p->particle_radius))
+                                             ? abs3(vab) : add3(abs3(vi), abs3(vj));
+                                scA = add3(scA, add3(muls3(abs3(rp), m1 * fabsf(temp) / dist),
+                                                     muls3(vin, s2 * fabsf(temp) / (rho * rho2 * dist))));
                             }
                         } else {
                             if (q < 2) {
@@ -698,12 +727,13 @@ static int force_one(const cmag_sph_params *p, const float *spos, const float *s
                                 float sv = m * temp * (p->mu + p->mu);
                                 f3 tv = divs3(smul3(sv, vab), rho * rho2 * dist);
                                 tA = add3(tA, tv);
-                                scA = add3(scA, abs3(tv));
+                                scA = add3(scA, muls3(add3(abs3(vi), abs3(vj)), fabsf(sv) / (rho * rho2 * dist)));
                                 /* pressure, PeristalsisPressureForce.cu:39-43 */
                                 float sp = -1.0f * m * temp * (pr / powf(rho, 2) + pr2 / powf(rho2, 2));
                                 f3 tp = smul3(sp, normalize3(rp));
                                 tB = add3(tB, tp);
-                                scB = add3(scB, abs3(tp));
+                                float pm = m * fabsf(temp) * (fabsf(pr) / powf(rho, 2) + fabsf(pr2) / powf(rho2, 2));
+                                scB = add3(scB, muls3(abs3(rp), pm / dist));
                             }
                         }
                     }
@@ -865,7 +895,7 @@ void orc_remove_right_boundary(cmag_sph_params *p, float *pos, uint32_t n)
  * poiseuilleFlowSystem.cpp:212-270, PeristalsisSystem::Update PeristalsisSystem.cpp:320-407 */
 void orc_step(cmag_sph_params *p, uint32_t n, uint64_t ncells, float *pos, float *vel, float *vlf,
               float *meas, float *acc, float *vforce, float *pforce, float *spos, float *svel,
-              uint32_t *hash, uint32_t *idx, uint32_t *cs, uint32_t *ce, float phase[4],
+              uint32_t *hash, uint32_t *idx, uint32_t *cs, uint32_t *ce, float phase[5],
               int threads, int stop_after)
 {
     float dt = p->delta_time;
@@ -894,6 +924,7 @@ void orc_step(cmag_sph_params *p, uint32_t n, uint64_t ncells, float *pos, float
     if (stop_after == CMAG_STAGE_FORCE) return;
     float t = 0.0f;
     if (p->system == CMAG_PERISTALSIS) t = p->is_boundary_configuration ? 0 : phase[0] - phase[1];
+    phase[4] = t;
     orc_integrate(p, pos, vel, vlf, acc, vforce, pforce, t, n);
     phase[0] += dt;
 }

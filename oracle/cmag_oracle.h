@@ -82,15 +82,16 @@ void orc_configure_boundary(const cmag_sph_params *p, float *pos, float wave_hei
 void orc_shift_right_boundary(const cmag_sph_params *p, float *pos, uint32_t n);
 void orc_remove_right_boundary(cmag_sph_params *p, float *pos, uint32_t n);
 
-/* Whole update() of one step.  phase[4] = {elapsed, time_shift, time_relax,
- * current_wave_height} (only elapsed is used outside Peristalsis); p may be
+/* Whole update() of one step.  phase[5] = {elapsed, time_shift, time_relax,
+ * current_wave_height, t} (only elapsed is used outside Peristalsis; t is an
+ * output: the time the integration of this step used); p may be
  * modified (Peristalsis boundary-configuration flag).  stop_after: enum
  * cmag_stage, stages after it are skipped and time is not advanced unless the
  * whole step runs. */
 void orc_step(cmag_sph_params *p, uint32_t n, uint64_t ncells, float *pos, float *vel, float *vlf,
               float *meas, float *acc, float *vforce, float *pforce, float *spos, float *svel,
               uint32_t *hash, uint32_t *idx, uint32_t *cell_start, uint32_t *cell_end,
-              float phase[4], int threads, int stop_after);
+              float phase[5], int threads, int stop_after);
 
 #ifdef __cplusplus
 }

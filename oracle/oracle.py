@@ -172,8 +172,8 @@ class _StateBase:
         self.idx = np.zeros(self.n, np.uint32)
         self.cell_start = np.full(self.ncells, 0xFFFFFFFF, np.uint32)
         self.cell_end = np.zeros(self.ncells, np.uint32)
-        # elapsed, time_shift, time_relax, current_wave_height
-        self.phase = np.zeros(4, np.float32)
+        # elapsed, time_shift, time_relax, current_wave_height, t of the last integration
+        self.phase = np.zeros(5, np.float32)
 
     def reset_reference(self):
         """reset()/Reset(): reference scene and initial arrays."""
@@ -207,6 +207,23 @@ class _StateBase:
         return float(self.phase[0])
 
 
+def integrate_from(pre, post, acc, vforce, pforce):
+    """The integration of the step pre -> post recomputed from given forces:
+    pre's arrays (walls placed by configureBoundary first when that step ran it),
+    post's parameters and time.  Returns (pos, vel, vlf)."""
+    pos, vel, vlf = pre.pos.copy(), pre.vel.copy(), pre.vlf.copy()
+    p = post.p
+    if (p.system == PERISTALSIS and pre.p.is_boundary_configuration
+            and pre.phase[3] < np.float32(pre.p.amplitude)):
+        lib().orc_configure_boundary(ctypes.byref(pre.p), fp(pos), float(pre.phase[3]), pre.n)
+    acc = np.ascontiguousarray(acc, np.float32)
+    vforce = np.ascontiguousarray(vforce, np.float32)
+    pforce = np.ascontiguousarray(pforce, np.float32)
+    lib().orc_integrate(ctypes.byref(p), fp(pos), fp(vel), fp(vlf), fp(acc), fp(vforce), fp(pforce),
+                        float(post.phase[4]), pre.n)
+    return pos, vel, vlf
+
+
 class OracleState(_StateBase):
     """One solver advanced by the C restatement."""
 
@@ -227,6 +244,23 @@ class OracleState(_StateBase):
                               up(self.idx), up(self.cell_start), up(self.cell_end), fp(sa), fp(sb),
                               self.n, threads)
         return sa, sb
+
+    def forces_on(self, meas, spos=None, svel=None, threads=1):
+        """This step's forces recomputed on given sorted inputs (e.g. another
+        implementation's measures), with this state's sort and cell ranges.
+        Returns (out_a, out_b, scale_a, scale_b), original order."""
+        meas = np.ascontiguousarray(meas, np.float32)
+        spos = self.spos if spos is None else np.ascontiguousarray(spos, np.float32)
+        svel = self.svel if svel is None else np.ascontiguousarray(svel, np.float32)
+        a = self.acc.copy() if self.p.system != PERISTALSIS else self.vforce.copy()
+        b = self.pforce.copy()
+        lib().orc_force(ctypes.byref(self.p), fp(spos), fp(svel), fp(meas), up(self.idx),
+                        up(self.cell_start), up(self.cell_end), fp(a), fp(b), self.n, threads)
+        sa = np.zeros((self.n, 4), np.float32)
+        sb = np.zeros((self.n, 4), np.float32)
+        lib().orc_force_scale(ctypes.byref(self.p), fp(spos), fp(svel), fp(meas), up(self.idx),
+                              up(self.cell_start), up(self.cell_end), fp(sa), fp(sb), self.n, threads)
+        return a, b, sa, sb
 
     def density_at(self, i):
         return float(lib().orc_density_at(ctypes.byref(self.p), fp(self.spos),

@@ -25,5 +25,5 @@ def oracle_input(name):
     st = O.OracleState(p, int(d["n"][0]))
     for k in IN_FIELDS:
         getattr(st, k)[:] = d["in_" + k]
-    st.phase[:] = d["phase"]
+    st.phase[:4] = d["phase"][:4]
     return st, d

@@ -92,7 +92,7 @@ def test_reference_constructor_values(built):
 def test_dambreak3d_scene_counts(built):
     p, n, tank, L = presets.dambreak3d()
     assert n == 524288 + 430572
-    assert list(p.grid_size) == [512, 256, 128]
+    assert list(p.grid_size) == [264, 245, 72]
     small, ns, ts, Ls = presets.dambreak3d(fluid=(8, 16, 8), tank=(32, 24, 8))
     pos = np.zeros((ns, 4), np.float32)
     check(lib().cmag_dambreak3d_scene_host(ctypes.byref(small), _abi.u3(ts), Ls, 0.01, 1973,
@@ -104,11 +104,11 @@ def test_dambreak3d_scene_counts(built):
 def test_create_reports_errors_without_exiting(built):
     """Invalid parameters come back as a status code and a message."""
     p = presets.dambreak_params((16, 32, 1), 1, (64, 64, 4), 1 / 256)
-    p.grid_size[0] = 60  # not a power of two
+    p.grid_size[0] = 5  # narrower than the 2*cell_count+1 searched cells
     h = ctypes.c_void_p()
     rc = lib().cmag_system_create(ctypes.byref(p), 100, ctypes.byref(h))
     assert rc == _abi.CMAG_ERR_INVALID
-    assert b"power" in lib().cmag_last_error()
+    assert b"2*cell_count+1" in lib().cmag_last_error()
     p.grid_size[0] = 64
     rc = lib().cmag_system_create(ctypes.byref(p), 0, ctypes.byref(h))
     assert rc == _abi.CMAG_ERR_INVALID

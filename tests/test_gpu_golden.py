@@ -18,10 +18,12 @@ CLASSES = {_abi.DAMBREAK: cm.DamBreakSystem, _abi.POISEUILLE: cm.PoiseuilleFlowS
            _abi.PERISTALSIS: cm.PeristalsisSystem}
 
 
+@pytest.mark.parametrize("lanes", [1, 2, 4])
 @pytest.mark.parametrize("name", NAMES)
-def test_gpu_step_matches_golden(gpu, name):
+def test_gpu_step_matches_golden(gpu, name, lanes):
     st, d = oracle_input(name)
     s = CLASSES[st.p.system](params=st.p, num_particles=st.n)
+    s.set_groups(lanes, lanes)
     s.load_state(st)
     s.update()
     got = s.state()
@@ -33,8 +35,10 @@ def test_gpu_step_matches_golden(gpu, name):
     assert_int_equal(np.flatnonzero(cs != 0xFFFFFFFF), occ, "occupied cells")
     assert_int_equal(cs[occ], d["out_cell_start"], "cellStart")
     assert_int_equal(ce[occ], d["out_cell_end"], "cellEnd")
+    from oracle import oracle as O
+    pre = O.OracleState(st.p, st.n).set_state(st)
     st.step()
-    errs = compare_step(got, st, label=name + ": ")
+    errs = compare_step(got, pre, st, label=name + ": ")
     assert np.float32(s.getElapsedTime()) == d["out_phase"][0]
     s.synchronize()
     s.close()

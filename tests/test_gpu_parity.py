@@ -100,24 +100,40 @@ def test_stages_bit_exact(gpu, name):
     s.close()
 
 
+@pytest.mark.parametrize("lanes", [1, 2, 4])
 @pytest.mark.parametrize("name", sorted(SCENES))
-def test_one_step_along_trajectory(gpu, name):
+def test_one_step_along_trajectory(gpu, name, lanes):
     """At several points of an oracle trajectory, one GPU step equals one oracle step."""
     s, ref = SCENES[name]()
+    s.set_groups(lanes, lanes)
     checkpoints = {0, 5, 20}
     errs = []
     for k in range(21):
         if k in checkpoints:
             s.load_state(ref)
+            pre = O.OracleState(ref.p, ref.n).set_state(ref)
             nxt = O.OracleState(ref.p, ref.n).set_state(ref)
-            nxt.cell_end[:] = 0
             s.update()
             nxt.step()
-            errs.append(compare_step(s.state(), nxt, label="%s step %d: " % (name, k)))
+            errs.append(compare_step(s.state(), pre, nxt, label="%s step %d: " % (name, k)))
         ref.step()
     s.synchronize()
     s.close()
     print(name, errs)
+
+
+def test_peristalsis_moving_walls_step(gpu):
+    """One step with the walls in motion (after the configuration phase)."""
+    s, ref = _peristalsis()
+    ref.p.is_boundary_configuration = 0
+    for _ in range(12):
+        ref.step()
+    s.load_state(ref)
+    pre = O.OracleState(ref.p, ref.n).set_state(ref)
+    ref.step()
+    s.update()
+    compare_step(s.state(), pre, ref, label="peristalsis moving: ")
+    s.close()
 
 
 @pytest.mark.parametrize("graphs", [True, False])
