@@ -72,7 +72,7 @@ __global__ void __launch_bounds__(256)
             if (s_hist[b]) atomicAdd(&hist[b], s_hist[b]);
 }
 
-__global__ void __launch_bounds__(kScanThreads)
+__global__ void __launch_bounds__(kScanThreads, 4)
     k_cell_scan(uint32_t *__restrict__ cnt, uint32_t *__restrict__ off, uint32_t m,
                 uint32_t *tile_ctr, uint32_t *status, uint32_t *err)
 {

@@ -50,56 +50,89 @@ __device__ __forceinline__ uint32_t wrap_axis(int v, uint32_t n)
     return (uint32_t)(m < 0 ? m + (int)n : m);
 }
 
-// Sorted range and image shift of row `r` of particle (fx,fy,fz) (fractional
-// cell coordinates) in cell g.  Fills up to two runs; returns how many.
+// The runs of one row of the cell box: [b0, e0) with x image shift sx0 and,
+// when the row wraps in x, [b1, e1) with sx1 (empty otherwise); sy, sz: the
+// row's image shifts.
+struct RowRuns {
+    uint32_t b0, e0, b1, e1;
+    float sx0, sx1, sy, sz;
+};
+
+// Row (dy, dz) of particle (fx,fy,fz) (fractional cell coordinates) in cell g.
+// Returns false when the row holds no candidates.
 template <int SYS, bool PLANAR, bool TRIM>
-__device__ __forceinline__ int row_runs(const DevParams &p, const uint32_t *__restrict__ off,
-                                        int r, int3 g, float fx, float fy, float fz,
-                                        uint32_t b[2], uint32_t e[2], float sx[2], float &sy,
-                                        float &sz)
+__device__ __forceinline__ bool row_runs(const DevParams &p, const uint32_t *__restrict__ off,
+                                         int dy, int dz, int3 g, float fx, float fy, float fz,
+                                         RowRuns &rr)
 {
     const int c = p.cell_count;
-    const int w = 2 * c + 1;
-    const int dy = (r % w) - c;
-    const int dz = PLANAR ? 0 : (r / w) - c;
     const int yu = g.y + dy, zu = g.z + dz;
     int xa = g.x - c, xb = g.x + c;
     if (TRIM) {
         float dym = 0.0f, dzm = 0.0f;
         if (dy > 0) dym = (float)yu - fy;
         if (dy < 0) dym = fy - (float)(yu + 1);
-        if (dz > 0) dzm = (float)zu - fz;
-        if (dz < 0) dzm = fz - (float)(zu + 1);
+        if (!PLANAR) {
+            if (dz > 0) dzm = (float)zu - fz;
+            if (dz < 0) dzm = fz - (float)(zu + 1);
+            dzm = fmaxf(dzm - kMargin, 0.0f);
+        }
         dym = fmaxf(dym - kMargin, 0.0f);
-        dzm = fmaxf(dzm - kMargin, 0.0f);
         const float r2 = p.support2_cells - dym * dym - dzm * dzm;
-        if (r2 < 0.0f) return 0;
-        const float R = sqrtf(r2) + kMargin;
+        if (r2 <= 0.0f) return false;
+        // conservative half width: the approximate square root errs by far less
+        // than the margin
+        const float R = r2 * rsqrtf(r2) + kMargin;
         xa = max(xa, __float2int_rd(fx - R));
         xb = min(xb, __float2int_rd(fx + R));
-        if (xa > xb) return 0;
+        if (xa > xb) return false;
     }
-    const uint32_t zm = PLANAR ? (uint32_t)(p.planar_layer) : wrap_axis(zu, p.gz);
+    const uint32_t zm = PLANAR ? p.planar_layer : wrap_axis(zu, p.gz);
     const uint32_t row = (zm * p.gy + wrap_axis(yu, p.gy)) * p.gx - p.scan_base;
-    if (row >= p.scan_cells) return 0;  // outside the offset table: no particles
-    sy = (SYS == CMAG_PERISTALSIS) ? (float)eval_shift(yu, p.gy) * p.wsy : 0.0f;
-    sz = (SYS == CMAG_PERISTALSIS && !PLANAR) ? (float)eval_shift(zu, p.gz) * p.wsz : 0.0f;
+    if (row >= p.scan_cells) return false;  // outside the offset table: no particles
+    rr.sy = (SYS == CMAG_PERISTALSIS) ? (float)eval_shift(yu, p.gy) * p.wsy : 0.0f;
+    rr.sz = (SYS == CMAG_PERISTALSIS && !PLANAR) ? (float)eval_shift(zu, p.gz) * p.wsz : 0.0f;
     const uint32_t xma = wrap_axis(xa, p.gx);
     const uint32_t len = (uint32_t)(xb - xa);
-    const float shift_a = (SYS == CMAG_DAMBREAK) ? 0.0f : (float)eval_shift(xa, p.gx) * p.wsx;
+    rr.sx0 = (SYS == CMAG_DAMBREAK) ? 0.0f : (float)eval_shift(xa, p.gx) * p.wsx;
+    rr.b0 = __ldg(off + row + xma);
     if (xma + len < p.gx) {
-        b[0] = __ldg(off + row + xma);
-        e[0] = __ldg(off + row + xma + len + 1);
-        sx[0] = shift_a;
-        return 1;
+        rr.e0 = __ldg(off + row + xma + len + 1);
+        rr.b1 = rr.e1 = 0;
+        rr.sx1 = 0.0f;
+    } else {
+        rr.e0 = __ldg(off + row + p.gx);
+        rr.b1 = __ldg(off + row);
+        rr.e1 = __ldg(off + row + (xma + len - p.gx) + 1);
+        rr.sx1 = (SYS == CMAG_DAMBREAK) ? 0.0f : (float)eval_shift(xb, p.gx) * p.wsx;
     }
-    b[0] = __ldg(off + row + xma);
-    e[0] = __ldg(off + row + p.gx);
-    sx[0] = shift_a;
-    b[1] = __ldg(off + row);
-    e[1] = __ldg(off + row + (xma + len - p.gx) + 1);
-    sx[1] = (SYS == CMAG_DAMBREAK) ? 0.0f : (float)eval_shift(xb, p.gx) * p.wsx;
-    return 2;
+    return true;
+}
+
+// Calls visit(j, sx, sy, sz) for every candidate of the rows this lane owns
+// (rows r = lane, lane + G, ... of the (2c+1)^2 box, dy fastest).
+template <int SYS, bool PLANAR, bool TRIM, int G, class Visit>
+__device__ __forceinline__ void for_each_candidate(const DevParams &p,
+                                                   const uint32_t *__restrict__ off, int lane,
+                                                   int3 g, float3 f, Visit &&visit)
+{
+    const int c = p.cell_count;
+    const int w = 2 * c + 1;
+    int dy = (G == 1) ? -c : (lane % w) - c;
+    int dz = PLANAR ? 0 : ((G == 1) ? -c : (lane / w) - c);
+    const int nrows = rows_of<PLANAR>(c);
+    for (int r = lane; r < nrows; r += G) {
+        RowRuns rr;
+        if (row_runs<SYS, PLANAR, TRIM>(p, off, dy, dz, g, f.x, f.y, f.z, rr)) {
+            for (uint32_t j = rr.b0; j < rr.e0; ++j) visit(j, rr.sx0, rr.sy, rr.sz);
+            for (uint32_t j = rr.b1; j < rr.e1; ++j) visit(j, rr.sx1, rr.sy, rr.sz);
+        }
+        dy += G;
+        while (dy > c) {
+            dy -= w;
+            ++dz;
+        }
+    }
 }
 
 template <int G>
@@ -116,8 +149,9 @@ __device__ __forceinline__ float3 frac_cell(const DevParams &p, float4 q)
 }
 
 // ---------------------------------------------------------------- density --
+// 256 threads, 6 blocks per SM: at most 42 registers, no spills
 template <int SYS, bool PLANAR, bool TRIM, int G>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 6)
     k_density(DevParams p, const float4 *__restrict__ spos, const uint32_t *__restrict__ off,
               float4 *__restrict__ meas, float2 *__restrict__ aux)
 {
@@ -131,22 +165,13 @@ __global__ void __launch_bounds__(256)
     float sum = 0.0f;
     if (active && !pinned) {
         const int3 g = grid_pos(p, pi.x, pi.y, pi.z);
-        const float3 f = frac_cell(p, pi);
-        const int nrows = rows_of<PLANAR>(p.cell_count);
-        for (int r = lane; r < nrows; r += G) {
-            uint32_t b[2], e[2];
-            float sx[2], sy, sz;
-            const int runs = row_runs<SYS, PLANAR, TRIM>(p, off, r, g, f.x, f.y, f.z, b, e, sx, sy, sz);
-            for (int k = 0; k < runs; ++k) {
-                for (uint32_t j = b[k]; j < e[k]; ++j) {
-                    const float4 pj = __ldg(spos + j);
-                    const float rx = pi.x - (pj.x + sx[k]), ry = pi.y - (pj.y + sy),
-                                rz = pi.z - (pj.z + sz);
-                    const float d2 = rx * rx + ry * ry + rz * rz;
-                    if (d2 < p.support2) sum += kernel_w(p, d2 * rsqrtf(fmaxf(d2, 1e-30f)) * p.inv_h);
-                }
-            }
-        }
+        for_each_candidate<SYS, PLANAR, TRIM, G>(
+            p, off, lane, g, frac_cell(p, pi), [&](uint32_t j, float sx, float sy, float sz) {
+                const float4 pj = __ldg(spos + j);
+                const float rx = pi.x - (pj.x + sx), ry = pi.y - (pj.y + sy), rz = pi.z - (pj.z + sz);
+                const float d2 = rx * rx + ry * ry + rz * rz;
+                if (d2 < p.support2) sum += kernel_w(p, d2 * rsqrtf(fmaxf(d2, 1e-30f)) * p.inv_h);
+            });
     }
     sum = group_sum<G>(sum);
     if (active && lane == 0) {
@@ -165,8 +190,9 @@ __global__ void __launch_bounds__(256)
 }
 
 // ------------------------------------------------------------------ force --
+// 256 threads, 4 blocks per SM: at most 64 registers
 template <int SYS, bool PLANAR, bool TRIM, int G>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 4)
     k_force(DevParams p, const float4 *__restrict__ spos, const float4 *__restrict__ svel,
             const float2 *__restrict__ aux, const uint32_t *__restrict__ idx,
             const uint32_t *__restrict__ off, float4 *__restrict__ out_a,
@@ -185,81 +211,73 @@ __global__ void __launch_bounds__(256)
         const float2 ai = aux[i];
         const float pterm = ai.x;
         const int3 g = grid_pos(p, pi.x, pi.y, pi.z);
-        const float3 f = frac_cell(p, pi);
-        const int nrows = rows_of<PLANAR>(p.cell_count);
-        for (int r = lane; r < nrows; r += G) {
-            uint32_t b[2], e[2];
-            float sx[2], sy, sz;
-            const int runs = row_runs<SYS, PLANAR, TRIM>(p, off, r, g, f.x, f.y, f.z, b, e, sx, sy, sz);
-            for (int k = 0; k < runs; ++k) {
-                for (uint32_t j = b[k]; j < e[k]; ++j) {
-                    if (j == i) continue;
-                    const float4 pj = __ldg(spos + j);
-                    const float rx = pi.x - (pj.x + sx[k]), ry = pi.y - (pj.y + sy),
-                                rz = pi.z - (pj.z + sz);
-                    const float d2 = rx * rx + ry * ry + rz * rz;
-                    if (SYS == CMAG_DAMBREAK) {
-                        if (pj.w != (float)CMAG_FLUID) {
-                            // Lennard-Jones wall force (fluid_kernel.cu:199-207)
-                            if (TRIM && !(d2 < p.support2)) continue;
-                            const float inv_d2 = __frcp_rn(d2);
-                            const float a2 = p.lj_a2 * inv_d2;
-                            const float a6 = a2 * a2 * a2;
-                            const float s = p.lj_D * (a6 * a6 - a6) * inv_d2;
-                            ax += s * rx; ay += s * ry; az += s * rz;
-                            continue;
-                        }
-                        if (!(d2 < p.support2)) continue;
-                        // pressure + Monaghan viscosity (fluid_kernel.cu:221-237)
-                        const float inv_d = rsqrtf(d2);
-                        const float temp = kernel_dw(p, d2 * inv_d * p.inv_h);
-                        const float2 aj = __ldg(aux + j);
-                        float s = pterm + aj.x;
-                        const float4 vj = __ldg(svel + j);
-                        const float vij = (vi.x - vj.x) * rx + (vi.y - vj.y) * ry + (vi.z - vj.z) * rz;
-                        if (vij < 0.0f) {
-                            const float nu = __fdividef(p.av_coeff, ai.y + aj.y);
-                            s -= __fdividef(nu * vij, d2 + p.av_eps2);
-                        }
-                        s *= -p.mass * temp * inv_d;
+        for_each_candidate<SYS, PLANAR, TRIM, G>(
+            p, off, lane, g, frac_cell(p, pi), [&](uint32_t j, float sx, float sy, float sz) {
+                if (j == i) return;
+                const float4 pj = __ldg(spos + j);
+                const float rx = pi.x - (pj.x + sx), ry = pi.y - (pj.y + sy),
+                            rz = pi.z - (pj.z + sz);
+                const float d2 = rx * rx + ry * ry + rz * rz;
+                if (SYS == CMAG_DAMBREAK) {
+                    if (pj.w != (float)CMAG_FLUID) {
+                        // Lennard-Jones wall force (fluid_kernel.cu:199-207)
+                        if (TRIM && !(d2 < p.support2)) return;
+                        const float inv_d2 = __frcp_rn(d2);
+                        const float a2 = p.lj_a2 * inv_d2;
+                        const float a6 = a2 * a2 * a2;
+                        const float s = p.lj_D * (a6 * a6 - a6) * inv_d2;
                         ax += s * rx; ay += s * ry; az += s * rz;
-                    } else if (SYS == CMAG_POISEUILLE) {
-                        if (!(d2 < p.support2)) continue;
-                        // pressure + Morris viscosity with wall extrapolation
-                        // (poiseuilleFlowKernel.cu:184-208, 236-245)
-                        const float inv_d = rsqrtf(d2);
-                        const float temp = kernel_dw(p, d2 * inv_d * p.inv_h);
-                        const float2 aj = __ldg(aux + j);
-                        const float4 vj = __ldg(svel + j);
-                        float vx, vy, vz;
-                        if (pj.w == 1.0f && (pj.y > p.wall_top || pj.y < p.wall_bottom)) {
-                            const bool top = pj.y > p.wall_top;
-                            const float da = top ? p.wall_top - pi.y : pi.y - p.wall_bottom;
-                            const float db = top ? pj.y - p.wall_top : p.wall_bottom - pj.y;
-                            const float beta = fminf(1000.0f, 1.0f + __fdividef(db, da));
-                            vx = beta * vi.x; vy = beta * vi.y; vz = beta * vi.z;
-                        } else {
-                            vx = vi.x - vj.x; vy = vi.y - vj.y; vz = vi.z - vj.z;
-                        }
-                        const float sp = -p.mass * (pterm + aj.x) * temp * inv_d;
-                        const float sv = p.visc_coeff * temp * ai.y * aj.y * inv_d;
-                        ax += sp * rx + sv * vx; ay += sp * ry + sv * vy; az += sp * rz + sv * vz;
-                    } else {
-                        if (!(d2 < p.support2)) continue;
-                        // viscous (PeristalsisViscousForce.cu:206-213) and pressure
-                        // (PeristalsisPressureForce.cu:39-43) from one pass
-                        const float inv_d = rsqrtf(d2);
-                        const float temp = kernel_dw(p, d2 * inv_d * p.inv_h);
-                        const float2 aj = __ldg(aux + j);
-                        const float4 vj = __ldg(svel + j);
-                        const float sv = p.visc_coeff * temp * ai.y * aj.y * inv_d;
-                        ax += sv * (vi.x - vj.x); ay += sv * (vi.y - vj.y); az += sv * (vi.z - vj.z);
-                        const float sp = -p.mass * temp * (pterm + aj.x) * inv_d;
-                        bx += sp * rx; by += sp * ry; bz += sp * rz;
+                        return;
                     }
+                    if (!(d2 < p.support2)) return;
+                    // pressure + Monaghan viscosity (fluid_kernel.cu:221-237)
+                    const float inv_d = rsqrtf(d2);
+                    const float temp = kernel_dw(p, d2 * inv_d * p.inv_h);
+                    const float2 aj = __ldg(aux + j);
+                    float s = pterm + aj.x;
+                    const float4 vj = __ldg(svel + j);
+                    const float vij = (vi.x - vj.x) * rx + (vi.y - vj.y) * ry + (vi.z - vj.z) * rz;
+                    if (vij < 0.0f) {
+                        const float nu = __fdividef(p.av_coeff, ai.y + aj.y);
+                        s -= __fdividef(nu * vij, d2 + p.av_eps2);
+                    }
+                    s *= -p.mass * temp * inv_d;
+                    ax += s * rx; ay += s * ry; az += s * rz;
+                } else if (SYS == CMAG_POISEUILLE) {
+                    if (!(d2 < p.support2)) return;
+                    // pressure + Morris viscosity with wall extrapolation
+                    // (poiseuilleFlowKernel.cu:184-208, 236-245)
+                    const float inv_d = rsqrtf(d2);
+                    const float temp = kernel_dw(p, d2 * inv_d * p.inv_h);
+                    const float2 aj = __ldg(aux + j);
+                    const float4 vj = __ldg(svel + j);
+                    float vx, vy, vz;
+                    if (pj.w == 1.0f && (pj.y > p.wall_top || pj.y < p.wall_bottom)) {
+                        const bool top = pj.y > p.wall_top;
+                        const float da = top ? p.wall_top - pi.y : pi.y - p.wall_bottom;
+                        const float db = top ? pj.y - p.wall_top : p.wall_bottom - pj.y;
+                        const float beta = fminf(1000.0f, 1.0f + __fdividef(db, da));
+                        vx = beta * vi.x; vy = beta * vi.y; vz = beta * vi.z;
+                    } else {
+                        vx = vi.x - vj.x; vy = vi.y - vj.y; vz = vi.z - vj.z;
+                    }
+                    const float sp = -p.mass * (pterm + aj.x) * temp * inv_d;
+                    const float sv = p.visc_coeff * temp * ai.y * aj.y * inv_d;
+                    ax += sp * rx + sv * vx; ay += sp * ry + sv * vy; az += sp * rz + sv * vz;
+                } else {
+                    if (!(d2 < p.support2)) return;
+                    // viscous (PeristalsisViscousForce.cu:206-213) and pressure
+                    // (PeristalsisPressureForce.cu:39-43) from one pass
+                    const float inv_d = rsqrtf(d2);
+                    const float temp = kernel_dw(p, d2 * inv_d * p.inv_h);
+                    const float2 aj = __ldg(aux + j);
+                    const float4 vj = __ldg(svel + j);
+                    const float sv = p.visc_coeff * temp * ai.y * aj.y * inv_d;
+                    ax += sv * (vi.x - vj.x); ay += sv * (vi.y - vj.y); az += sv * (vi.z - vj.z);
+                    const float sp = -p.mass * temp * (pterm + aj.x) * inv_d;
+                    bx += sp * rx; by += sp * ry; bz += sp * rz;
                 }
-            }
-        }
+            });
     }
     if (G > 1) {
         ax = group_sum<G>(ax); ay = group_sum<G>(ay); az = group_sum<G>(az);

@@ -507,6 +507,18 @@ static float kernel_dw(const cmag_sph_params *p, float q)
     return s * (-0.75f * t * t);
 }
 
+/* 1 + |d ln(dW/dr) / d ln q|: how much a relative rounding of the distance is
+ * amplified in the kernel derivative (large near q = 2, where dW/dr -> 0) */
+static float kernel_dw_cond(const cmag_sph_params *p, float q)
+{
+    if (p->kernel == CMAG_KERNEL_WENDLAND) {
+        float t = 1.0f - 0.5f * q;
+        return 1.0f + fabsf(1.0f - 1.5f * q / fmaxf(t, 1e-6f));
+    }
+    if (q < 1.0f) return 1.0f + fabsf((-3.0f + 4.5f * q) / (-3.0f + 2.25f * q));
+    return 1.0f + 2.0f * q / fmaxf(2.0f - q, 1e-6f);
+}
+
 static float eos_pressure(const cmag_sph_params *p, float dens)
 {
     if (p->eos == CMAG_EOS_TAIT || p->system == CMAG_DAMBREAK)
@@ -670,7 +682,8 @@ static int force_one(const cmag_sph_params *p, const float *spos, const float *s
                                 f3 term = divs3(smul3(s, rp), powf(dist, 2));
                                 tA = add3(tA, term);
                                 float smag = fabsf(p->lj_D) * (powf(p->lj_a / dist, 12) + powf(p->lj_a / dist, 6));
-                                scA = add3(scA, divs3(smul3(smag, abs3(rp)), powf(dist, 2)));
+                                /* (a/r)^12 amplifies a relative rounding of r twelve times */
+                                scA = add3(scA, divs3(smul3(13.0f * smag, abs3(rp)), powf(dist, 2)));
                                 continue;
                             }
                             if (q < 2) { /* fluid_kernel.cu:221-237 */
@@ -696,7 +709,7 @@ static int force_one(const cmag_sph_params *p, const float *spos, const float *s
                                               dot3(vs, abs3(rp)) / (dot3(rp, rp) + 0.001f * powf(h, 2));
                                 }
                                 float smag = m * (fabsf(pr) / powf(rho, 2) + fabsf(pr2) / powf(rho2, 2) + art_mag);
-                                scA = add3(scA, muls3(abs3(rp), smag * fabsf(temp) / dist));
+                                scA = add3(scA, muls3(abs3(rp), smag * fabsf(temp) * kernel_dw_cond(p, q) / dist));
                             }
                         } else if (p->system == CMAG_POISEUILLE) {
                             if (q < 2) { /* poiseuilleFlowKernel.cu:236-245 */
@@ -714,8 +727,9 @@ static int force_one(const cmag_sph_params *p, const float *spos, const float *s
                                                                    p->fluid_size[1] * 2.0f * p->particle_radius ||
                                                          pj.y < p->world_origin[1] + p->boundary_offset * 2.0f * p->particle_radius))
                                              ? abs3(vab) : add3(abs3(vi), abs3(vj));
-                                scA = add3(scA, add3(muls3(abs3(rp), m1 * fabsf(temp) / dist),
-                                                     muls3(vin, s2 * fabsf(temp) / (rho * rho2 * dist))));
+                                float ct = fabsf(temp) * kernel_dw_cond(p, q);
+                                scA = add3(scA, add3(muls3(abs3(rp), m1 * ct / dist),
+                                                     muls3(vin, s2 * ct / (rho * rho2 * dist))));
                             }
                         } else {
                             if (q < 2) {
@@ -727,12 +741,14 @@ static int force_one(const cmag_sph_params *p, const float *spos, const float *s
                                 float sv = m * temp * (p->mu + p->mu);
                                 f3 tv = divs3(smul3(sv, vab), rho * rho2 * dist);
                                 tA = add3(tA, tv);
-                                scA = add3(scA, muls3(add3(abs3(vi), abs3(vj)), fabsf(sv) / (rho * rho2 * dist)));
+                                scA = add3(scA, muls3(add3(abs3(vi), abs3(vj)),
+                                                      fabsf(sv) * kernel_dw_cond(p, q) / (rho * rho2 * dist)));
                                 /* pressure, PeristalsisPressureForce.cu:39-43 */
                                 float sp = -1.0f * m * temp * (pr / powf(rho, 2) + pr2 / powf(rho2, 2));
                                 f3 tp = smul3(sp, normalize3(rp));
                                 tB = add3(tB, tp);
-                                float pm = m * fabsf(temp) * (fabsf(pr) / powf(rho, 2) + fabsf(pr2) / powf(rho2, 2));
+                                float pm = m * fabsf(temp) * kernel_dw_cond(p, q) *
+                                           (fabsf(pr) / powf(rho, 2) + fabsf(pr2) / powf(rho2, 2));
                                 scB = add3(scB, muls3(abs3(rp), pm / dist));
                             }
                         }
