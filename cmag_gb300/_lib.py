@@ -68,6 +68,9 @@ SIGNATURES = {
     "cmag_system_set_stage_timing": ([c_sys, ctypes.c_int32], ctypes.c_int),
     "cmag_system_stage_times": ([c_sys, c_f32p, c_u32p], ctypes.c_int),
     "cmag_sort_particles": ([c_u32p, c_u32p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_void_p], ctypes.c_int),
+    "cmag_sort_particles_noalloc": ([c_u32p, c_u32p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_void_p],
+                                    ctypes.c_int),
+    "cmag_sort_particles_noalloc_error": ([], ctypes.c_char_p),
 }
 
 

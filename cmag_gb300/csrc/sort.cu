@@ -16,6 +16,10 @@
 // CMAG_DEVERR_LOOKBACK_TIMEOUT, treats the missing count as zero and finishes.
 #include <cuda_runtime.h>
 
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+
 #include "kernels.h"
 
 namespace cmag {
@@ -223,3 +227,111 @@ void launch_onesweep_pass(const uint32_t *kin, const uint32_t *vin, uint32_t *ko
 }
 
 }  // namespace cmag
+
+// ---------------------------------------------------------------------------
+// Sort without any allocation: fixed scratch in device memory of this library.
+//
+// Some callers cannot call cudaMalloc at the moment they need the sort: code
+// that runs between the begin and end of a CUDA stream capture (allocation
+// calls are not capturable), latency-critical loops where an allocation would
+// stall the device, and hosts whose device memory all comes from their own
+// pool.  For them the sort's workspace lives in one file-scope device array,
+// sized for at most kNoAllocMaxKeys keys and held by every GPU that loads this
+// library until the process exits.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr uint32_t kNoAllocMaxKeys = 1u << 20;  // 1,048,576 (hash, index) pairs
+constexpr uint32_t kNoAllocMaxTiles = (kNoAllocMaxKeys + cmag::kSortTile - 1) / cmag::kSortTile;
+// histograms + tile counters + look-back status of up to four passes
+constexpr size_t kNoAllocWsWords = (size_t)cmag::kMaxPasses * cmag::kRadix + cmag::kMaxPasses +
+                                   (size_t)cmag::kMaxPasses * kNoAllocMaxTiles * cmag::kRadix;
+// + error word, then the alternate key and value buffers
+constexpr size_t kNoAllocWords = kNoAllocWsWords + 1 + 2 * (size_t)kNoAllocMaxKeys;
+
+__device__ __align__(256) uint32_t g_noalloc_scratch[kNoAllocWords];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+uint32_t *g_noalloc_ptr[kMaxDevices] = {};
+
+thread_local char g_noalloc_msg[256];
+
+int noalloc_fail(int code, const char *msg, cudaError_t e = cudaSuccess)
+{
+    if (e != cudaSuccess)
+        std::snprintf(g_noalloc_msg, sizeof(g_noalloc_msg), "%s: %s", msg, cudaGetErrorString(e));
+    else
+        std::snprintf(g_noalloc_msg, sizeof(g_noalloc_msg), "%s", msg);
+    return code;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *cmag_sort_particles_noalloc_error(void) { return g_noalloc_msg; }
+
+int cmag_sort_particles_noalloc(uint32_t *d_hash, uint32_t *d_index, uint32_t n, uint32_t key_bits,
+                                void *cuda_stream)
+{
+    using namespace cmag;
+    if (n == 0) return CMAG_OK;
+    if (!d_hash || !d_index) return noalloc_fail(CMAG_ERR_INVALID, "null argument");
+    if (n > kNoAllocMaxKeys)
+        return noalloc_fail(CMAG_ERR_INVALID,
+                            "cmag_sort_particles_noalloc sorts at most 1048576 pairs; use "
+                            "cmag_sort_particles for more");
+    if (key_bits > 32) return noalloc_fail(CMAG_ERR_INVALID, "key_bits must be at most 32");
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return noalloc_fail(CMAG_ERR_CUDA, "cudaGetDevice", e);
+    if (dev < 0 || dev >= kMaxDevices) return noalloc_fail(CMAG_ERR_INVALID, "device ordinal out of range");
+    uint32_t *base;
+    {
+        // once per device, with that device current: the device address of the
+        // scratch array (the host-side symbol is not a device address)
+        std::lock_guard<std::mutex> lock(g_noalloc_mu);
+        if (!g_noalloc_ptr[dev]) {
+            void *ptr = nullptr;
+            e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+            if (e != cudaSuccess || !ptr)
+                return noalloc_fail(CMAG_ERR_CUDA, "cudaGetSymbolAddress(scratch)", e);
+            g_noalloc_ptr[dev] = static_cast<uint32_t *>(ptr);
+        }
+        base = g_noalloc_ptr[dev];
+    }
+    cudaStream_t st = (cudaStream_t)cuda_stream;
+    int passes = sort_passes(key_bits);
+    if (passes < 1) passes = 1;
+    // the scratch keeps the previous call's contents: clear the counters and the
+    // look-back status this call reads, and the error word
+    const size_t clear_words = sort_workspace_words(n, passes);
+    uint32_t *err = base + kNoAllocWsWords;
+    uint32_t *alt_keys = err + 1, *alt_vals = alt_keys + kNoAllocMaxKeys;
+    e = cudaMemsetAsync(base, 0, clear_words * sizeof(uint32_t), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(err, 0, sizeof(uint32_t), st);
+    if (e != cudaSuccess) return noalloc_fail(CMAG_ERR_CUDA, "cudaMemsetAsync", e);
+    SortWorkspace sw = sort_workspace_view(base, n);
+    launch_digit_hist(d_hash, n, passes, sw.hist, st);
+    uint32_t *kb[2] = {d_hash, alt_keys}, *vb[2] = {d_index, alt_vals};
+    for (int k = 0; k < passes; ++k) {
+        const int src = k & 1, dst = src ^ 1;
+        launch_onesweep_pass(kb[src], vb[src], kb[dst], vb[dst], n, k, false, sw, err, st);
+    }
+    if (passes & 1) {
+        e = cudaMemcpyAsync(d_hash, alt_keys, sizeof(uint32_t) * (size_t)n, cudaMemcpyDeviceToDevice, st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(d_index, alt_vals, sizeof(uint32_t) * (size_t)n, cudaMemcpyDeviceToDevice, st);
+        if (e != cudaSuccess) return noalloc_fail(CMAG_ERR_CUDA, "cudaMemcpyAsync", e);
+    }
+    uint32_t bits = 0;
+    e = cudaMemcpyAsync(&bits, err, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) return noalloc_fail(CMAG_ERR_CUDA, "sort", e);
+    if (bits) return noalloc_fail(CMAG_ERR_DEVICE, "sort look-back spin limit reached");
+    return CMAG_OK;
+}
+
+}  // extern "C"

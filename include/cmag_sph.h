@@ -312,6 +312,26 @@ const char *cmag_last_error(void);
 int cmag_sort_particles(uint32_t *d_hash, uint32_t *d_index, uint32_t n, uint32_t key_bits,
                         void *cuda_stream);
 
+/* The same stable sort without allocating anything, for callers that cannot call
+ * cudaMalloc where they sort: inside a CUDA stream capture (allocation is not
+ * capturable), in latency-critical loops where an allocation would stall the
+ * device, or in hosts whose device memory all comes from their own pool.  No
+ * counterpart in the reference (its thrust::sort_by_key allocates temporaries).
+ *  - Works on at most 1,048,576 pairs; larger n returns CMAG_ERR_INVALID.
+ *  - Its workspace (about 9.3 MB: look-back status and alternate key/value
+ *    buffers) is a fixed device array inside this library, held by every GPU that
+ *    loads the library until the process exits; no cudaMalloc/cudaFree is called.
+ *  - The first call on each device looks up that array's device address
+ *    (cudaGetSymbolAddress) with the device current; make that first call before
+ *    any stream capture.
+ *  - Every call shares the one array: calls whose work overlaps on the GPU (other
+ *    streams, other threads) race and must be serialised by the caller.
+ *  - Like cmag_sort_particles it waits for the stream before returning, to report
+ *    a failed device-side check; messages: cmag_sort_particles_noalloc_error(). */
+int cmag_sort_particles_noalloc(uint32_t *d_hash, uint32_t *d_index, uint32_t n,
+                                uint32_t key_bits, void *cuda_stream);
+const char *cmag_sort_particles_noalloc_error(void);
+
 /* Library version string. */
 const char *cmag_version(void);
 /* sizeof(cmag_sph_params) as compiled into the library (for FFI layout checks). */
