@@ -57,6 +57,8 @@ SIGNATURES = {
     "cmag_system_set_elapsed_time": ([c_sys, ctypes.c_float], ctypes.c_int),
     "cmag_peristalsis_set_phase": ([c_sys, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                                     ctypes.c_int32], ctypes.c_int),
+    "cmag_system_fluid_extent": ([c_sys, c_f32p, c_f32p], ctypes.c_int),
+    "cmag_system_fluid_sum": ([c_sys, ctypes.c_int32, P(ctypes.c_double), c_u32p], ctypes.c_int),
     "cmag_system_set_stream": ([c_sys, ctypes.c_void_p], ctypes.c_int),
     "cmag_system_stream": ([c_sys], ctypes.c_void_p),
     "cmag_system_set_graphs": ([c_sys, ctypes.c_int32], ctypes.c_int),

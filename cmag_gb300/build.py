@@ -11,7 +11,8 @@ SRC = os.path.join(PKG, "csrc")
 OUT_DIR = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libcmag_sph.so")
 
-SOURCES = ["sort.cu", "cells.cu", "neighbors.cu", "integrate.cu", "system.cu", "host_scenes.cpp"]
+SOURCES = ["sort.cu", "cells.cu", "neighbors.cu", "integrate.cu", "reduce.cu", "system.cu",
+           "host_scenes.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # host code: no fused multiply-add, so host float arithmetic (parameters, scenes,
 # phase mirror) matches the reference expressions on x86_64 and aarch64 alike
@@ -51,6 +52,23 @@ def build(verbose=False, extra=()):
         raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), out.stderr))
     os.replace(tmp, LIB)
     return LIB
+
+
+HARNESS = os.path.join(OUT_DIR, "report")
+
+
+def build_harness():
+    """The ported Report programs (host C++ on include/cmag/systems.hpp)."""
+    os.makedirs(OUT_DIR, exist_ok=True)
+    root = os.path.dirname(PKG)
+    cuda = os.path.dirname(os.path.dirname(nvcc()))
+    cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-I" + os.path.join(root, "include"),
+           "-I" + os.path.join(cuda, "include"), os.path.join(PKG, "harness", "report.cpp"),
+           "-L" + PKG, "-lcmag_sph", "-Wl,-rpath," + PKG, "-o", HARNESS]
+    out = subprocess.run(cmd, capture_output=True, text=True)
+    if out.returncode != 0:
+        raise RuntimeError("harness build failed:\n%s\n%s" % (" ".join(cmd), out.stderr))
+    return HARNESS
 
 
 def stale():

@@ -75,4 +75,11 @@ void launch_integrate(const DevParams &p, float4 *pos, float4 *vel, float4 *vlf,
 void launch_gate(const DevParams &p, float4 *pos, int remove, float dx, float fx, float fy,
                  cudaStream_t st);
 
+// ---- reductions over fluid particles (reduce.cu) -------------------------------
+// out6: order-preserving keys of min x,y,z then max x,y,z (init 0xffffffff, 0)
+void launch_fluid_extent(int32_t system, const float4 *pos, uint32_t n, uint32_t *out6,
+                         cudaStream_t st);
+void launch_fluid_sum(int32_t system, const float4 *type_src, const float4 *a, uint32_t n,
+                      double *sums4, unsigned long long *count, cudaStream_t st);
+
 }  // namespace cmag

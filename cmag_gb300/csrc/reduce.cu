@@ -1,0 +1,94 @@
+// reduce.cu -- device reductions over the fluid particles (front, height,
+// averages), replacing the Report harnesses' host-side work:
+//   XFrontTest.h:75-86 / YFrontTest.h:79-90: D2H copy + host thrust::sort for
+//     the largest x / y of a fluid particle;
+//   density.h:51-67, forces.h:56-82: D2H copies + host loops averaging density
+//     and forces over fluid particles.
+#include <cuda_runtime.h>
+
+#include "kernels.h"
+
+namespace cmag {
+
+namespace {
+
+__device__ __forceinline__ bool is_fluid(int32_t system, float w)
+{
+    return system == CMAG_DAMBREAK ? w == (float)CMAG_FLUID : w == 0.0f;
+}
+
+// order-preserving float <-> uint mapping for atomicMin/atomicMax
+__device__ __forceinline__ uint32_t fkey(float f)
+{
+    uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+// out[0..2] min keys, out[3..5] max keys (initialised to 0xffffffff / 0)
+__global__ void __launch_bounds__(256) k_extent(int32_t system, const float4 *__restrict__ pos,
+                                                uint32_t n, uint32_t *out)
+{
+    float lo[3] = {3.4e38f, 3.4e38f, 3.4e38f}, hi[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float4 q = pos[i];
+        if (!is_fluid(system, q.w)) continue;
+        lo[0] = fminf(lo[0], q.x); lo[1] = fminf(lo[1], q.y); lo[2] = fminf(lo[2], q.z);
+        hi[0] = fmaxf(hi[0], q.x); hi[1] = fmaxf(hi[1], q.y); hi[2] = fmaxf(hi[2], q.z);
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+        for (int o = 16; o > 0; o >>= 1) {
+            lo[k] = fminf(lo[k], __shfl_xor_sync(0xffffffffu, lo[k], o));
+            hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xffffffffu, hi[k], o));
+        }
+    if ((threadIdx.x & 31) == 0)
+        for (int k = 0; k < 3; ++k) {
+            atomicMin(&out[k], fkey(lo[k]));
+            atomicMax(&out[3 + k], fkey(hi[k]));
+        }
+}
+
+// sums[0..3] (double) and the count of fluid particles
+__global__ void __launch_bounds__(256) k_fluid_sum(int32_t system, const float4 *__restrict__ type_src,
+                                                   const float4 *__restrict__ a, uint32_t n,
+                                                   double *sums, unsigned long long *count)
+{
+    double s[4] = {0, 0, 0, 0};
+    unsigned long long c = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (!is_fluid(system, type_src[i].w)) continue;
+        float4 v = a[i];
+        s[0] += v.x; s[1] += v.y; s[2] += v.z; s[3] += v.w;
+        ++c;
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        for (int o = 16; o > 0; o >>= 1) s[k] += __shfl_xor_sync(0xffffffffu, s[k], o);
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0) {
+        for (int k = 0; k < 4; ++k) atomicAdd(&sums[k], s[k]);
+        atomicAdd(count, c);
+    }
+}
+
+uint32_t blocks_for(uint32_t n)
+{
+    uint32_t b = (n + 255) / 256;
+    return b < 1 ? 1 : (b > 1216 ? 1216 : b);
+}
+
+}  // namespace
+
+void launch_fluid_extent(int32_t system, const float4 *pos, uint32_t n, uint32_t *out6,
+                         cudaStream_t st)
+{
+    k_extent<<<blocks_for(n), 256, 0, st>>>(system, pos, n, out6);
+}
+
+void launch_fluid_sum(int32_t system, const float4 *type_src, const float4 *a, uint32_t n,
+                      double *sums4, unsigned long long *count, cudaStream_t st)
+{
+    k_fluid_sum<<<blocks_for(n), 256, 0, st>>>(system, type_src, a, n, sums4, count);
+}
+
+}  // namespace cmag

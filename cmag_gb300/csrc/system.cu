@@ -40,6 +40,7 @@ struct cmag_system {
     uint32_t *err = nullptr;
     PhaseState *phase = nullptr;
     uint32_t *view_cs = nullptr, *view_ce = nullptr;
+    uint32_t *red = nullptr;  // reduction results: 6 extent keys, pad, 4 doubles, 1 count
 
     // host mirrors of device-side scalars
     float elapsed = 0.0f;
@@ -409,7 +410,7 @@ void free_all(cmag_system *s)
     s->events.clear();
     void *ptrs[] = {s->pos, s->vel, s->vlf, s->meas, s->acc, s->vforce, s->pforce, s->pred,
                     s->spos, s->svel, s->hash[0], s->hash[1], s->idx[0], s->idx[1], s->cnt,
-                    s->off, s->aux, s->ws, s->err, s->phase, s->view_cs, s->view_ce};
+                    s->off, s->aux, s->ws, s->err, s->phase, s->view_cs, s->view_ce, s->red};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (s->own_stream) cudaStreamDestroy(s->own_stream);
@@ -585,6 +586,7 @@ int cmag_system_create(const cmag_sph_params *params, uint32_t n, cmag_system **
     step(dalloc(s, &s->ws, sizeof(uint32_t) * s->ws_words));
     step(dalloc(s, &s->err, sizeof(uint32_t)));
     step(dalloc(s, &s->phase, sizeof(PhaseState)));
+    step(dalloc(s, &s->red, 64));
     if (rc != CMAG_OK) {
         std::string msg = s->last_error;
         free_all(s);
@@ -910,6 +912,51 @@ int cmag_peristalsis_phase(const cmag_system *s, float *wave_height, float *time
     if (time_relax) *time_relax = s->host_phase.time_relax;
     if (time_shift) *time_shift = s->host_phase.time_shift;
     if (is_bc) *is_bc = s->host_phase.is_bc;
+    return CMAG_OK;
+}
+
+int cmag_system_fluid_extent(cmag_system *s, float lo[3], float hi[3])
+{
+    if (!s || !lo || !hi) return fail(s, CMAG_ERR_INVALID, "null argument");
+    cudaStream_t st = st_of(s);
+    CM_CUDA(s, cudaMemsetAsync(s->red, 0xff, 3 * sizeof(uint32_t), st));
+    CM_CUDA(s, cudaMemsetAsync(s->red + 3, 0, 3 * sizeof(uint32_t), st));
+    launch_fluid_extent(s->p.system, s->pos, s->n, s->red, st);
+    uint32_t keys[6];
+    CM_CUDA(s, cudaMemcpyAsync(keys, s->red, sizeof(keys), cudaMemcpyDeviceToHost, st));
+    CM_CUDA(s, cudaStreamSynchronize(st));
+    auto back = [](uint32_t k) {
+        uint32_t u = (k & 0x80000000u) ? (k & 0x7fffffffu) : ~k;
+        float f;
+        std::memcpy(&f, &u, sizeof(f));
+        return f;
+    };
+    for (int k = 0; k < 3; ++k) {
+        lo[k] = back(keys[k]);
+        hi[k] = back(keys[3 + k]);
+    }
+    return CMAG_OK;
+}
+
+int cmag_system_fluid_sum(cmag_system *s, int32_t array, double sum[4], uint32_t *count)
+{
+    if (!s || !sum) return fail(s, CMAG_ERR_INVALID, "null argument");
+    float4 *a = float_array(s, array);
+    if (!a) return fail(s, CMAG_ERR_INVALID, "not a float4 array: " + std::to_string(array));
+    const bool sorted = array == CMAG_MEASURES || array == CMAG_SORTEDPOSITION ||
+                        array == CMAG_SORTEDVELOCITY;
+    cudaStream_t st = st_of(s);
+    double *sums = reinterpret_cast<double *>(s->red + 8);
+    unsigned long long *cnt = reinterpret_cast<unsigned long long *>(s->red + 8 + 8);
+    CM_CUDA(s, cudaMemsetAsync(sums, 0, 4 * sizeof(double) + sizeof(unsigned long long), st));
+    launch_fluid_sum(s->p.system, sorted ? s->spos : s->pos, a, s->n, sums, cnt, st);
+    double h[4];
+    unsigned long long c = 0;
+    CM_CUDA(s, cudaMemcpyAsync(h, sums, sizeof(h), cudaMemcpyDeviceToHost, st));
+    CM_CUDA(s, cudaMemcpyAsync(&c, cnt, sizeof(c), cudaMemcpyDeviceToHost, st));
+    CM_CUDA(s, cudaStreamSynchronize(st));
+    for (int k = 0; k < 4; ++k) sum[k] = h[k];
+    if (count) *count = (uint32_t)c;
     return CMAG_OK;
 }
 

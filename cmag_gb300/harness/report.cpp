@@ -1,0 +1,186 @@
+// report.cpp -- the reference's headless Report programs, on the drop-in classes.
+//
+//   report xfront  [dir]     DamBreak.Report/XFrontTest.h:16-90   -> XFrontOutput
+//   report yfront  [dir]     DamBreak.Report/YFrontTest.h:16-94   -> YFrontOutput
+//   report poiseuille [dir]  Poiseuille.Report/dump.h:15-86      -> XVelocityYPosition<t>.dat
+//   report density [dir] [T] Peristalsis.Report/density.h:12-70  -> density.dat
+//   report forces  [dir] [T] Peristalsis.Report/forces.h:13-88   -> press_{x,y}.dat, visc_{x,y}.dat
+//
+// Same scenes, time frames and output formats as the reference.  The front,
+// height and per-step averages come from device reductions over the fluid
+// particles instead of copying every particle to the host and sorting there.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <cmag/systems.hpp>
+
+namespace {
+
+std::string path(const std::string &dir, const std::string &name) { return dir + "/" + name; }
+
+// XFrontTest.h:45-62 (dimensionless time, surge front), Martin & Moyce table 2
+const float kXFront[][2] = {{0.00f, 1.0f},  {0.41f, 1.11f}, {0.84f, 1.22f}, {1.19f, 1.44f},
+                            {1.43f, 1.67f}, {1.63f, 1.89f}, {1.83f, 2.11f}, {1.98f, 2.33f},
+                            {2.20f, 2.56f}, {2.32f, 2.78f}, {2.51f, 3.00f}, {2.65f, 3.22f},
+                            {2.83f, 3.44f}, {2.97f, 3.67f}, {3.11f, 3.89f}};
+// YFrontTest.h:136-153 (dimensionless time, column height), table 6
+const float kYFront[][2] = {{0.0f, 1.0f},   {0.56f, 0.94f}, {0.77f, 0.89f}, {0.93f, 0.83f},
+                            {1.08f, 0.78f}, {1.28f, 0.72f}, {1.46f, 0.67f}, {1.66f, 0.61f},
+                            {1.84f, 0.56f}, {2.00f, 0.50f}, {2.21f, 0.44f}, {2.45f, 0.39f},
+                            {2.70f, 0.33f}, {3.06f, 0.28f}, {3.44f, 0.22f}};
+
+DamBreakSystem *relaxed_column()
+{
+    const int num = 128;
+    const float radius = 1.0f / (2 * num);
+    DamBreakSystem *s = new DamBreakSystem(make_uint3(num, 2 * num, 1), 1, make_uint3(512, 256, 4),
+                                           radius, false);
+    s->reset();
+    while (s->getElapsedTime() < 1.5f) s->update();  // relax
+    std::printf("relaxed at t = %f\n", s->getElapsedTime());
+    s->removeRightBoundary();
+    return s;
+}
+
+int xfront(const std::string &dir)
+{
+    const int num = 128, off = 1;
+    const float radius = 1.0f / (2 * num);
+    DamBreakSystem *s = relaxed_column();
+    const float xwidth = (num + off) * 2 * radius;
+    const float scale = std::sqrt(2 * std::fabs(s->getGravity().y) / xwidth);
+    FILE *f = std::fopen(path(dir, "XFrontOutput").c_str(), "w");
+    for (const auto &fr : kXFront) {
+        while (s->getElapsedTime() * scale < fr[0]) s->update();
+        const float x = s->fluidMax().x;
+        std::fprintf(f, "%f %f %f %f \n", fr[0], s->getElapsedTime(), fr[1],
+                     (x + radius - s->getWorldOrigin().x) / xwidth);
+    }
+    std::fclose(f);
+    delete s;
+    return 0;
+}
+
+int yfront(const std::string &dir)
+{
+    const int num = 128;
+    const float radius = 1.0f / (2 * num);
+    DamBreakSystem *s = relaxed_column();
+    const float yheight = s->fluidMax().y + radius - s->getWorldOrigin().y;
+    const float scale = std::sqrt(2 * std::fabs(s->getGravity().y) / yheight);
+    FILE *f = std::fopen(path(dir, "YFrontOutput").c_str(), "w");
+    for (const auto &fr : kYFront) {
+        while (s->getElapsedTime() * scale < fr[0]) s->update();
+        const float y = s->fluidMax().y;
+        std::fprintf(f, "%f %f %f %f \n", fr[0], s->getElapsedTime(), fr[1],
+                     (y + radius - s->getWorldOrigin().y) / yheight);
+    }
+    std::fclose(f);
+    delete s;
+    return 0;
+}
+
+int poiseuille(const std::string &dir)
+{
+    const int off = 3;
+    const uint3 grid = make_uint3(16, 64, 4);
+    const float radius = 1.0f / (2 * (grid.y - 2 * off) * 1000);
+    PoiseuilleFlowSystem s(make_uint3(grid.x, grid.y - 2 * off, 1), off, grid, radius, false);
+    s.reset();
+    const int n = s.getNumParticles();
+    std::vector<float> pos(4 * (size_t)n), vel(4 * (size_t)n);
+    const float frames[] = {0.0225f, 0.045f, 0.1125f, 0.225f, 1.0f};
+    for (float t : frames) {
+        while (s.getElapsedTime() < t) s.update();
+        s.getArray(CMAG_POSITION, pos.data(), 0, n);
+        s.getArray(CMAG_VELOCITY, vel.data(), 0, n);
+        char name[64];
+        std::snprintf(name, sizeof(name), "XVelocityYPosition%g.dat", t);
+        FILE *f = std::fopen(path(dir, name).c_str(), "w");
+        std::fprintf(f, "0.0 0.0\n");
+        for (int i = 0; i < n; ++i) {
+            const float *p = &pos[4 * (size_t)i];
+            if (p[0] > 0 && p[0] < 2 * radius && p[3] == 0.0f)
+                std::fprintf(f, "%g %g\n", vel[4 * (size_t)i],
+                             p[1] + std::fabs(s.getWorldOrigin().y) - off * 2 * radius);
+        }
+        std::fprintf(f, "0.000000 0.001000\n");
+        std::fclose(f);
+    }
+    return 0;
+}
+
+PeristalsisSystem *channel()
+{
+    const int off = 3;
+    const float c = std::pow(10.0f, -4.0f);
+    const float radius = 1.0f / (2 * (64 - 6) * 1000);
+    return new PeristalsisSystem(std::pow(10.0f, -4.0f), make_uint3(256, 64 - 2 * off, 1),
+                                 0.6f * 35 * radius, 100 * c, c, make_float3(0, 0, 0), off,
+                                 make_uint3(256, 128, 4), radius, false);
+}
+
+int density(const std::string &dir, float until)
+{
+    PeristalsisSystem *s = channel();
+    s->Reset();
+    const uint32_t fluid = 256 * 58;
+    FILE *f = std::fopen(path(dir, "density.dat").c_str(), "w");
+    while (s->GetElapsedTime() < until) {
+        s->Update();
+        std::fprintf(f, "%g %g\n", s->GetElapsedTime(), s->fluidAverage(CMAG_MEASURES, fluid).x);
+    }
+    std::fclose(f);
+    delete s;
+    return 0;
+}
+
+int forces(const std::string &dir, float until)
+{
+    PeristalsisSystem *s = channel();
+    s->Reset();
+    const uint32_t fluid = 256 * 58;
+    const char *names[4] = {"press_x.dat", "press_y.dat", "visc_x.dat", "visc_y.dat"};
+    FILE *f[4];
+    for (int k = 0; k < 4; ++k) f[k] = std::fopen(path(dir, names[k]).c_str(), "w");
+    while (s->GetElapsedTime() < until) {
+        s->Update();
+        const float4 pr = s->fluidAverage(CMAG_PRESSUREFORCE, fluid);
+        const float4 vi = s->fluidAverage(CMAG_VISCOUSFORCE, fluid);
+        const float t = s->GetElapsedTime();
+        std::fprintf(f[0], "%g %g\n", t, pr.x);
+        std::fprintf(f[1], "%g %g\n", t, pr.y);
+        std::fprintf(f[2], "%g %g\n", t, vi.x);
+        std::fprintf(f[3], "%g %g\n", t, vi.y);
+    }
+    for (int k = 0; k < 4; ++k) std::fclose(f[k]);
+    delete s;
+    return 0;
+}
+
+}  // namespace
+
+int main(int argc, char **argv)
+{
+    if (argc < 2) {
+        std::fprintf(stderr, "usage: report xfront|yfront|poiseuille|density|forces [dir] [until]\n");
+        return 2;
+    }
+    const std::string what = argv[1], dir = argc > 2 ? argv[2] : ".";
+    const float until = argc > 3 ? (float)std::atof(argv[3]) : 1.0f;
+    try {
+        if (what == "xfront") return xfront(dir);
+        if (what == "yfront") return yfront(dir);
+        if (what == "poiseuille") return poiseuille(dir);
+        if (what == "density") return density(dir, until);
+        if (what == "forces") return forces(dir, until);
+    } catch (const cmag::Error &e) {
+        std::fprintf(stderr, "cmag error %d: %s\n", e.code, e.what());
+        return 1;
+    }
+    std::fprintf(stderr, "unknown report %s\n", what.c_str());
+    return 2;
+}

@@ -212,6 +212,19 @@ class _System:
         self._chk(lib().cmag_system_stage_times(self._h, ms, ctypes.byref(steps)))
         return list(ms), steps.value
 
+    def fluid_extent(self):
+        """(min xyz, max xyz) over fluid particles, reduced on the device."""
+        lo, hi = (ctypes.c_float * 3)(), (ctypes.c_float * 3)()
+        self._chk(lib().cmag_system_fluid_extent(self._h, lo, hi))
+        return tuple(lo), tuple(hi)
+
+    def fluid_sum(self, array):
+        """(sum of the float4 components over fluid particles, fluid count)."""
+        s = (ctypes.c_double * 4)()
+        c = ctypes.c_uint32()
+        self._chk(lib().cmag_system_fluid_sum(self._h, int(array), s, ctypes.byref(c)))
+        return tuple(s), c.value
+
     def set_elapsed_time(self, t):
         self._chk(lib().cmag_system_set_elapsed_time(self._h, float(t)))
 

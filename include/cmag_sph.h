@@ -274,6 +274,16 @@ int cmag_system_set_elapsed_time(cmag_system *s, float elapsed);
 int cmag_peristalsis_set_phase(cmag_system *s, float current_wave_height, float time_relax,
                                float time_shift, int32_t is_boundary_configuration);
 
+/* Device reductions over the fluid particles (DamBreak type CMAG_FLUID, the other
+ * families type 0), replacing the Report harnesses' host-side sorts and loops:
+ * the surge front and column height (XFrontTest.h:75-86, YFrontTest.h:79-90) are
+ * hi[0] and hi[1] of cmag_system_fluid_extent; the per-step averages of density.h
+ * (:51-67) and forces.h (:56-82) are cmag_system_fluid_sum / count.
+ * fluid_sum accepts any float4 array; sorted-order arrays (MEASURES, SORTED*)
+ * take the particle type from the sorted positions, the others from POSITION. */
+int cmag_system_fluid_extent(cmag_system *s, float lo[3], float hi[3]);
+int cmag_system_fluid_sum(cmag_system *s, int32_t array, double sum[4], uint32_t *count);
+
 /* Use a caller-owned cudaStream_t (NULL = the instance's own stream). */
 int cmag_system_set_stream(cmag_system *s, void *cuda_stream);
 void *cmag_system_stream(const cmag_system *s);

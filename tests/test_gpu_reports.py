@@ -1,0 +1,101 @@
+"""The ported Report programs (cmag_gb300/harness/report.cpp, on the C++ drop-in
+classes) and the device reductions they use.
+
+* Poiseuille.Report/dump.h: u_x(y) at t = 0.0225 ... 1 s against the analytic
+  transient series the reference plots it against (Poiseuille.Report/
+  XVelocityYPosition.m:10-12: F = 1e-4, l = 1e-3, nu = 1e-6, 101 terms).
+* DamBreak.Report/XFrontTest.h, YFrontTest.h: surge front and column height against
+  the Martin & Moyce tables the reference prints beside them (a sanity band: a 2-D
+  SPH column is not the experiment).
+* Peristalsis.Report/density.h, forces.h: per-step averages over fluid particles.
+"""
+import math
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import cmag_gb300 as cm
+from cmag_gb300 import build as B
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def harness(gpu):
+    if not os.path.exists(B.HARNESS) or os.path.getmtime(B.HARNESS) < os.path.getmtime(B.LIB):
+        B.build_harness()
+    return B.HARNESS
+
+
+def run(harness, what, tmp_path, *extra):
+    out = subprocess.run([harness, what, str(tmp_path)] + [str(e) for e in extra],
+                         capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr + out.stdout
+    return out.stdout
+
+
+def poiseuille_series(y, t, F=1e-4, l=1e-3, nu=1e-6, terms=101):
+    """-Vel(y, t) of XVelocityYPosition.m:12."""
+    v = F * y * (y - l) / (2 * nu)
+    for n in range(terms):
+        k = 2 * n + 1
+        v = v + 4 * F * l ** 2 * np.sin(math.pi * y * k / l) * np.exp(-k * k * math.pi ** 2 * nu * t / l ** 2) \
+            / (nu * math.pi ** 3 * k ** 3)
+    return -v
+
+
+def test_poiseuille_profile_matches_analytic_series(harness, tmp_path):
+    run(harness, "poiseuille", tmp_path)
+    errs = {}
+    for t in (0.0225, 0.045, 0.1125, 0.225, 1.0):
+        d = np.loadtxt(tmp_path / ("XVelocityYPosition%g.dat" % t))[1:-1]
+        u, y = d[:, 0], d[:, 1]
+        exact = poiseuille_series(y, t)
+        errs[t] = float(np.abs(u - exact).max() / np.abs(exact).max())
+    print("max |u - series| / max|series| per time:", errs)
+    assert all(e < 0.05 for e in errs.values()), errs
+
+
+def test_dambreak_front_and_height(harness, tmp_path):
+    run(harness, "xfront", tmp_path)
+    run(harness, "yfront", tmp_path)
+    x = np.loadtxt(tmp_path / "XFrontOutput")
+    y = np.loadtxt(tmp_path / "YFrontOutput")
+    # columns: T* experiment, t, experiment value, simulated value
+    assert np.all(np.diff(x[:, 3]) >= -1e-3), "front must advance"
+    assert np.all(np.diff(y[:, 3]) <= 1e-3), "column must fall"
+    assert abs(x[0, 3] - 1.0) < 0.03 and abs(y[0, 3] - 1.0) < 1e-6
+    rel_x = np.abs(x[:, 3] - x[:, 2]) / x[:, 2]
+    rel_y = np.abs(y[:, 3] - y[:, 2]) / y[:, 2]
+    print("front vs Martin & Moyce:", np.round(rel_x, 3), "height:", np.round(rel_y, 3))
+    assert rel_x.max() < 0.35 and rel_y.max() < 0.35
+
+
+def test_peristalsis_averages(harness, tmp_path):
+    run(harness, "density", tmp_path, 0.25)
+    run(harness, "forces", tmp_path, 0.02)
+    d = np.loadtxt(tmp_path / "density.dat")
+    assert d.shape[0] > 2000
+    assert np.all(np.abs(d[:, 1] - 1000.0) < 60.0), (d[:, 1].min(), d[:, 1].max())
+    for name in ("press_x", "press_y", "visc_x", "visc_y"):
+        f = np.loadtxt(tmp_path / (name + ".dat"))
+        assert np.all(np.isfinite(f[:, 1]))
+
+
+def test_fluid_reductions_match_host(gpu):
+    s = cm.DamBreakSystem((32, 64, 1), 1, (128, 64, 4), 1.0 / 256)
+    s.reset()
+    s.update_n(20)
+    pos = s.getArray(cm.POSITION)
+    fluid = pos[:, 3] == cm.FLUID
+    lo, hi = s.fluid_extent()
+    assert np.allclose(lo, pos[fluid, :3].min(axis=0)) and np.allclose(hi, pos[fluid, :3].max(axis=0))
+    spos = s.getArray(cm.SORTEDPOSITION)
+    meas = s.getArray(cm.MEASURES)
+    sums, count = s.fluid_sum(cm.MEASURES)
+    sel = spos[:, 3] == cm.FLUID
+    assert count == sel.sum() == 32 * 64
+    assert np.allclose(sums[:2], meas[sel, :2].astype(np.float64).sum(axis=0), rtol=1e-9)
+    s.close()
