@@ -135,6 +135,17 @@ __device__ __forceinline__ void for_each_candidate(const DevParams &p,
     }
 }
 
+// Relative position of candidate j seen through its image shift.  Only the
+// families with periodic images add the shift (DamBreak none, Poiseuille x only);
+// the compiler cannot drop an added 0.0f by itself (signed zeros).
+template <int SYS>
+__device__ __forceinline__ float3 rel(float4 pi, float4 pj, float sx, float sy, float sz)
+{
+    if (SYS == CMAG_DAMBREAK) return make_float3(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z);
+    if (SYS == CMAG_POISEUILLE) return make_float3(pi.x - (pj.x + sx), pi.y - pj.y, pi.z - pj.z);
+    return make_float3(pi.x - (pj.x + sx), pi.y - (pj.y + sy), pi.z - (pj.z + sz));
+}
+
 template <int G>
 __device__ __forceinline__ float group_sum(float v)
 {
@@ -167,9 +178,8 @@ __global__ void __launch_bounds__(256, 6)
         const int3 g = grid_pos(p, pi.x, pi.y, pi.z);
         for_each_candidate<SYS, PLANAR, TRIM, G>(
             p, off, lane, g, frac_cell(p, pi), [&](uint32_t j, float sx, float sy, float sz) {
-                const float4 pj = __ldg(spos + j);
-                const float rx = pi.x - (pj.x + sx), ry = pi.y - (pj.y + sy), rz = pi.z - (pj.z + sz);
-                const float d2 = rx * rx + ry * ry + rz * rz;
+                const float3 r = rel<SYS>(pi, __ldg(spos + j), sx, sy, sz);
+                const float d2 = r.x * r.x + r.y * r.y + r.z * r.z;
                 if (d2 < p.support2) sum += kernel_w(p, d2 * rsqrtf(fmaxf(d2, 1e-30f)) * p.inv_h);
             });
     }
@@ -215,8 +225,8 @@ __global__ void __launch_bounds__(256, 4)
             p, off, lane, g, frac_cell(p, pi), [&](uint32_t j, float sx, float sy, float sz) {
                 if (j == i) return;
                 const float4 pj = __ldg(spos + j);
-                const float rx = pi.x - (pj.x + sx), ry = pi.y - (pj.y + sy),
-                            rz = pi.z - (pj.z + sz);
+                const float3 rv = rel<SYS>(pi, pj, sx, sy, sz);
+                const float rx = rv.x, ry = rv.y, rz = rv.z;
                 const float d2 = rx * rx + ry * ry + rz * rz;
                 if (SYS == CMAG_DAMBREAK) {
                     if (pj.w != (float)CMAG_FLUID) {
