@@ -124,6 +124,7 @@ __device__ __forceinline__ void for_each_candidate(const DevParams &p,
     for (int r = lane; r < nrows; r += G) {
         RowRuns rr;
         if (row_runs<SYS, PLANAR, TRIM>(p, off, dy, dz, g, f.x, f.y, f.z, rr)) {
+#pragma unroll 2
             for (uint32_t j = rr.b0; j < rr.e0; ++j) visit(j, rr.sx0, rr.sy, rr.sz);
             for (uint32_t j = rr.b1; j < rr.e1; ++j) visit(j, rr.sx1, rr.sy, rr.sz);
         }
@@ -180,7 +181,9 @@ __global__ void __launch_bounds__(256, 6)
             p, off, lane, g, frac_cell(p, pi), [&](uint32_t j, float sx, float sy, float sz) {
                 const float3 r = rel<SYS>(pi, __ldg(spos + j), sx, sy, sz);
                 const float d2 = r.x * r.x + r.y * r.y + r.z * r.z;
-                if (d2 < p.support2) sum += kernel_w(p, d2 * rsqrtf(fmaxf(d2, 1e-30f)) * p.inv_h);
+                // evaluated for every candidate and selected: no divergent branch
+                const float w = kernel_w(p, fminf(d2 * rsqrtf(fmaxf(d2, 1e-30f)) * p.inv_h, 2.0f));
+                sum += (d2 < p.support2) ? w : 0.0f;
             });
     }
     sum = group_sum<G>(sum);

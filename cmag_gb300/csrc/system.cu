@@ -82,12 +82,16 @@ int fail(cmag_system *s, int code, const std::string &msg)
     return code;
 }
 
+// On failure: report, and clear the runtime's (non-sticky) last error so that it
+// does not surface later in an unrelated caller's CUDA call.
 #define CM_CUDA(s, call)                                                                    \
     do {                                                                                    \
         cudaError_t e_ = (call);                                                            \
-        if (e_ != cudaSuccess)                                                              \
+        if (e_ != cudaSuccess) {                                                            \
+            (void)cudaGetLastError();                                                       \
             return fail((s), e_ == cudaErrorMemoryAllocation ? CMAG_ERR_NOMEM : CMAG_ERR_CUDA, \
                         std::string(#call) + ": " + cudaGetErrorString(e_));                \
+        }                                                                                   \
     } while (0)
 
 bool is_pow2(uint32_t v) { return v && !(v & (v - 1)); }
@@ -586,7 +590,8 @@ int cmag_system_create(const cmag_sph_params *params, uint32_t n, cmag_system **
     step(dalloc(s, &s->ws, sizeof(uint32_t) * s->ws_words));
     step(dalloc(s, &s->err, sizeof(uint32_t)));
     step(dalloc(s, &s->phase, sizeof(PhaseState)));
-    step(dalloc(s, &s->red, 64));
+    // 6 extent keys + pad (32 B), 4 doubles (32 B), 1 count (8 B)
+    step(dalloc(s, &s->red, 128));
     if (rc != CMAG_OK) {
         std::string msg = s->last_error;
         free_all(s);
