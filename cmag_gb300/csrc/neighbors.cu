@@ -109,12 +109,11 @@ __device__ __forceinline__ bool row_runs(const DevParams &p, const uint32_t *__r
     return true;
 }
 
-// Calls visit(j, sx, sy, sz) for every candidate of the rows this lane owns
+// Calls visit_run(b, e, sx, sy, sz) for every run of the rows this lane owns
 // (rows r = lane, lane + G, ... of the (2c+1)^2 box, dy fastest).
-template <int SYS, bool PLANAR, bool TRIM, int G, class Visit>
-__device__ __forceinline__ void for_each_candidate(const DevParams &p,
-                                                   const uint32_t *__restrict__ off, int lane,
-                                                   int3 g, float3 f, Visit &&visit)
+template <int SYS, bool PLANAR, bool TRIM, int G, class VisitRun>
+__device__ __forceinline__ void for_each_run(const DevParams &p, const uint32_t *__restrict__ off,
+                                             int lane, int3 g, float3 f, VisitRun &&visit_run)
 {
     const int c = p.cell_count;
     const int w = 2 * c + 1;
@@ -124,9 +123,8 @@ __device__ __forceinline__ void for_each_candidate(const DevParams &p,
     for (int r = lane; r < nrows; r += G) {
         RowRuns rr;
         if (row_runs<SYS, PLANAR, TRIM>(p, off, dy, dz, g, f.x, f.y, f.z, rr)) {
-#pragma unroll 2
-            for (uint32_t j = rr.b0; j < rr.e0; ++j) visit(j, rr.sx0, rr.sy, rr.sz);
-            for (uint32_t j = rr.b1; j < rr.e1; ++j) visit(j, rr.sx1, rr.sy, rr.sz);
+            visit_run(rr.b0, rr.e0, rr.sx0, rr.sy, rr.sz);
+            if (rr.e1 > rr.b1) visit_run(rr.b1, rr.e1, rr.sx1, rr.sy, rr.sz);
         }
         dy += G;
         while (dy > c) {
@@ -134,6 +132,19 @@ __device__ __forceinline__ void for_each_candidate(const DevParams &p,
             ++dz;
         }
     }
+}
+
+// Calls visit(j, sx, sy, sz) for every candidate of the rows this lane owns.
+template <int SYS, bool PLANAR, bool TRIM, int G, class Visit>
+__device__ __forceinline__ void for_each_candidate(const DevParams &p,
+                                                   const uint32_t *__restrict__ off, int lane,
+                                                   int3 g, float3 f, Visit &&visit)
+{
+    for_each_run<SYS, PLANAR, TRIM, G>(p, off, lane, g, f,
+                                       [&](uint32_t b, uint32_t e, float sx, float sy, float sz) {
+#pragma unroll 2
+                                           for (uint32_t j = b; j < e; ++j) visit(j, sx, sy, sz);
+                                       });
 }
 
 // Relative position of candidate j seen through its image shift.  Only the
@@ -145,6 +156,49 @@ __device__ __forceinline__ float3 rel(float4 pi, float4 pj, float sx, float sy, 
     if (SYS == CMAG_DAMBREAK) return make_float3(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z);
     if (SYS == CMAG_POISEUILLE) return make_float3(pi.x - (pj.x + sx), pi.y - pj.y, pi.z - pj.z);
     return make_float3(pi.x - (pj.x + sx), pi.y - (pj.y + sy), pi.z - (pj.z + sz));
+}
+
+// Un-normalised Wendland sum over candidates [b, e) of one run, two candidates
+// per step in paired FP32 (FFMA2/FMUL2/FADD2: two FP32 operations per issued
+// instruction on sm_100+), scalar tail.  Adds (1 - q/2)^4 (2q + 1) for q < 2.
+template <int SYS>
+__device__ __forceinline__ void wendland_run(const DevParams &p, const float4 *__restrict__ spos,
+                                             uint32_t b, uint32_t e, float4 pi, float sx, float sy,
+                                             float sz, float2 &acc)
+{
+    const float2 px = make_float2(pi.x, pi.x), py = make_float2(pi.y, pi.y),
+                 pz = make_float2(pi.z, pi.z);
+    const float2 m1 = make_float2(-1.0f, -1.0f), half = make_float2(-0.5f, -0.5f),
+                 one = make_float2(1.0f, 1.0f), two = make_float2(2.0f, 2.0f),
+                 ih = make_float2(p.inv_h, p.inv_h);
+    uint32_t j = b;
+    for (; j + 1 < e; j += 2) {
+        const float4 a = __ldg(spos + j), c = __ldg(spos + j + 1);
+        float2 ax = make_float2(a.x, c.x), ay = make_float2(a.y, c.y), az = make_float2(a.z, c.z);
+        if (SYS != CMAG_DAMBREAK) ax = __fadd2_rn(ax, make_float2(sx, sx));
+        if (SYS == CMAG_PERISTALSIS) {
+            ay = __fadd2_rn(ay, make_float2(sy, sy));
+            az = __fadd2_rn(az, make_float2(sz, sz));
+        }
+        const float2 rx = __ffma2_rn(ax, m1, px), ry = __ffma2_rn(ay, m1, py), rz = __ffma2_rn(az, m1, pz);
+        const float2 d2 = __ffma2_rn(rz, rz, __ffma2_rn(ry, ry, __fmul2_rn(rx, rx)));
+        const float2 rs = make_float2(rsqrtf(fmaxf(d2.x, 1e-30f)), rsqrtf(fmaxf(d2.y, 1e-30f)));
+        float2 q = __fmul2_rn(__fmul2_rn(d2, rs), ih);
+        q = make_float2(fminf(q.x, 2.0f), fminf(q.y, 2.0f));
+        const float2 t = __ffma2_rn(q, half, one);
+        const float2 t2 = __fmul2_rn(t, t);
+        float2 w = __fmul2_rn(__fmul2_rn(t2, t2), __ffma2_rn(q, two, one));
+        w.x = (d2.x < p.support2) ? w.x : 0.0f;
+        w.y = (d2.y < p.support2) ? w.y : 0.0f;
+        acc = __fadd2_rn(acc, w);
+    }
+    if (j < e) {
+        const float3 r = rel<SYS>(pi, __ldg(spos + j), sx, sy, sz);
+        const float d2 = r.x * r.x + r.y * r.y + r.z * r.z;
+        const float q = fminf(d2 * rsqrtf(fmaxf(d2, 1e-30f)) * p.inv_h, 2.0f);
+        const float t = 1.0f - 0.5f * q, t2 = t * t;
+        acc.x += (d2 < p.support2) ? t2 * t2 * (2.0f * q + 1.0f) : 0.0f;
+    }
 }
 
 template <int G>
@@ -177,14 +231,24 @@ __global__ void __launch_bounds__(256, 6)
     float sum = 0.0f;
     if (active && !pinned) {
         const int3 g = grid_pos(p, pi.x, pi.y, pi.z);
-        for_each_candidate<SYS, PLANAR, TRIM, G>(
-            p, off, lane, g, frac_cell(p, pi), [&](uint32_t j, float sx, float sy, float sz) {
-                const float3 r = rel<SYS>(pi, __ldg(spos + j), sx, sy, sz);
-                const float d2 = r.x * r.x + r.y * r.y + r.z * r.z;
-                // evaluated for every candidate and selected: no divergent branch
-                const float w = kernel_w(p, fminf(d2 * rsqrtf(fmaxf(d2, 1e-30f)) * p.inv_h, 2.0f));
-                sum += (d2 < p.support2) ? w : 0.0f;
-            });
+        if (p.kernel == CMAG_KERNEL_WENDLAND) {
+            float2 acc = make_float2(0.0f, 0.0f);
+            for_each_run<SYS, PLANAR, TRIM, G>(
+                p, off, lane, g, frac_cell(p, pi),
+                [&](uint32_t b, uint32_t e, float sx, float sy, float sz) {
+                    wendland_run<SYS>(p, spos, b, e, pi, sx, sy, sz, acc);
+                });
+            sum = p.w_norm * (acc.x + acc.y);
+        } else {
+            for_each_candidate<SYS, PLANAR, TRIM, G>(
+                p, off, lane, g, frac_cell(p, pi), [&](uint32_t j, float sx, float sy, float sz) {
+                    const float3 r = rel<SYS>(pi, __ldg(spos + j), sx, sy, sz);
+                    const float d2 = r.x * r.x + r.y * r.y + r.z * r.z;
+                    // evaluated for every candidate and selected: no divergent branch
+                    const float w = kernel_w(p, fminf(d2 * rsqrtf(fmaxf(d2, 1e-30f)) * p.inv_h, 2.0f));
+                    sum += (d2 < p.support2) ? w : 0.0f;
+                });
+        }
     }
     sum = group_sum<G>(sum);
     if (active && lane == 0) {
