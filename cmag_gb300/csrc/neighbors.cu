@@ -201,6 +201,103 @@ __device__ __forceinline__ void wendland_run(const DevParams &p, const float4 *_
     }
 }
 
+// One DamBreak candidate pair, scalar: Lennard-Jones from walls
+// (fluid_kernel.cu:199-207), pressure + Monaghan viscosity from fluid
+// (fluid_kernel.cu:221-237).  Adds to a.
+template <bool TRIM>
+__device__ __forceinline__ void dambreak_pair(const DevParams &p, const float4 *__restrict__ svel,
+                                              const float2 *__restrict__ aux, uint32_t j, float4 pj,
+                                              float4 pi, float4 vi, float2 ai, float3 &a)
+{
+    const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
+    const float d2 = rx * rx + ry * ry + rz * rz;
+    if (pj.w != (float)CMAG_FLUID) {
+        if (TRIM && !(d2 < p.support2)) return;
+        const float inv_d2 = __frcp_rn(d2);
+        const float a2 = p.lj_a2 * inv_d2;
+        const float a6 = a2 * a2 * a2;
+        const float s = p.lj_D * (a6 * a6 - a6) * inv_d2;
+        a.x += s * rx; a.y += s * ry; a.z += s * rz;
+        return;
+    }
+    if (!(d2 < p.support2)) return;
+    const float inv_d = rsqrtf(d2);
+    const float temp = kernel_dw(p, d2 * inv_d * p.inv_h);
+    const float2 aj = __ldg(aux + j);
+    float s = ai.x + aj.x;
+    const float4 vj = __ldg(svel + j);
+    const float vij = (vi.x - vj.x) * rx + (vi.y - vj.y) * ry + (vi.z - vj.z) * rz;
+    if (vij < 0.0f) {
+        const float nu = __fdividef(p.av_coeff, ai.y + aj.y);
+        s -= __fdividef(nu * vij, d2 + p.av_eps2);
+    }
+    s *= -p.mass * temp * inv_d;
+    a.x += s * rx; a.y += s * ry; a.z += s * rz;
+}
+
+// DamBreak force over candidates [b, e) of one run (sorted particle i excluded):
+// fluid-fluid pairs two at a time in paired FP32 with selects instead of
+// branches; a step that meets a wall candidate falls back to the scalar path.
+template <bool TRIM>
+__device__ __forceinline__ void dambreak_force_run(const DevParams &p, const float4 *__restrict__ spos,
+                                                   const float4 *__restrict__ svel,
+                                                   const float2 *__restrict__ aux, uint32_t b,
+                                                   uint32_t e, uint32_t i, float4 pi, float4 vi,
+                                                   float2 ai, float3 &a)
+{
+    const float2 px = make_float2(pi.x, pi.x), py = make_float2(pi.y, pi.y),
+                 pz = make_float2(pi.z, pi.z), m1 = make_float2(-1.0f, -1.0f);
+    const float2 vx = make_float2(vi.x, vi.x), vy = make_float2(vi.y, vi.y), vz = make_float2(vi.z, vi.z);
+    const float2 ih = make_float2(p.inv_h, p.inv_h), half = make_float2(-0.5f, -0.5f),
+                 one = make_float2(1.0f, 1.0f);
+    float2 ax2 = make_float2(0.0f, 0.0f), ay2 = ax2, az2 = ax2;
+    uint32_t j = b;
+    for (; j + 1 < e; j += 2) {
+        const float4 pa = __ldg(spos + j), pc = __ldg(spos + j + 1);
+        if (pa.w != (float)CMAG_FLUID || pc.w != (float)CMAG_FLUID) {
+            if (j != i) dambreak_pair<TRIM>(p, svel, aux, j, pa, pi, vi, ai, a);
+            if (j + 1 != i) dambreak_pair<TRIM>(p, svel, aux, j + 1, pc, pi, vi, ai, a);
+            continue;
+        }
+        const float2 rx = __ffma2_rn(make_float2(pa.x, pc.x), m1, px);
+        const float2 ry = __ffma2_rn(make_float2(pa.y, pc.y), m1, py);
+        const float2 rz = __ffma2_rn(make_float2(pa.z, pc.z), m1, pz);
+        const float2 d2 = __ffma2_rn(rz, rz, __ffma2_rn(ry, ry, __fmul2_rn(rx, rx)));
+        const float2 inv_d = make_float2(rsqrtf(fmaxf(d2.x, 1e-30f)), rsqrtf(fmaxf(d2.y, 1e-30f)));
+        float2 q = __fmul2_rn(__fmul2_rn(d2, inv_d), ih);
+        q = make_float2(fminf(q.x, 2.0f), fminf(q.y, 2.0f));
+        const float2 t = __ffma2_rn(q, half, one);
+        // dW/dr / (-2.5 dw_norm) = q t^3
+        const float2 qt3 = __fmul2_rn(q, __fmul2_rn(t, __fmul2_rn(t, t)));
+        const float2 aa = __ldg(aux + j), ac = __ldg(aux + j + 1);
+        const float4 va = __ldg(svel + j), vc = __ldg(svel + j + 1);
+        float2 s = __fadd2_rn(make_float2(ai.x, ai.x), make_float2(aa.x, ac.x));
+        const float2 dvx = __ffma2_rn(make_float2(va.x, vc.x), m1, vx);
+        const float2 dvy = __ffma2_rn(make_float2(va.y, vc.y), m1, vy);
+        const float2 dvz = __ffma2_rn(make_float2(va.z, vc.z), m1, vz);
+        const float2 vij = __ffma2_rn(dvz, rz, __ffma2_rn(dvy, ry, __fmul2_rn(dvx, rx)));
+        // Monaghan term where approaching: nu vij / (d2 + eps), nu = av / (rho_i + rho_j)
+        const float2 rs = __fadd2_rn(make_float2(ai.y, ai.y), make_float2(aa.y, ac.y));
+        const float2 den = __fadd2_rn(d2, make_float2(p.av_eps2, p.av_eps2));
+        const float2 art = __fmul2_rn(__fmul2_rn(make_float2(p.av_coeff, p.av_coeff), vij),
+                                      make_float2(__frcp_rn(rs.x * den.x), __frcp_rn(rs.y * den.y)));
+        s.x -= (vij.x < 0.0f) ? art.x : 0.0f;
+        s.y -= (vij.y < 0.0f) ? art.y : 0.0f;
+        // -m (p_i/rho_i^2 + p_j/rho_j^2 + art) dW/dr / d, with dW/dr = -2.5 dw_norm q t^3
+        const float c = 2.5f * p.mass * p.dw_norm;
+        s = __fmul2_rn(__fmul2_rn(s, qt3), __fmul2_rn(make_float2(c, c), inv_d));
+        s.x = (d2.x < p.support2 && j != i) ? s.x : 0.0f;
+        s.y = (d2.y < p.support2 && j + 1 != i) ? s.y : 0.0f;
+        ax2 = __ffma2_rn(s, rx, ax2);
+        ay2 = __ffma2_rn(s, ry, ay2);
+        az2 = __ffma2_rn(s, rz, az2);
+    }
+    if (j < e && j != i) dambreak_pair<TRIM>(p, svel, aux, j, __ldg(spos + j), pi, vi, ai, a);
+    a.x += ax2.x + ax2.y;
+    a.y += ay2.x + ay2.y;
+    a.z += az2.x + az2.y;
+}
+
 template <int G>
 __device__ __forceinline__ float group_sum(float v)
 {
@@ -288,6 +385,14 @@ __global__ void __launch_bounds__(256, 4)
         const float2 ai = aux[i];
         const float pterm = ai.x;
         const int3 g = grid_pos(p, pi.x, pi.y, pi.z);
+        if (SYS == CMAG_DAMBREAK && p.kernel == CMAG_KERNEL_WENDLAND) {
+            float3 a = make_float3(0.0f, 0.0f, 0.0f);
+            for_each_run<SYS, PLANAR, TRIM, G>(
+                p, off, lane, g, frac_cell(p, pi), [&](uint32_t b, uint32_t e, float, float, float) {
+                    dambreak_force_run<TRIM>(p, spos, svel, aux, b, e, i, pi, vi, ai, a);
+                });
+            ax = a.x; ay = a.y; az = a.z;
+        } else
         for_each_candidate<SYS, PLANAR, TRIM, G>(
             p, off, lane, g, frac_cell(p, pi), [&](uint32_t j, float sx, float sy, float sz) {
                 if (j == i) return;
