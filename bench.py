@@ -2,7 +2,7 @@
 (524,288 fluid + 430,572 wall particles, h = 1.3 dx, Tait, alpha = 0.01).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
-                  [--workload dambreak3d|peristalsis|poiseuille]
+                  [--workload dambreak3d|peristalsis|poiseuille|batched]
 
 Own arm: the CUDA solver through its C ABI.  `value` is fluid particles x steps /
 device seconds with the state resident in HBM (the step is replayed as a CUDA
@@ -144,6 +144,79 @@ def make_workload(name):
     return s, p, n, fluid, cfg
 
 
+class BatchedRun:
+    """The batched-scenes workload behind the calls main() makes on a solver.
+    With N ranks, rank r takes the scenes k with k % N == r (no exchange)."""
+
+    def __init__(self, rank=0, world=1):
+        from cmag_gb300 import presets
+        from cmag_gb300.batch import Batch
+        P, N, F, D = presets.batched_scenes()
+        mine = [k for k in range(len(P)) if k % world == rank]
+        self.P = [P[k] for k in mine]
+        self.N = [N[k] for k in mine]
+        self.F = [F[k] for k in mine]
+        self.D = [D[k] for k in mine]
+        self.b = Batch(self.P, self.N)
+        for k, p in enumerate(self.P):
+            self.b.reset(k)
+            if p.system == 0:  # release the dam (the reference harnesses' removeRightBoundary)
+                self.b.dambreak_remove_right_boundary(k)
+        self.b.set_graphs(True, 10)
+        self.n = self.b.num_particles
+        self.ranges = [self.b.scene_range(k) for k in range(len(self.P))]
+        self.table_cells = sum(int(p.grid_size[0]) * int(p.grid_size[1]) for p in self.P)
+
+    def update_n(self, k):
+        self.b.update_n(k)
+
+    def update(self):
+        self.b.update()
+
+    def autotune(self, reps):
+        self.b.autotune(reps)
+        return [[g["density_lanes"], g["force_lanes"]] for g in self.b.groups()]
+
+    def timed_update(self, k):
+        return self.b.timed_update(k)
+
+    def synchronize(self):
+        self.b.synchronize()
+
+    def set_stage_timing(self, on):
+        self.b.set_stage_timing(on)
+
+    def stage_times(self):
+        return self.b.stage_times()
+
+    def upload(self, array, host):
+        for k, (a, n) in enumerate(self.ranges):
+            self.b.set_array(k, array, host[a:a + n])
+
+    def download(self, array, host):
+        for k, (a, n) in enumerate(self.ranges):
+            self.b.get_array(k, array, out=host[a:a + n])
+
+    def close(self):
+        self.b.close()
+
+
+def make_batched(rank, world):
+    run = BatchedRun(rank, world)
+    groups = run.b.groups()
+    cfg = {"workload": "batched256", "scenes": 256, "scenes_this_rank": len(run.P),
+           "families": {"poiseuille": sum(d[0] == "poiseuille" for d in run.D),
+                        "dambreak": sum(d[0] == "dambreak" for d in run.D)},
+           "fluid_counts": "log-uniform [4096, 262144] (seed 1973)",
+           "nu": "log-uniform [1e-6, 1e-4] (Poiseuille; body force scaled with nu)",
+           "particles": run.n, "fluid": int(sum(run.F)), "table_cells": run.table_cells,
+           "launch_groups": len(groups), "steps_per_graph": 10, "kernel": "wendland-2d"}
+    passes = max(1, (int(np.ceil(np.log2(max(run.table_cells, 2)))) + 7) // 8)
+    meta = {"passes": passes, "force_b": 68, "integrate_b": 112,
+            "launches": 1 + 1 + passes + 1 + 2 * len(groups) + 1}
+    return run, run.n, int(sum(run.F)), cfg, meta
+
+
 def oracle_state_for(name, p, n):
     from oracle import oracle as O
     from cmag_gb300 import presets
@@ -182,6 +255,11 @@ def dist_init(n_gpus):
 def barrier_max(dist, value):
     from cmag_gb300.replicas import aggregate
     return aggregate(dist, value, 0.0, device="cuda")[0]
+
+
+def barrier_sum(dist, value):
+    from cmag_gb300.replicas import aggregate
+    return aggregate(dist, 0.0, value, device="cuda")[1]
 
 
 def run_reference(args):
@@ -239,13 +317,44 @@ def make_workload_cpu(name):
     return None, p, n, 4096, {"workload": "poiseuille2d", "particles": n, "grid": list(p.grid_size)}
 
 
+def cpu_run_batched(run, threads, budget_s=20.0):
+    """Oracle port on a bounded sample of the batch: the smallest, median and
+    largest scene of each family, one step each after a warm step, repeated
+    while within the time budget.  Returns particle-updates/s and the sample."""
+    from oracle import oracle as O
+    picks = []
+    for fam in ("poiseuille", "dambreak"):
+        ks = sorted([k for k, d in enumerate(run.D) if d[0] == fam], key=lambda k: run.F[k])
+        if ks:
+            picks += sorted({ks[0], ks[len(ks) // 2], ks[-1]})
+    states = []
+    for k in picks:
+        st = O.OracleState(run.P[k], run.N[k]).reset_reference()
+        st.step(threads=threads)
+        states.append((k, st))
+    fluid = 0
+    t0 = time.perf_counter()
+    rounds = 0
+    while True:
+        for k, st in states:
+            st.step(threads=threads)
+            fluid += run.F[k]
+        rounds += 1
+        if time.perf_counter() - t0 > budget_s or rounds >= 5:
+            break
+    dt = time.perf_counter() - t0
+    return fluid / dt, dt, "%d round(s) of one step of scenes %s (min/median/max fluid count per family)" % (
+        rounds, picks)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="own", choices=["own", "reference"])
-    ap.add_argument("--workload", default="dambreak3d", choices=["dambreak3d", "peristalsis", "poiseuille"])
+    ap.add_argument("--workload", default="dambreak3d",
+                    choices=["dambreak3d", "peristalsis", "poiseuille", "batched"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-steps", type=int, default=1)
     args = ap.parse_args()
@@ -263,11 +372,23 @@ def main():
     world = dist.get_world_size() if dist else 1
     import torch
     torch.cuda.init()
+    import cmag_gb300 as cm
 
-    s, p, n, fluid, cfg = make_workload(args.workload)
-    cfg["parallelism"] = "replicas%d" % world
-    cfg["l2"] = "inputs larger than L2 (working set %.0f MB)" % (
-        (n * (7 * 16 + 4 * 4) + 8 * p.num_grid_cells) / 1e6)
+    batched = args.workload == "batched"
+    if batched:
+        s, n, fluid, cfg, meta = make_batched(rank, world)
+        p = None
+        cfg["parallelism"] = "scenes sharded over %d rank(s)" % world
+        cells = s.table_cells
+    else:
+        s, p, n, fluid, cfg = make_workload(args.workload)
+        cfg["parallelism"] = "replicas%d" % world
+        cells = p.num_grid_cells
+        passes = max(1, (int(np.ceil(np.log2(max(cells, 2)))) + 7) // 8)
+        meta = {"passes": passes, "force_b": STAGE_BYTES["force"][p.system],
+                "integrate_b": STAGE_BYTES["integrate"][p.system],
+                "launches": {0: 4 + passes + 3, 1: 4 + passes + 3, 2: 6 + passes + 3}[p.system]}
+    cfg["l2"] = "inputs larger than L2 (working set %.0f MB)" % ((n * (7 * 16 + 4 * 4) + 8 * cells) / 1e6)
 
     # warm-up (graph capture happens on the first step), then pick the lanes per
     # particle of the neighbour loops on this workload
@@ -288,7 +409,8 @@ def main():
     torch.cuda.synchronize()
     ms = barrier_max(dist, ms)
     secs = ms / 1e3
-    value = fluid * args.steps * world / secs
+    total_fluid = fluid if not dist else int(barrier_sum(dist, fluid))
+    value = total_fluid * args.steps / secs if batched else fluid * args.steps * world / secs
     s.synchronize()
 
     # ---- per-stage times (plain launches, events around each stage) ----
@@ -299,10 +421,9 @@ def main():
     names = ["hash", "sort", "reorder", "density", "force", "integrate"]
     per_stage = {nm: stage_ms[k] / max(tsteps, 1) for k, nm in enumerate(names)}
     dom = max(per_stage, key=per_stage.get)
-    passes = max(1, (int(np.ceil(np.log2(max(p.num_grid_cells, 2)))) + 7) // 8)
-    bytes_pp = {"hash": STAGE_BYTES["hash"], "sort": sort_bytes(passes), "reorder": STAGE_BYTES["reorder"],
-                "density": STAGE_BYTES["density"], "force": STAGE_BYTES["force"][p.system],
-                "integrate": STAGE_BYTES["integrate"][p.system]}
+    bytes_pp = {"hash": STAGE_BYTES["hash"], "sort": sort_bytes(meta["passes"]),
+                "reorder": STAGE_BYTES["reorder"], "density": STAGE_BYTES["density"],
+                "force": meta["force_b"], "integrate": meta["integrate_b"]}
     peak, peak_kind = load_peaks()
     achieved = bytes_pp[dom] * n / (per_stage[dom] / 1e3) / 1e9
     traffic = None
@@ -312,33 +433,41 @@ def main():
             traffic = json.load(f).get(dom)
 
     # ---- end-to-end through the public API with host buffers ----
-    import cmag_gb300 as cm
     arrays = [cm.POSITION, cm.VELOCITY, cm.VELOCITYLEAPFROG]
     host = {a: torch.empty((n, 4), dtype=torch.float32, pin_memory=True).numpy() for a in arrays}
+    if batched:
+        put = lambda a: s.upload(a, host[a])  # noqa: E731
+        get = lambda a: s.download(a, host[a])  # noqa: E731
+    else:
+        put = lambda a: s.setArray(a, host[a])  # noqa: E731
+
+        def get(a):
+            host[a][:] = s.getArray(a)
     for a in arrays:
-        host[a][:] = s.getArray(a)
-    e2e_steps = max(1, min(args.steps, 50))
+        get(a)
+    e2e_steps = max(1, min(args.steps, 20 if batched else 50))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         for a in arrays:
-            s.setArray(a, host[a])
+            put(a)
         s.update()
         for a in arrays:
-            host[a][:] = s.getArray(a)
+            get(a)
     e2e_secs = barrier_max(dist, time.perf_counter() - t0)
-    e2e_value = fluid * e2e_steps * world / e2e_secs
+    e2e_value = (total_fluid if batched else fluid * world) * e2e_steps / e2e_secs
     io_bytes = 3 * 16 * n
 
-    launches_per_step = {0: 4 + passes + 3, 1: 4 + passes + 3, 2: 6 + passes + 3}[p.system]
     line = {
         "metric": METRIC, "value": value, "unit": "particle-updates/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded lattice + jitter, seed 1973)", "config": cfg,
+        "higher_is_better": True, "scaling": "strong" if batched else "weak", "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded lattices%s, seed 1973)" % ("" if batched else " + jitter"),
+        "config": cfg,
         "e2e": {"value": e2e_value, "unit": "particle-updates/s", "h2d_bytes_per_step": io_bytes,
                 "d2h_bytes_per_step": io_bytes, "steps": e2e_steps},
-        "gpu_launches": launches_per_step * args.steps,
+        "gpu_launches": meta["launches"] * args.steps,
         "stage_ms": {k: round(v, 5) for k, v in per_stage.items()},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
@@ -349,11 +478,13 @@ def main():
         threads = os.cpu_count() or 1
         from oracle import oracle as O
         O.build()
-        v, dt = cpu_run(args.workload, p, n, fluid, args.cpu_steps, threads)
+        if batched:
+            v, dt, sample = cpu_run_batched(s, threads)
+        else:
+            v, dt = cpu_run(args.workload, p, n, fluid, args.cpu_steps, threads)
+            sample = "%d full step(s) of the same %d-particle scene" % (args.cpu_steps, n)
         line["cpu_baseline"] = {"value": v, "unit": "particle-updates/s", "cores": threads,
-                                "kind": "port", "seconds": dt,
-                                "sample": "%d full step(s) of the same %d-particle scene"
-                                          % (args.cpu_steps, n)}
+                                "kind": "port", "seconds": dt, "sample": sample}
     s.close()
     if rank == 0:
         print(json.dumps(line))

@@ -6,5 +6,6 @@ mirror of the reference solver classes."""
 from . import _abi  # noqa: F401
 from ._abi import *  # noqa: F401,F403
 from ._lib import CmagError, LIB_PATH, lib  # noqa: F401
+from .batch import Batch  # noqa: F401
 from .systems import (DamBreakSystem, PeristalsisSystem, PoiseuilleFlowSystem,  # noqa: F401
                       sort_particles)

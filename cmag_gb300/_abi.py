@@ -110,3 +110,17 @@ def u3(v):
 
 def f3(v):
     return f32x3(*[float(x) for x in v])
+
+
+class BatchGroup(ctypes.Structure):
+    """cmag_batch_group: one launch group of a batch."""
+    _fields_ = [
+        ("system", ctypes.c_int32),
+        ("planar", ctypes.c_int32),
+        ("trim", ctypes.c_int32),
+        ("size_bucket", ctypes.c_uint32),
+        ("scenes", ctypes.c_uint32),
+        ("particles", ctypes.c_uint32),
+        ("density_lanes", ctypes.c_int32),
+        ("force_lanes", ctypes.c_int32),
+    ]

@@ -5,7 +5,7 @@ first use instead of falling back to anything else."""
 import ctypes
 import os
 
-from ._abi import SphParams
+from ._abi import BatchGroup, SphParams
 
 PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "libcmag_sph.so")
@@ -16,6 +16,9 @@ P = ctypes.POINTER
 c_u32p = P(ctypes.c_uint32)
 c_f32p = P(ctypes.c_float)
 c_sys = ctypes.c_void_p
+c_bat = ctypes.c_void_p
+c_u32 = ctypes.c_uint32
+c_i32 = ctypes.c_int32
 
 # every symbol the header declares, with its ctypes signature
 SIGNATURES = {
@@ -73,6 +76,42 @@ SIGNATURES = {
     "cmag_sort_particles_noalloc": ([c_u32p, c_u32p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_void_p],
                                     ctypes.c_int),
     "cmag_sort_particles_noalloc_error": ([], ctypes.c_char_p),
+    # batches
+    "cmag_batch_create": ([P(SphParams), c_u32p, c_u32, P(c_bat)], ctypes.c_int),
+    "cmag_batch_destroy": ([c_bat], ctypes.c_int),
+    "cmag_batch_num_scenes": ([c_bat, c_u32p], ctypes.c_int),
+    "cmag_batch_num_particles": ([c_bat, c_u32p], ctypes.c_int),
+    "cmag_batch_scene_range": ([c_bat, c_u32, c_u32p, c_u32p], ctypes.c_int),
+    "cmag_batch_reset": ([c_bat], ctypes.c_int),
+    "cmag_batch_reset_scene": ([c_bat, c_u32], ctypes.c_int),
+    "cmag_batch_set_array": ([c_bat, c_u32, c_i32, c_f32p, c_u32, c_u32], ctypes.c_int),
+    "cmag_batch_get_array": ([c_bat, c_u32, c_i32, c_f32p, c_u32, c_u32], ctypes.c_int),
+    "cmag_batch_get_uint_array": ([c_bat, c_u32, c_i32, c_u32p, c_u32, c_u32], ctypes.c_int),
+    "cmag_batch_device_array": ([c_bat, c_i32], ctypes.c_void_p),
+    "cmag_batch_get_params": ([c_bat, c_u32, P(SphParams)], ctypes.c_int),
+    "cmag_batch_set_params": ([c_bat, c_u32, P(SphParams)], ctypes.c_int),
+    "cmag_batch_update": ([c_bat], ctypes.c_int),
+    "cmag_batch_update_n": ([c_bat, c_u32], ctypes.c_int),
+    "cmag_batch_timed_update": ([c_bat, c_u32, c_f32p], ctypes.c_int),
+    "cmag_batch_run_stages": ([c_bat, c_i32], ctypes.c_int),
+    "cmag_batch_elapsed_time": ([c_bat, c_u32, c_f32p], ctypes.c_int),
+    "cmag_batch_dambreak_change_right_boundary": ([c_bat, c_u32], ctypes.c_int),
+    "cmag_batch_dambreak_remove_right_boundary": ([c_bat, c_u32], ctypes.c_int),
+    "cmag_batch_poiseuille_change_gravity": ([c_bat, c_u32], ctypes.c_int),
+    "cmag_batch_fluid_extents": ([c_bat, c_f32p, c_f32p], ctypes.c_int),
+    "cmag_batch_set_stream": ([c_bat, ctypes.c_void_p], ctypes.c_int),
+    "cmag_batch_stream": ([c_bat], ctypes.c_void_p),
+    "cmag_batch_set_graphs": ([c_bat, c_i32, c_u32], ctypes.c_int),
+    "cmag_batch_synchronize": ([c_bat], ctypes.c_int),
+    "cmag_batch_device_error_bits": ([c_bat, c_u32p], ctypes.c_int),
+    "cmag_batch_num_groups": ([c_bat, c_u32p], ctypes.c_int),
+    "cmag_batch_group_info": ([c_bat, c_u32, P(BatchGroup)], ctypes.c_int),
+    "cmag_batch_scene_group": ([c_bat, c_u32, c_u32p], ctypes.c_int),
+    "cmag_batch_set_group_lanes": ([c_bat, c_u32, c_i32, c_i32], ctypes.c_int),
+    "cmag_batch_autotune": ([c_bat, c_i32], ctypes.c_int),
+    "cmag_batch_set_stage_timing": ([c_bat, c_i32], ctypes.c_int),
+    "cmag_batch_stage_times": ([c_bat, c_f32p, c_u32p], ctypes.c_int),
+    "cmag_batch_last_error": ([c_bat], ctypes.c_char_p),
 }
 
 
@@ -98,9 +137,14 @@ def lib():
     return _lib
 
 
-def check(rc, handle=None):
+def check(rc, handle=None, batch=None):
     if rc != 0:
         L = lib()
-        msg = (L.cmag_system_last_error(handle) if handle else L.cmag_last_error()) or b""
-        raise CmagError(rc, msg.decode(errors="replace"))
+        if batch:
+            msg = L.cmag_batch_last_error(batch)
+        elif handle:
+            msg = L.cmag_system_last_error(handle)
+        else:
+            msg = L.cmag_last_error()
+        raise CmagError(rc, (msg or b"").decode(errors="replace"))
     return rc

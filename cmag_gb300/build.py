@@ -11,13 +11,15 @@ SRC = os.path.join(PKG, "csrc")
 OUT_DIR = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libcmag_sph.so")
 
-SOURCES = ["sort.cu", "cells.cu", "neighbors.cu", "integrate.cu", "reduce.cu", "system.cu",
+SOURCES = ["sort.cu", "cells.cu", "neighbors.cu", "integrate.cu", "reduce.cu", "system.cu", "batch.cu",
            "host_scenes.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # host code: no fused multiply-add, so host float arithmetic (parameters, scenes,
-# phase mirror) matches the reference expressions on x86_64 and aarch64 alike
+# phase mirror) matches the reference expressions on x86_64 and aarch64 alike.
+# device code (-fmad=false): only the fused multiply-adds written out in the
+# kernels, so every template variant of a kernel rounds identically
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
-         "-ffp-contract=off", "--expt-relaxed-constexpr", "-I" + SRC]
+         "-ffp-contract=off", "-fmad=false", "--expt-relaxed-constexpr", "-I" + SRC]
 
 
 def nvcc():

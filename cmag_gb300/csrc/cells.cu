@@ -27,9 +27,15 @@ constexpr uint32_t kFlagPrefix = 2u << 30;
 constexpr uint32_t kCountMask = (1u << 30) - 1u;
 constexpr int kSpinLimit = 1 << 22;
 
-// calcHashD (fluid_kernel.cu:34-48) + per-cell counts + radix digit histograms
+// calcHashD (fluid_kernel.cu:34-48) + per-cell counts + radix digit histograms.
+// The sort key is the reference hash for a single scene; in a batch it is the
+// particle's cell index in the shared offset table (scene table base + cell), so
+// one sort orders by scene, then by cell.  A particle whose cell lies outside
+// its offset table (a planar scene's particle that left its z layer) is counted
+// in the table's last cell and reported as CMAG_DEVERR_RANGE.
+template <bool BATCH>
 __global__ void __launch_bounds__(256)
-    k_hash(DevParams p, const float4 *__restrict__ pos, uint32_t *__restrict__ hash,
+    k_hash(DevParams pv, BatchView bv, const float4 *__restrict__ pos, uint32_t *__restrict__ hash,
            uint32_t *__restrict__ cnt, uint32_t *__restrict__ hist, int passes,
            uint32_t *err)
 {
@@ -38,25 +44,29 @@ __global__ void __launch_bounds__(256)
         for (int b = threadIdx.x; b < passes * kRadix; b += blockDim.x) s_hist[b] = 0;
     __syncthreads();
     const uint32_t stride = gridDim.x * blockDim.x;
-    const uint32_t n = p.n;
+    const uint32_t n = BATCH ? bv.n_total : pv.n;
     // every lane runs the same trip count so the warp-collective calls stay converged
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
         uint32_t i = base + threadIdx.x;
         bool valid = i < n;
-        uint32_t h = 0xffffffffu;
+        uint32_t h = 0xffffffffu, slot = 0;
         if (valid) {
+            const DevParams &p = BATCH ? bv.scenes[bv.scene_of[i]] : pv;
             float4 q = pos[i];
             int3 g = grid_pos(p, q.x, q.y, q.z);
-            h = grid_hash(p, g.x, g.y, g.z);
+            const uint32_t hr = grid_hash(p, g.x, g.y, g.z);
+            uint32_t rel = hr - p.scan_base;  // wraps for hr < scan_base
+            if (rel >= p.scan_cells) {
+                set_error(err, CMAG_DEVERR_RANGE);
+                rel = p.scan_cells - 1;
+            }
+            slot = p.table_base + rel;
+            h = BATCH ? slot : p.scan_base + rel;  // = hr inside the table
             hash[i] = h;
         }
         uint32_t peers = __match_any_sync(0xffffffffu, h);
         bool leader = (threadIdx.x & 31) == (uint32_t)(__ffs(peers) - 1);
-        if (valid && leader) {
-            const uint32_t rel = h - p.scan_base;  // wraps for h < scan_base
-            if (rel < p.scan_cells) atomicAdd(&cnt[rel], (uint32_t)__popc(peers));
-            else set_error(err, CMAG_DEVERR_RANGE);
-        }
+        if (valid && leader) atomicAdd(&cnt[slot], (uint32_t)__popc(peers));
         if (hist) {
             for (int ps = 0; ps < passes; ++ps) {
                 uint32_t dg = valid ? ((h >> (8 * ps)) & 255u) : 0xffffffffu;
@@ -208,13 +218,15 @@ __global__ void k_cell_view(const uint32_t *__restrict__ off, uint32_t scan_base
 
 }  // namespace
 
-void launch_hash(const DevParams &p, const float4 *pos, uint32_t *hash, uint32_t *cnt,
-                 uint32_t *hist, int passes, uint32_t *err, cudaStream_t st)
+void launch_hash(const DevParams &p, const BatchView &bv, const float4 *pos, uint32_t *hash,
+                 uint32_t *cnt, uint32_t *hist, int passes, uint32_t *err, cudaStream_t st)
 {
-    if (p.n == 0) return;
-    uint32_t blocks = (p.n + 256 * 8 - 1) / (256 * 8);
+    const uint32_t n = bv.scenes ? bv.n_total : p.n;
+    if (n == 0) return;
+    uint32_t blocks = (n + 256 * 8 - 1) / (256 * 8);
     if (blocks < 1) blocks = 1;
-    k_hash<<<blocks, 256, 0, st>>>(p, pos, hash, cnt, hist, passes, err);
+    if (bv.scenes) k_hash<true><<<blocks, 256, 0, st>>>(p, bv, pos, hash, cnt, hist, passes, err);
+    else k_hash<false><<<blocks, 256, 0, st>>>(p, bv, pos, hash, cnt, hist, passes, err);
 }
 
 size_t cell_scan_workspace_words(uint32_t m) { return 1 + (m + kScanTile - 1) / kScanTile; }

@@ -20,9 +20,9 @@ __device__ __forceinline__ float get_wave(const DevParams &p, float x, float t)
     return sinf(p.wave_k * ((x - p.ox) - p.wave_speed * t));
 }
 
-// One thread advances the boundary-configuration phase exactly as the host
-// mirror does (separately rounded adds and multiplies, no contraction).
-__global__ void k_phase(DevParams p, PhaseState *ph, float k_milli)
+// Advance one boundary-configuration phase exactly as the host mirror does
+// (separately rounded adds and multiplies, no contraction).
+__device__ __forceinline__ void advance_phase(const DevParams &p, PhaseState *ph, float k_milli)
 {
     PhaseState s = *ph;
     s.configure = 0;
@@ -42,13 +42,28 @@ __global__ void k_phase(DevParams p, PhaseState *ph, float k_milli)
     *ph = s;
 }
 
-__global__ void __launch_bounds__(256)
-    k_configure_boundary(DevParams p, float4 *__restrict__ pos, const PhaseState *__restrict__ ph)
+__global__ void k_phase(DevParams p, PhaseState *ph, float k_milli) { advance_phase(p, ph, k_milli); }
+
+__global__ void k_phase_batch(const DevParams *__restrict__ scenes, uint32_t nscenes,
+                              PhaseState *ph, float k_milli)
 {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < nscenes && scenes[s].system == CMAG_PERISTALSIS) advance_phase(scenes[s], ph + s, k_milli);
+}
+
+template <bool BATCH>
+__global__ void __launch_bounds__(256)
+    k_configure_boundary(DevParams pv, BatchView bv, float4 *__restrict__ pos,
+                         const PhaseState *__restrict__ ph_all)
+{
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (BATCH ? bv.n_total : pv.n)) return;
+    const uint32_t sc = BATCH ? bv.scene_of[i] : 0u;
+    const DevParams &p = BATCH ? bv.scenes[sc] : pv;
+    if (BATCH && p.system != CMAG_PERISTALSIS) return;
+    const PhaseState *ph = ph_all + sc;
     if (!ph->configure) return;
     const float wh = ph->configure_height;
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= p.n) return;
     float4 q = pos[i];
     if (q.w > 0.0f) {
         q.y = -p.half_fluid_h + wh * get_wave(p, q.x, 0.0f) - p.r * (q.w - 1.0f);
@@ -59,14 +74,18 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+template <bool BATCH>
 __global__ void __launch_bounds__(256)
-    k_integrate(DevParams p, float4 *__restrict__ pos, float4 *__restrict__ vel,
+    k_integrate(DevParams pv, BatchView bv, float4 *__restrict__ pos, float4 *__restrict__ vel,
                 float4 *__restrict__ vlf, const float4 *__restrict__ acc,
                 const float4 *__restrict__ vforce, const float4 *__restrict__ pforce,
-                const PhaseState *__restrict__ ph)
+                const PhaseState *__restrict__ ph_all)
 {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= p.n) return;
+    if (i >= (BATCH ? bv.n_total : pv.n)) return;
+    const uint32_t sc = BATCH ? bv.scene_of[i] : 0u;
+    const DevParams &p = BATCH ? bv.scenes[sc] : pv;
+    const PhaseState *ph = ph_all + sc;
     float4 q = pos[i];
     float ax, ay, az;
     if (p.system == CMAG_DAMBREAK) {
@@ -132,19 +151,32 @@ void launch_phase(const DevParams &p, PhaseState *ph, float k_milli, cudaStream_
     k_phase<<<1, 1, 0, st>>>(p, ph, k_milli);
 }
 
-void launch_configure_boundary(const DevParams &p, float4 *pos, const PhaseState *ph,
-                               cudaStream_t st)
+void launch_phase_batch(const DevParams *scenes, uint32_t nscenes, PhaseState *ph, float k_milli,
+                        cudaStream_t st)
 {
-    if (p.n == 0) return;
-    k_configure_boundary<<<(p.n + 255) / 256, 256, 0, st>>>(p, pos, ph);
+    if (nscenes == 0) return;
+    k_phase_batch<<<(nscenes + 127) / 128, 128, 0, st>>>(scenes, nscenes, ph, k_milli);
 }
 
-void launch_integrate(const DevParams &p, float4 *pos, float4 *vel, float4 *vlf,
-                      const float4 *acc, const float4 *vforce, const float4 *pforce,
+void launch_configure_boundary(const DevParams &p, const BatchView &bv, float4 *pos,
+                               const PhaseState *ph, cudaStream_t st)
+{
+    const uint32_t n = bv.scenes ? bv.n_total : p.n;
+    if (n == 0) return;
+    if (bv.scenes) k_configure_boundary<true><<<(n + 255) / 256, 256, 0, st>>>(p, bv, pos, ph);
+    else k_configure_boundary<false><<<(n + 255) / 256, 256, 0, st>>>(p, bv, pos, ph);
+}
+
+void launch_integrate(const DevParams &p, const BatchView &bv, float4 *pos, float4 *vel,
+                      float4 *vlf, const float4 *acc, const float4 *vforce, const float4 *pforce,
                       const PhaseState *ph, cudaStream_t st)
 {
-    if (p.n == 0) return;
-    k_integrate<<<(p.n + 255) / 256, 256, 0, st>>>(p, pos, vel, vlf, acc, vforce, pforce, ph);
+    const uint32_t n = bv.scenes ? bv.n_total : p.n;
+    if (n == 0) return;
+    if (bv.scenes)
+        k_integrate<true><<<(n + 255) / 256, 256, 0, st>>>(p, bv, pos, vel, vlf, acc, vforce, pforce, ph);
+    else
+        k_integrate<false><<<(n + 255) / 256, 256, 0, st>>>(p, bv, pos, vel, vlf, acc, vforce, pforce, ph);
 }
 
 // shiftRightBoundaryD (remove = 0: x += dx) and removeRightBoundaryD

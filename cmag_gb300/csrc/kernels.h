@@ -43,8 +43,8 @@ void launch_onesweep_pass(const uint32_t *kin, const uint32_t *vin, uint32_t *ko
 // ---- cells (cells.cu) --------------------------------------------------------
 // Hash every particle, count particles per cell and accumulate the sort's digit
 // histograms.  hist may be null.
-void launch_hash(const DevParams &p, const float4 *pos, uint32_t *hash, uint32_t *cnt,
-                 uint32_t *hist, int passes, uint32_t *err, cudaStream_t st);
+void launch_hash(const DevParams &p, const BatchView &bv, const float4 *pos, uint32_t *hash,
+                 uint32_t *cnt, uint32_t *hist, int passes, uint32_t *err, cudaStream_t st);
 // Exclusive scan of cnt[0..m) into off[0..m) (single pass, chained look-back),
 // clearing cnt for the next step.  ws must hold cell_scan_workspace_words(m), zeroed.
 size_t cell_scan_workspace_words(uint32_t m);
@@ -58,20 +58,27 @@ void launch_cell_view(const uint32_t *off, uint32_t scan_base, uint32_t scan_cel
                       uint64_t ncells, uint32_t *cell_start, uint32_t *cell_end, cudaStream_t st);
 
 // ---- neighbour loops (neighbors.cu) ----------------------------------------
-// density also writes aux[i] = (p/rho^2, rho) (DamBreak) or (p/rho^2, 1/rho)
-void launch_density(const DevParams &p, int group, const float4 *spos, const uint32_t *off,
-                    float4 *meas, float2 *aux, cudaStream_t st);
-void launch_force(const DevParams &p, int group, const float4 *spos, const float4 *svel,
-                  const float2 *aux, const uint32_t *idx, const uint32_t *off, float4 *out_a,
-                  float4 *out_b, cudaStream_t st);
+// density also writes aux[i] = (p/rho^2, rho) (DamBreak) or (p/rho^2, 1/rho).
+// bv empty: one scene with parameters p; otherwise one launch group of a batch
+// (p = the parameters of any of the group's scenes).
+void launch_density(const DevParams &p, const BatchView &bv, int group, const float4 *spos,
+                    const uint32_t *off, float4 *meas, float2 *aux, cudaStream_t st);
+void launch_force(const DevParams &p, const BatchView &bv, int group, const float4 *spos,
+                  const float4 *svel, const float2 *aux, const uint32_t *idx, const uint32_t *off,
+                  float4 *out_a, float4 *out_b, cudaStream_t st);
 
 // ---- integration and wall motion (integrate.cu) ------------------------------
+// bv empty: one scene; otherwise every particle of the batch with its scene's
+// parameters and phase (ph holds one PhaseState per scene).
 void launch_phase(const DevParams &p, PhaseState *ph, float k_milli, cudaStream_t st);
-void launch_configure_boundary(const DevParams &p, float4 *pos, const PhaseState *ph,
-                               cudaStream_t st);
-void launch_integrate(const DevParams &p, float4 *pos, float4 *vel, float4 *vlf,
-                      const float4 *acc, const float4 *vforce, const float4 *pforce,
+void launch_configure_boundary(const DevParams &p, const BatchView &bv, float4 *pos,
+                               const PhaseState *ph, cudaStream_t st);
+void launch_integrate(const DevParams &p, const BatchView &bv, float4 *pos, float4 *vel,
+                      float4 *vlf, const float4 *acc, const float4 *vforce, const float4 *pforce,
                       const PhaseState *ph, cudaStream_t st);
+// the phase machines of the batch's Peristalsis scenes (one thread per scene)
+void launch_phase_batch(const DevParams *scenes, uint32_t nscenes, PhaseState *ph, float k_milli,
+                        cudaStream_t st);
 void launch_gate(const DevParams &p, float4 *pos, int remove, float dx, float fx, float fy,
                  cudaStream_t st);
 
@@ -79,6 +86,9 @@ void launch_gate(const DevParams &p, float4 *pos, int remove, float dx, float fx
 // out6: order-preserving keys of min x,y,z then max x,y,z (init 0xffffffff, 0)
 void launch_fluid_extent(int32_t system, const float4 *pos, uint32_t n, uint32_t *out6,
                          cudaStream_t st);
+// per-scene extents of a batch: out[6 s ..] as out6 above (initialised the same way)
+void launch_fluid_extents_batch(const BatchView &bv, const float4 *pos, uint32_t *out,
+                                cudaStream_t st);
 void launch_fluid_sum(int32_t system, const float4 *type_src, const float4 *a, uint32_t n,
                       double *sums4, unsigned long long *count, cudaStream_t st);
 

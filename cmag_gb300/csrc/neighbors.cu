@@ -23,6 +23,11 @@
 // fractional cell coordinates.  The density kernel also stores, per particle,
 // p/rho^2 and rho (DamBreak) or 1/rho (the others), so the force loop needs no
 // division per pair.
+//
+// Every fused multiply-add is written out (__fmaf_rn and the paired forms); the
+// library is compiled with -fmad=false, so no other multiply and add are fused.
+// Results therefore do not depend on how the compiler schedules a particular
+// template variant: a scene gives the same bits alone and inside a batch.
 #include <cuda_runtime.h>
 
 #include "kernels.h"
@@ -192,110 +197,14 @@ __device__ __forceinline__ void wendland_run(const DevParams &p, const float4 *_
         w.y = (d2.y < p.support2) ? w.y : 0.0f;
         acc = __fadd2_rn(acc, w);
     }
-    if (j < e) {
+    if (j < e) {  // the same operations as one half of a pair step
         const float3 r = rel<SYS>(pi, __ldg(spos + j), sx, sy, sz);
-        const float d2 = r.x * r.x + r.y * r.y + r.z * r.z;
-        const float q = fminf(d2 * rsqrtf(fmaxf(d2, 1e-30f)) * p.inv_h, 2.0f);
-        const float t = 1.0f - 0.5f * q, t2 = t * t;
-        acc.x += (d2 < p.support2) ? t2 * t2 * (2.0f * q + 1.0f) : 0.0f;
+        const float d2 = __fmaf_rn(r.z, r.z, __fmaf_rn(r.y, r.y, __fmul_rn(r.x, r.x)));
+        const float q = fminf(__fmul_rn(__fmul_rn(d2, rsqrtf(fmaxf(d2, 1e-30f))), p.inv_h), 2.0f);
+        const float t = __fmaf_rn(q, -0.5f, 1.0f), t2 = __fmul_rn(t, t);
+        const float w = __fmul_rn(__fmul_rn(t2, t2), __fmaf_rn(q, 2.0f, 1.0f));
+        acc.x = __fadd_rn(acc.x, (d2 < p.support2) ? w : 0.0f);
     }
-}
-
-// One DamBreak candidate pair, scalar: Lennard-Jones from walls
-// (fluid_kernel.cu:199-207), pressure + Monaghan viscosity from fluid
-// (fluid_kernel.cu:221-237).  Adds to a.
-template <bool TRIM>
-__device__ __forceinline__ void dambreak_pair(const DevParams &p, const float4 *__restrict__ svel,
-                                              const float2 *__restrict__ aux, uint32_t j, float4 pj,
-                                              float4 pi, float4 vi, float2 ai, float3 &a)
-{
-    const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
-    const float d2 = rx * rx + ry * ry + rz * rz;
-    if (pj.w != (float)CMAG_FLUID) {
-        if (TRIM && !(d2 < p.support2)) return;
-        const float inv_d2 = __frcp_rn(d2);
-        const float a2 = p.lj_a2 * inv_d2;
-        const float a6 = a2 * a2 * a2;
-        const float s = p.lj_D * (a6 * a6 - a6) * inv_d2;
-        a.x += s * rx; a.y += s * ry; a.z += s * rz;
-        return;
-    }
-    if (!(d2 < p.support2)) return;
-    const float inv_d = rsqrtf(d2);
-    const float temp = kernel_dw(p, d2 * inv_d * p.inv_h);
-    const float2 aj = __ldg(aux + j);
-    float s = ai.x + aj.x;
-    const float4 vj = __ldg(svel + j);
-    const float vij = (vi.x - vj.x) * rx + (vi.y - vj.y) * ry + (vi.z - vj.z) * rz;
-    if (vij < 0.0f) {
-        const float nu = __fdividef(p.av_coeff, ai.y + aj.y);
-        s -= __fdividef(nu * vij, d2 + p.av_eps2);
-    }
-    s *= -p.mass * temp * inv_d;
-    a.x += s * rx; a.y += s * ry; a.z += s * rz;
-}
-
-// DamBreak force over candidates [b, e) of one run (sorted particle i excluded):
-// fluid-fluid pairs two at a time in paired FP32 with selects instead of
-// branches; a step that meets a wall candidate falls back to the scalar path.
-template <bool TRIM>
-__device__ __forceinline__ void dambreak_force_run(const DevParams &p, const float4 *__restrict__ spos,
-                                                   const float4 *__restrict__ svel,
-                                                   const float2 *__restrict__ aux, uint32_t b,
-                                                   uint32_t e, uint32_t i, float4 pi, float4 vi,
-                                                   float2 ai, float3 &a)
-{
-    const float2 px = make_float2(pi.x, pi.x), py = make_float2(pi.y, pi.y),
-                 pz = make_float2(pi.z, pi.z), m1 = make_float2(-1.0f, -1.0f);
-    const float2 vx = make_float2(vi.x, vi.x), vy = make_float2(vi.y, vi.y), vz = make_float2(vi.z, vi.z);
-    const float2 ih = make_float2(p.inv_h, p.inv_h), half = make_float2(-0.5f, -0.5f),
-                 one = make_float2(1.0f, 1.0f);
-    float2 ax2 = make_float2(0.0f, 0.0f), ay2 = ax2, az2 = ax2;
-    uint32_t j = b;
-    for (; j + 1 < e; j += 2) {
-        const float4 pa = __ldg(spos + j), pc = __ldg(spos + j + 1);
-        if (pa.w != (float)CMAG_FLUID || pc.w != (float)CMAG_FLUID) {
-            if (j != i) dambreak_pair<TRIM>(p, svel, aux, j, pa, pi, vi, ai, a);
-            if (j + 1 != i) dambreak_pair<TRIM>(p, svel, aux, j + 1, pc, pi, vi, ai, a);
-            continue;
-        }
-        const float2 rx = __ffma2_rn(make_float2(pa.x, pc.x), m1, px);
-        const float2 ry = __ffma2_rn(make_float2(pa.y, pc.y), m1, py);
-        const float2 rz = __ffma2_rn(make_float2(pa.z, pc.z), m1, pz);
-        const float2 d2 = __ffma2_rn(rz, rz, __ffma2_rn(ry, ry, __fmul2_rn(rx, rx)));
-        const float2 inv_d = make_float2(rsqrtf(fmaxf(d2.x, 1e-30f)), rsqrtf(fmaxf(d2.y, 1e-30f)));
-        float2 q = __fmul2_rn(__fmul2_rn(d2, inv_d), ih);
-        q = make_float2(fminf(q.x, 2.0f), fminf(q.y, 2.0f));
-        const float2 t = __ffma2_rn(q, half, one);
-        // dW/dr / (-2.5 dw_norm) = q t^3
-        const float2 qt3 = __fmul2_rn(q, __fmul2_rn(t, __fmul2_rn(t, t)));
-        const float2 aa = __ldg(aux + j), ac = __ldg(aux + j + 1);
-        const float4 va = __ldg(svel + j), vc = __ldg(svel + j + 1);
-        float2 s = __fadd2_rn(make_float2(ai.x, ai.x), make_float2(aa.x, ac.x));
-        const float2 dvx = __ffma2_rn(make_float2(va.x, vc.x), m1, vx);
-        const float2 dvy = __ffma2_rn(make_float2(va.y, vc.y), m1, vy);
-        const float2 dvz = __ffma2_rn(make_float2(va.z, vc.z), m1, vz);
-        const float2 vij = __ffma2_rn(dvz, rz, __ffma2_rn(dvy, ry, __fmul2_rn(dvx, rx)));
-        // Monaghan term where approaching: nu vij / (d2 + eps), nu = av / (rho_i + rho_j)
-        const float2 rs = __fadd2_rn(make_float2(ai.y, ai.y), make_float2(aa.y, ac.y));
-        const float2 den = __fadd2_rn(d2, make_float2(p.av_eps2, p.av_eps2));
-        const float2 art = __fmul2_rn(__fmul2_rn(make_float2(p.av_coeff, p.av_coeff), vij),
-                                      make_float2(__frcp_rn(rs.x * den.x), __frcp_rn(rs.y * den.y)));
-        s.x -= (vij.x < 0.0f) ? art.x : 0.0f;
-        s.y -= (vij.y < 0.0f) ? art.y : 0.0f;
-        // -m (p_i/rho_i^2 + p_j/rho_j^2 + art) dW/dr / d, with dW/dr = -2.5 dw_norm q t^3
-        const float c = 2.5f * p.mass * p.dw_norm;
-        s = __fmul2_rn(__fmul2_rn(s, qt3), __fmul2_rn(make_float2(c, c), inv_d));
-        s.x = (d2.x < p.support2 && j != i) ? s.x : 0.0f;
-        s.y = (d2.y < p.support2 && j + 1 != i) ? s.y : 0.0f;
-        ax2 = __ffma2_rn(s, rx, ax2);
-        ay2 = __ffma2_rn(s, ry, ay2);
-        az2 = __ffma2_rn(s, rz, az2);
-    }
-    if (j < e && j != i) dambreak_pair<TRIM>(p, svel, aux, j, __ldg(spos + j), pi, vi, ai, a);
-    a.x += ax2.x + ax2.y;
-    a.y += ay2.x + ay2.y;
-    a.z += az2.x + az2.y;
 }
 
 template <int G>
@@ -313,15 +222,19 @@ __device__ __forceinline__ float3 frac_cell(const DevParams &p, float4 q)
 
 // ---------------------------------------------------------------- density --
 // 256 threads, 6 blocks per SM: at most 42 registers, no spills
-template <int SYS, bool PLANAR, bool TRIM, int G>
+template <int SYS, bool PLANAR, bool TRIM, int G, bool BATCH>
 __global__ void __launch_bounds__(256, 6)
-    k_density(DevParams p, const float4 *__restrict__ spos, const uint32_t *__restrict__ off,
-              float4 *__restrict__ meas, float2 *__restrict__ aux)
+    k_density(DevParams pv, BatchView bv, const float4 *__restrict__ spos,
+              const uint32_t *__restrict__ off_all, float4 *__restrict__ meas,
+              float2 *__restrict__ aux)
 {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t i = t / G;
+    const uint32_t i = (BATCH ? bv.first : 0u) + t / G;
     const int lane = (int)(t % G);
-    const bool active = i < p.n;
+    const bool active = t / G < (BATCH ? bv.count : pv.n);
+    // a batch reads its scene's parameters; the scene's cells start at table_base
+    const DevParams &p = BATCH ? bv.scenes[active ? bv.scene_of[i] : bv.scene_of[bv.first]] : pv;
+    const uint32_t *off = off_all + p.table_base;
     const float4 pi = active ? spos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     // Poiseuille walls keep rest density (poiseuilleFlowKernel.cu:154-158)
     const bool pinned = SYS == CMAG_POISEUILLE && pi.w == 1.0f;
@@ -340,7 +253,7 @@ __global__ void __launch_bounds__(256, 6)
             for_each_candidate<SYS, PLANAR, TRIM, G>(
                 p, off, lane, g, frac_cell(p, pi), [&](uint32_t j, float sx, float sy, float sz) {
                     const float3 r = rel<SYS>(pi, __ldg(spos + j), sx, sy, sz);
-                    const float d2 = r.x * r.x + r.y * r.y + r.z * r.z;
+                    const float d2 = __fmaf_rn(r.z, r.z, __fmaf_rn(r.y, r.y, __fmul_rn(r.x, r.x)));
                     // evaluated for every candidate and selected: no divergent branch
                     const float w = kernel_w(p, fminf(d2 * rsqrtf(fmaxf(d2, 1e-30f)) * p.inv_h, 2.0f));
                     sum += (d2 < p.support2) ? w : 0.0f;
@@ -365,17 +278,20 @@ __global__ void __launch_bounds__(256, 6)
 
 // ------------------------------------------------------------------ force --
 // 256 threads, 4 blocks per SM: at most 64 registers
-template <int SYS, bool PLANAR, bool TRIM, int G>
+template <int SYS, bool PLANAR, bool TRIM, int G, bool BATCH>
 __global__ void __launch_bounds__(256, 4)
-    k_force(DevParams p, const float4 *__restrict__ spos, const float4 *__restrict__ svel,
-            const float2 *__restrict__ aux, const uint32_t *__restrict__ idx,
-            const uint32_t *__restrict__ off, float4 *__restrict__ out_a,
-            float4 *__restrict__ out_b)
+    k_force(DevParams pv, BatchView bv, const float4 *__restrict__ spos,
+            const float4 *__restrict__ svel, const float2 *__restrict__ aux,
+            const uint32_t *__restrict__ idx, const uint32_t *__restrict__ off_all,
+            float4 *__restrict__ out_a, float4 *__restrict__ out_b)
 {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t i = t / G;
+    const uint32_t i = (BATCH ? bv.first : 0u) + t / G;
     const int lane = (int)(t % G);
-    bool active = i < p.n;
+    const uint32_t n_all = BATCH ? bv.n_total : pv.n;
+    bool active = t / G < (BATCH ? bv.count : pv.n);
+    const DevParams &p = BATCH ? bv.scenes[active ? bv.scene_of[i] : bv.scene_of[bv.first]] : pv;
+    const uint32_t *off = off_all + p.table_base;
     const float4 pi = active ? spos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     // DamBreak: fluid particles only (fluid_kernel.cu:258)
     if (SYS == CMAG_DAMBREAK && pi.w != (float)CMAG_FLUID) active = false;
@@ -385,21 +301,16 @@ __global__ void __launch_bounds__(256, 4)
         const float2 ai = aux[i];
         const float pterm = ai.x;
         const int3 g = grid_pos(p, pi.x, pi.y, pi.z);
-        if (SYS == CMAG_DAMBREAK && p.kernel == CMAG_KERNEL_WENDLAND) {
-            float3 a = make_float3(0.0f, 0.0f, 0.0f);
-            for_each_run<SYS, PLANAR, TRIM, G>(
-                p, off, lane, g, frac_cell(p, pi), [&](uint32_t b, uint32_t e, float, float, float) {
-                    dambreak_force_run<TRIM>(p, spos, svel, aux, b, e, i, pi, vi, ai, a);
-                });
-            ax = a.x; ay = a.y; az = a.z;
-        } else
         for_each_candidate<SYS, PLANAR, TRIM, G>(
             p, off, lane, g, frac_cell(p, pi), [&](uint32_t j, float sx, float sy, float sz) {
                 if (j == i) return;
                 const float4 pj = __ldg(spos + j);
                 const float3 rv = rel<SYS>(pi, pj, sx, sy, sz);
                 const float rx = rv.x, ry = rv.y, rz = rv.z;
-                const float d2 = rx * rx + ry * ry + rz * rz;
+                const float d2 = __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, rx * rx));
+                // a coincident pair has no direction (the reference's terms turn into
+                // NaN there: 0 * inf); it contributes nothing
+                if (d2 == 0.0f) return;
                 if (SYS == CMAG_DAMBREAK) {
                     if (pj.w != (float)CMAG_FLUID) {
                         // Lennard-Jones wall force (fluid_kernel.cu:199-207)
@@ -407,8 +318,8 @@ __global__ void __launch_bounds__(256, 4)
                         const float inv_d2 = __frcp_rn(d2);
                         const float a2 = p.lj_a2 * inv_d2;
                         const float a6 = a2 * a2 * a2;
-                        const float s = p.lj_D * (a6 * a6 - a6) * inv_d2;
-                        ax += s * rx; ay += s * ry; az += s * rz;
+                        const float s = p.lj_D * __fmaf_rn(a6, a6, -a6) * inv_d2;
+                        ax = __fmaf_rn(s, rx, ax); ay = __fmaf_rn(s, ry, ay); az = __fmaf_rn(s, rz, az);
                         return;
                     }
                     if (!(d2 < p.support2)) return;
@@ -418,13 +329,14 @@ __global__ void __launch_bounds__(256, 4)
                     const float2 aj = __ldg(aux + j);
                     float s = pterm + aj.x;
                     const float4 vj = __ldg(svel + j);
-                    const float vij = (vi.x - vj.x) * rx + (vi.y - vj.y) * ry + (vi.z - vj.z) * rz;
+                    const float vij =
+                        __fmaf_rn(vi.z - vj.z, rz, __fmaf_rn(vi.y - vj.y, ry, (vi.x - vj.x) * rx));
                     if (vij < 0.0f) {
                         const float nu = __fdividef(p.av_coeff, ai.y + aj.y);
                         s -= __fdividef(nu * vij, d2 + p.av_eps2);
                     }
                     s *= -p.mass * temp * inv_d;
-                    ax += s * rx; ay += s * ry; az += s * rz;
+                    ax = __fmaf_rn(s, rx, ax); ay = __fmaf_rn(s, ry, ay); az = __fmaf_rn(s, rz, az);
                 } else if (SYS == CMAG_POISEUILLE) {
                     if (!(d2 < p.support2)) return;
                     // pressure + Morris viscosity with wall extrapolation
@@ -445,7 +357,9 @@ __global__ void __launch_bounds__(256, 4)
                     }
                     const float sp = -p.mass * (pterm + aj.x) * temp * inv_d;
                     const float sv = p.visc_coeff * temp * ai.y * aj.y * inv_d;
-                    ax += sp * rx + sv * vx; ay += sp * ry + sv * vy; az += sp * rz + sv * vz;
+                    ax = __fmaf_rn(sv, vx, __fmaf_rn(sp, rx, ax));
+                    ay = __fmaf_rn(sv, vy, __fmaf_rn(sp, ry, ay));
+                    az = __fmaf_rn(sv, vz, __fmaf_rn(sp, rz, az));
                 } else {
                     if (!(d2 < p.support2)) return;
                     // viscous (PeristalsisViscousForce.cu:206-213) and pressure
@@ -455,9 +369,11 @@ __global__ void __launch_bounds__(256, 4)
                     const float2 aj = __ldg(aux + j);
                     const float4 vj = __ldg(svel + j);
                     const float sv = p.visc_coeff * temp * ai.y * aj.y * inv_d;
-                    ax += sv * (vi.x - vj.x); ay += sv * (vi.y - vj.y); az += sv * (vi.z - vj.z);
+                    ax = __fmaf_rn(sv, vi.x - vj.x, ax);
+                    ay = __fmaf_rn(sv, vi.y - vj.y, ay);
+                    az = __fmaf_rn(sv, vi.z - vj.z, az);
                     const float sp = -p.mass * temp * (pterm + aj.x) * inv_d;
-                    bx += sp * rx; by += sp * ry; bz += sp * rz;
+                    bx = __fmaf_rn(sp, rx, bx); by = __fmaf_rn(sp, ry, by); bz = __fmaf_rn(sp, rz, bz);
                 }
             });
     }
@@ -469,78 +385,88 @@ __global__ void __launch_bounds__(256, 4)
     }
     if (active && lane == 0) {
         const uint32_t o = idx[i];
-        if (o >= p.n) return;  // only after a failed sort (reported by the sort itself)
+        if (o >= n_all) return;  // only after a failed sort (reported by the sort itself)
         out_a[o] = make_float4(ax, ay, az, 0.0f);
         if (SYS == CMAG_PERISTALSIS) out_b[o] = make_float4(bx, by, bz, 0.0f);
     }
 }
 
 template <int SYS, bool PLANAR, bool TRIM, int G>
-void launch_pair(bool force, const DevParams &p, const float4 *spos, const float4 *svel,
-                 float4 *meas, float2 *aux, const uint32_t *idx, const uint32_t *off, float4 *a,
-                 float4 *b, cudaStream_t st)
+void launch_pair(bool force, const DevParams &p, const BatchView &bv, const float4 *spos,
+                 const float4 *svel, float4 *meas, float2 *aux, const uint32_t *idx,
+                 const uint32_t *off, float4 *a, float4 *b, cudaStream_t st)
 {
-    const uint64_t threads = (uint64_t)p.n * G;
+    const uint64_t threads = (uint64_t)(bv.scenes ? bv.count : p.n) * G;
     const uint32_t blocks = (uint32_t)((threads + 255) / 256);
-    if (force)
-        k_force<SYS, PLANAR, TRIM, G><<<blocks, 256, 0, st>>>(p, spos, svel, aux, idx, off, a, b);
-    else
-        k_density<SYS, PLANAR, TRIM, G><<<blocks, 256, 0, st>>>(p, spos, off, meas, aux);
+    if (bv.scenes) {
+        if (force)
+            k_force<SYS, PLANAR, TRIM, G, true><<<blocks, 256, 0, st>>>(p, bv, spos, svel, aux, idx, off, a, b);
+        else
+            k_density<SYS, PLANAR, TRIM, G, true><<<blocks, 256, 0, st>>>(p, bv, spos, off, meas, aux);
+    } else {
+        if (force)
+            k_force<SYS, PLANAR, TRIM, G, false><<<blocks, 256, 0, st>>>(p, bv, spos, svel, aux, idx, off, a, b);
+        else
+            k_density<SYS, PLANAR, TRIM, G, false><<<blocks, 256, 0, st>>>(p, bv, spos, off, meas, aux);
+    }
 }
 
+struct PairArgs {
+    bool force;
+    const float4 *spos, *svel;
+    float4 *meas;
+    float2 *aux;
+    const uint32_t *idx, *off;
+    float4 *a, *b;
+};
+
 template <int SYS, bool PLANAR, bool TRIM>
-void dispatch_g(int group, bool force, const DevParams &p, const float4 *spos, const float4 *svel,
-                float4 *meas, float2 *aux, const uint32_t *idx, const uint32_t *off, float4 *a,
-                float4 *b, cudaStream_t st)
+void dispatch_g(int group, const DevParams &p, const BatchView &bv, const PairArgs &x, cudaStream_t st)
 {
     switch (group) {
-    case 2: launch_pair<SYS, PLANAR, TRIM, 2>(force, p, spos, svel, meas, aux, idx, off, a, b, st); break;
-    case 4: launch_pair<SYS, PLANAR, TRIM, 4>(force, p, spos, svel, meas, aux, idx, off, a, b, st); break;
-    default: launch_pair<SYS, PLANAR, TRIM, 1>(force, p, spos, svel, meas, aux, idx, off, a, b, st); break;
+    case 2: launch_pair<SYS, PLANAR, TRIM, 2>(x.force, p, bv, x.spos, x.svel, x.meas, x.aux, x.idx, x.off, x.a, x.b, st); break;
+    case 4: launch_pair<SYS, PLANAR, TRIM, 4>(x.force, p, bv, x.spos, x.svel, x.meas, x.aux, x.idx, x.off, x.a, x.b, st); break;
+    default: launch_pair<SYS, PLANAR, TRIM, 1>(x.force, p, bv, x.spos, x.svel, x.meas, x.aux, x.idx, x.off, x.a, x.b, st); break;
     }
 }
 
 template <int SYS>
-void dispatch(int group, bool force, const DevParams &p, const float4 *spos, const float4 *svel,
-              float4 *meas, float2 *aux, const uint32_t *idx, const uint32_t *off, float4 *a,
-              float4 *b, cudaStream_t st)
+void dispatch(int group, const DevParams &p, const BatchView &bv, const PairArgs &x, cudaStream_t st)
 {
     if (p.planar) {
-        if (p.trim) dispatch_g<SYS, true, true>(group, force, p, spos, svel, meas, aux, idx, off, a, b, st);
-        else dispatch_g<SYS, true, false>(group, force, p, spos, svel, meas, aux, idx, off, a, b, st);
+        if (p.trim) dispatch_g<SYS, true, true>(group, p, bv, x, st);
+        else dispatch_g<SYS, true, false>(group, p, bv, x, st);
     } else {
-        if (p.trim) dispatch_g<SYS, false, true>(group, force, p, spos, svel, meas, aux, idx, off, a, b, st);
-        else dispatch_g<SYS, false, false>(group, force, p, spos, svel, meas, aux, idx, off, a, b, st);
+        if (p.trim) dispatch_g<SYS, false, true>(group, p, bv, x, st);
+        else dispatch_g<SYS, false, false>(group, p, bv, x, st);
     }
 }
 
-void dispatch_sys(int group, bool force, const DevParams &p, const float4 *spos,
-                  const float4 *svel, float4 *meas, float2 *aux, const uint32_t *idx,
-                  const uint32_t *off, float4 *a, float4 *b, cudaStream_t st)
+// p: the scene's parameters, or for a batch launch group the parameters of any
+// scene of the group (family, planar and trim select the kernel variant)
+void dispatch_sys(int group, const DevParams &p, const BatchView &bv, const PairArgs &x,
+                  cudaStream_t st)
 {
-    if (p.n == 0) return;
-    if (p.system == CMAG_DAMBREAK)
-        dispatch<CMAG_DAMBREAK>(group, force, p, spos, svel, meas, aux, idx, off, a, b, st);
-    else if (p.system == CMAG_POISEUILLE)
-        dispatch<CMAG_POISEUILLE>(group, force, p, spos, svel, meas, aux, idx, off, a, b, st);
-    else
-        dispatch<CMAG_PERISTALSIS>(group, force, p, spos, svel, meas, aux, idx, off, a, b, st);
+    if ((bv.scenes ? bv.count : p.n) == 0) return;
+    if (p.system == CMAG_DAMBREAK) dispatch<CMAG_DAMBREAK>(group, p, bv, x, st);
+    else if (p.system == CMAG_POISEUILLE) dispatch<CMAG_POISEUILLE>(group, p, bv, x, st);
+    else dispatch<CMAG_PERISTALSIS>(group, p, bv, x, st);
 }
 
 }  // namespace
 
-void launch_density(const DevParams &p, int group, const float4 *spos, const uint32_t *off,
-                    float4 *meas, float2 *aux, cudaStream_t st)
+void launch_density(const DevParams &p, const BatchView &bv, int group, const float4 *spos,
+                    const uint32_t *off, float4 *meas, float2 *aux, cudaStream_t st)
 {
-    dispatch_sys(group, false, p, spos, nullptr, meas, aux, nullptr, off, nullptr, nullptr, st);
+    dispatch_sys(group, p, bv, PairArgs{false, spos, nullptr, meas, aux, nullptr, off, nullptr, nullptr}, st);
 }
 
-void launch_force(const DevParams &p, int group, const float4 *spos, const float4 *svel,
-                  const float2 *aux, const uint32_t *idx, const uint32_t *off, float4 *out_a,
-                  float4 *out_b, cudaStream_t st)
+void launch_force(const DevParams &p, const BatchView &bv, int group, const float4 *spos,
+                  const float4 *svel, const float2 *aux, const uint32_t *idx, const uint32_t *off,
+                  float4 *out_a, float4 *out_b, cudaStream_t st)
 {
-    dispatch_sys(group, true, p, spos, svel, nullptr, const_cast<float2 *>(aux), idx, off, out_a,
-                 out_b, st);
+    dispatch_sys(group, p, bv,
+                 PairArgs{true, spos, svel, nullptr, const_cast<float2 *>(aux), idx, off, out_a, out_b}, st);
 }
 
 }  // namespace cmag

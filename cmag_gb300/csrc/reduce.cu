@@ -71,6 +71,50 @@ __global__ void __launch_bounds__(256) k_fluid_sum(int32_t system, const float4 
     }
 }
 
+// Per-scene extents of a batch: out[6 s .. 6 s + 5] as in k_extent.  Scenes are
+// contiguous, so a warp almost always holds one scene and reduces before its
+// atomics; a warp that straddles scenes falls back to one atomic per lane.
+__global__ void __launch_bounds__(256) k_extent_batch(BatchView bv, const float4 *__restrict__ pos,
+                                                      uint32_t *out)
+{
+    const uint32_t n = bv.n_total, stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+        const uint32_t i = base + threadIdx.x;
+        const bool valid = i < n;
+        const uint32_t s = valid ? bv.scene_of[i] : 0xffffffffu;
+        float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+        bool fluid = false;
+        if (valid) {
+            q = pos[i];
+            fluid = is_fluid(bv.scenes[s].system, q.w);
+        }
+        float lo[3] = {fluid ? q.x : 3.4e38f, fluid ? q.y : 3.4e38f, fluid ? q.z : 3.4e38f};
+        float hi[3] = {fluid ? q.x : -3.4e38f, fluid ? q.y : -3.4e38f, fluid ? q.z : -3.4e38f};
+        const uint32_t s0 = __shfl_sync(0xffffffffu, s, 0);
+        const bool uniform = __all_sync(0xffffffffu, s == s0 || !valid);
+        if (uniform) {
+            const bool any = __any_sync(0xffffffffu, fluid);
+            if (!any) continue;
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+                for (int o = 16; o > 0; o >>= 1) {
+                    lo[k] = fminf(lo[k], __shfl_xor_sync(0xffffffffu, lo[k], o));
+                    hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xffffffffu, hi[k], o));
+                }
+            if ((threadIdx.x & 31) == 0)
+                for (int k = 0; k < 3; ++k) {
+                    atomicMin(&out[6 * s0 + k], fkey(lo[k]));
+                    atomicMax(&out[6 * s0 + 3 + k], fkey(hi[k]));
+                }
+        } else if (fluid) {
+            for (int k = 0; k < 3; ++k) {
+                atomicMin(&out[6 * s + k], fkey(lo[k]));
+                atomicMax(&out[6 * s + 3 + k], fkey(hi[k]));
+            }
+        }
+    }
+}
+
 uint32_t blocks_for(uint32_t n)
 {
     uint32_t b = (n + 255) / 256;
@@ -83,6 +127,11 @@ void launch_fluid_extent(int32_t system, const float4 *pos, uint32_t n, uint32_t
                          cudaStream_t st)
 {
     k_extent<<<blocks_for(n), 256, 0, st>>>(system, pos, n, out6);
+}
+
+void launch_fluid_extents_batch(const BatchView &bv, const float4 *pos, uint32_t *out, cudaStream_t st)
+{
+    k_extent_batch<<<blocks_for(bv.n_total), 256, 0, st>>>(bv, pos, out);
 }
 
 void launch_fluid_sum(int32_t system, const float4 *type_src, const float4 *a, uint32_t n,

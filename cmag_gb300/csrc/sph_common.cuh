@@ -15,7 +15,7 @@ constexpr uint32_t kEmptyCell = 0xffffffffu;
 // plus coefficients the host derives once (kernel normalisation, clamps).
 struct DevParams {
     int32_t system, dims, kernel, eos;
-    uint32_t gx, gy, gz;          // grid cells per axis (powers of two)
+    uint32_t gx, gy, gz;          // grid cells per axis
     uint32_t n;                   // particles
     uint32_t scan_base;           // first cell covered by the dense offset table
     uint32_t scan_cells;          // cells covered (one z layer for planar scenes)
@@ -48,6 +48,24 @@ struct DevParams {
     float lj_a2;                  // a^2 of the wall force
     float av_coeff;               // 2 alpha h c0 (fluid_kernel.cu:229-230)
     float visc_coeff;             // m (mu + mu) (poiseuilleFlowKernel.cu:242-243)
+    // batches: where this scene's cell table and particles start in the shared arrays
+    uint32_t table_base;
+    uint32_t part_base;
+};
+
+// Several independent scenes advanced by the same launches: the per-scene
+// parameter blocks and the scene of every particle.  Scene s owns particles
+// [part_base, part_base + n) and cells [table_base, table_base + scan_cells) of
+// the shared arrays; its sort keys are table_base + cell, so the sort keeps every
+// scene inside its own particle range and scene_of serves the original and the
+// sorted order alike.  A neighbour-loop launch covers one launch group (scenes of
+// one family and search shape): particles [first, first + count).  Empty
+// (scenes == nullptr) for a single scene, whose parameters travel by value.
+struct BatchView {
+    const DevParams *scenes;
+    const uint16_t *scene_of;
+    uint32_t n_total;
+    uint32_t first, count;
 };
 
 // Device-resident per-step scalars of the Peristalsis phase machine
@@ -118,9 +136,9 @@ __device__ __forceinline__ int eval_shift(int pos, uint32_t size)
 __device__ __forceinline__ float kernel_w(const DevParams &p, float q)
 {
     if (p.kernel == CMAG_KERNEL_WENDLAND) {
-        float t = 1.0f - 0.5f * q;
+        float t = __fmaf_rn(q, -0.5f, 1.0f);  // = 1 - q/2 (q/2 is exact)
         float t2 = t * t;
-        return p.w_norm * (t2 * t2) * (2.0f * q + 1.0f);
+        return p.w_norm * (t2 * t2) * __fmaf_rn(q, 2.0f, 1.0f);
     }
     if (q < 1.0f) return p.w_norm * (1.0f - 1.5f * q * q + 0.75f * q * q * q);
     float t = 2.0f - q;
@@ -133,7 +151,7 @@ __device__ __forceinline__ float kernel_w(const DevParams &p, float q)
 __device__ __forceinline__ float kernel_dw(const DevParams &p, float q)
 {
     if (p.kernel == CMAG_KERNEL_WENDLAND) {
-        float t = 1.0f - 0.5f * q;
+        float t = __fmaf_rn(q, -0.5f, 1.0f);
         return -2.5f * p.dw_norm * q * (t * t * t);
     }
     if (q < 1.0f) return p.dw_norm * (-3.0f * q + 2.25f * q * q);

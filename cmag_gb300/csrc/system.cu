@@ -14,6 +14,7 @@
 #include <string>
 #include <vector>
 
+#include "host_common.h"
 #include "host_scenes.h"
 #include "kernels.h"
 
@@ -71,28 +72,14 @@ struct cmag_system {
     std::string last_error;
 };
 
+namespace cmag {
+
 namespace {
-
 thread_local std::string g_last_error;
-
-int fail(cmag_system *s, int code, const std::string &msg)
-{
-    if (s) s->last_error = msg;
-    g_last_error = msg;
-    return code;
 }
 
-// On failure: report, and clear the runtime's (non-sticky) last error so that it
-// does not surface later in an unrelated caller's CUDA call.
-#define CM_CUDA(s, call)                                                                    \
-    do {                                                                                    \
-        cudaError_t e_ = (call);                                                            \
-        if (e_ != cudaSuccess) {                                                            \
-            (void)cudaGetLastError();                                                       \
-            return fail((s), e_ == cudaErrorMemoryAllocation ? CMAG_ERR_NOMEM : CMAG_ERR_CUDA, \
-                        std::string(#call) + ": " + cudaGetErrorString(e_));                \
-        }                                                                                   \
-    } while (0)
+void set_last_error(const std::string &msg) { g_last_error = msg; }
+const std::string &last_error() { return g_last_error; }
 
 bool is_pow2(uint32_t v) { return v && !(v & (v - 1)); }
 
@@ -103,7 +90,7 @@ uint32_t log2u(uint64_t v)
     return b;
 }
 
-int validate(const cmag_sph_params &p, uint32_t n, std::string &why)
+int validate_params(const cmag_sph_params &p, uint32_t n, std::string &why)
 {
     if (p.system < CMAG_DAMBREAK || p.system > CMAG_PERISTALSIS) return why = "unknown system", 1;
     for (int k = 0; k < 3; ++k)
@@ -131,18 +118,19 @@ int validate(const cmag_sph_params &p, uint32_t n, std::string &why)
     return 0;
 }
 
+namespace {
 const double kPi = 3.14159265358979323846;
+}
 
-DevParams make_dev(const cmag_system *s)
+DevParams make_dev_params(const cmag_sph_params &p, uint32_t n, const SceneLayout &lay)
 {
-    const cmag_sph_params &p = s->p;
     DevParams d;
     std::memset(&d, 0, sizeof(d));
     d.system = p.system; d.dims = p.dims; d.kernel = p.kernel; d.eos = p.eos;
     d.gx = p.grid_size[0]; d.gy = p.grid_size[1]; d.gz = p.grid_size[2];
-    d.n = s->n;
-    d.scan_base = s->scan_base;
-    d.scan_cells = s->scan_cells;
+    d.n = n;
+    d.scan_base = lay.scan_base;
+    d.scan_cells = lay.scan_cells;
     d.ox = p.world_origin[0]; d.oy = p.world_origin[1]; d.oz = p.world_origin[2];
     d.csx = p.cell_size[0]; d.csy = p.cell_size[1]; d.csz = p.cell_size[2];
     d.r = p.particle_radius;
@@ -155,7 +143,7 @@ DevParams make_dev(const cmag_system *s)
     d.mu = p.mu;
     d.gvx = p.gravity[0]; d.gvy = p.gravity[1]; d.gvz = p.gravity[2];
     d.cell_count = p.cell_count;
-    d.planar = s->planar ? 1 : 0;
+    d.planar = lay.planar ? 1 : 0;
     // rows can be trimmed to the support sphere unless some interaction reaches
     // past q = 2 (the reference DamBreak wall force has no cut-off)
     d.trim = (p.system != CMAG_DAMBREAK || p.lj_cutoff) ? 1 : 0;
@@ -200,14 +188,13 @@ DevParams make_dev(const cmag_system *s)
     // trimming works in cell units: it needs cubic cells
     if (!(p.cell_size[0] == p.cell_size[1] && p.cell_size[1] == p.cell_size[2])) d.trim = 0;
     d.pow2_grid = (is_pow2(p.grid_size[0]) && is_pow2(p.grid_size[1]) && is_pow2(p.grid_size[2])) ? 1u : 0u;
-    d.planar_layer = s->planar_layer;
+    d.planar_layer = lay.planar_layer;
     d.lj_a2 = p.lj_a * p.lj_a;
     d.av_coeff = (float)(2.0 * p.av_alpha * h * p.soundspeed);
     d.visc_coeff = (float)((double)p.particle_mass * (2.0 * p.mu));
     return d;
 }
 
-// z cell of a position, as the hash computes it
 int z_cell(const cmag_sph_params &p, float z)
 {
     float c = (p.system == CMAG_DAMBREAK) ? std::floor((z - p.world_origin[2]) / p.cell_size[2])
@@ -218,6 +205,63 @@ int z_cell(const cmag_sph_params &p, float z)
     return (int)c;
 }
 
+bool planar_allowed(const cmag_sph_params &p, bool z_uniform, bool vz_nonzero)
+{
+    return p.dims == 2 && z_uniform && !vz_nonzero && p.gravity[2] == 0.0f &&
+           (int)p.grid_size[2] > p.cell_count;
+}
+
+SceneLayout layout_for(const cmag_sph_params &p, bool planar, float z_value)
+{
+    SceneLayout l;
+    l.planar = planar;
+    l.scan_cells = p.grid_size[0] * p.grid_size[1] * p.grid_size[2];
+    if (planar) {
+        const int64_t zc = z_cell(p, z_value), nz = p.grid_size[2];
+        l.planar_layer = (uint32_t)(((zc % nz) + nz) % nz);
+        l.scan_cells = p.grid_size[0] * p.grid_size[1];
+        l.scan_base = l.planar_layer * l.scan_cells;
+    }
+    return l;
+}
+
+}  // namespace cmag
+
+namespace {
+
+int fail(cmag_system *s, int code, const std::string &msg)
+{
+    if (s) s->last_error = msg;
+    set_last_error(msg);
+    return code;
+}
+
+// On failure: report, and clear the runtime's (non-sticky) last error so that it
+// does not surface later in an unrelated caller's CUDA call.
+#define CM_CUDA(s, call)                                                                    \
+    do {                                                                                    \
+        cudaError_t e_ = (call);                                                            \
+        if (e_ != cudaSuccess) {                                                            \
+            (void)cudaGetLastError();                                                       \
+            return fail((s), e_ == cudaErrorMemoryAllocation ? CMAG_ERR_NOMEM : CMAG_ERR_CUDA, \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                \
+        }                                                                                   \
+    } while (0)
+
+int validate(const cmag_sph_params &p, uint32_t n, std::string &why) { return validate_params(p, n, why); }
+
+SceneLayout layout_of(const cmag_system *s)
+{
+    SceneLayout l;
+    l.planar = s->planar;
+    l.planar_layer = s->planar_layer;
+    l.scan_base = s->scan_base;
+    l.scan_cells = s->scan_cells;
+    return l;
+}
+
+DevParams make_dev(const cmag_system *s) { return make_dev_params(s->p, s->n, layout_of(s)); }
+
 void invalidate_graph(cmag_system *s)
 {
     if (s->gexec) cudaGraphExecDestroy(s->gexec);
@@ -225,27 +269,16 @@ void invalidate_graph(cmag_system *s)
     s->gvalid = false;
 }
 
-// Planar 2-D scenes (every particle at one z, no z motion) search and scan only
-// their own z layer; the result equals the full search whenever the grid has
-// more than cell_count layers (the layer is then reached only with dz = 0 and
-// every other layer is empty).
+// Planar 2-D scenes search and scan only their own z layer (planar_allowed).
 void refresh_layout(cmag_system *s)
 {
-    const cmag_sph_params &p = s->p;
-    bool planar = p.dims == 2 && s->z_uniform && !s->vz_nonzero && p.gravity[2] == 0.0f &&
-                  (int)p.grid_size[2] > p.cell_count;
-    uint32_t base = 0, cells = (uint32_t)s->ncells, layer = 0;
-    if (planar) {
-        const int64_t zc = z_cell(p, s->z_value), nz = p.grid_size[2];
-        layer = (uint32_t)(((zc % nz) + nz) % nz);
-        cells = p.grid_size[0] * p.grid_size[1];
-        base = layer * cells;
-    }
-    if (planar != s->planar || base != s->scan_base || cells != s->scan_cells) invalidate_graph(s);
-    s->planar = planar;
-    s->planar_layer = layer;
-    s->scan_base = base;
-    s->scan_cells = cells;
+    const SceneLayout l = layout_for(s->p, planar_allowed(s->p, s->z_uniform, s->vz_nonzero), s->z_value);
+    if (l.planar != s->planar || l.scan_base != s->scan_base || l.scan_cells != s->scan_cells)
+        invalidate_graph(s);
+    s->planar = l.planar;
+    s->planar_layer = l.planar_layer;
+    s->scan_base = l.scan_base;
+    s->scan_cells = l.scan_cells;
 }
 
 cudaStream_t st_of(cmag_system *s) { return s->stream; }
@@ -279,12 +312,12 @@ int record_step(cmag_system *s, int last, bool timed)
 
     if (p.system == CMAG_PERISTALSIS) {
         launch_phase(d, s->phase, s->k_milli, st);
-        launch_configure_boundary(d, s->pos, s->phase, st);
+        launch_configure_boundary(d, BatchView{}, s->pos, s->phase, st);
     }
     mark(0);
     CM_CUDA(s, cudaMemsetAsync(s->ws, 0, s->ws_words * sizeof(uint32_t), st));
     SortWorkspace sw = sort_workspace_view(s->ws, s->n);
-    launch_hash(d, s->pos, s->hash[0], s->cnt, sw.hist, s->passes, s->err, st);
+    launch_hash(d, BatchView{}, s->pos, s->hash[0], s->cnt, sw.hist, s->passes, s->err, st);
     launch_cell_scan(s->cnt, s->off, s->scan_cells + 1, s->ws + s->sort_words, s->err, st);
     mark(1);
     if (last >= CMAG_STAGE_SORT) {
@@ -299,19 +332,19 @@ int record_step(cmag_system *s, int last, bool timed)
         launch_reorder(sorted_idx(s), s->pos, s->vlf, s->spos, s->svel, s->n, st);
     mark(3);
     if (last >= CMAG_STAGE_DENSITY)
-        launch_density(d, s->g_density, s->spos, s->off, s->meas, s->aux, st);
+        launch_density(d, BatchView{}, s->g_density, s->spos, s->off, s->meas, s->aux, st);
     mark(4);
     if (last >= CMAG_STAGE_FORCE) {
         if (p.system == CMAG_PERISTALSIS)
-            launch_force(d, s->g_force, s->spos, s->svel, s->aux, sorted_idx(s), s->off,
+            launch_force(d, BatchView{}, s->g_force, s->spos, s->svel, s->aux, sorted_idx(s), s->off,
                          s->vforce, s->pforce, st);
         else
-            launch_force(d, s->g_force, s->spos, s->svel, s->aux, sorted_idx(s), s->off, s->acc,
+            launch_force(d, BatchView{}, s->g_force, s->spos, s->svel, s->aux, sorted_idx(s), s->off, s->acc,
                          nullptr, st);
     }
     mark(5);
     if (last >= CMAG_STAGE_INTEGRATE)
-        launch_integrate(d, s->pos, s->vel, s->vlf, s->acc, s->vforce, s->pforce, s->phase, st);
+        launch_integrate(d, BatchView{}, s->pos, s->vel, s->vlf, s->acc, s->vforce, s->pforce, s->phase, st);
     mark(6);
     CM_CUDA(s, cudaGetLastError());
     return CMAG_OK;
@@ -449,11 +482,11 @@ const char *cmag_version(void) { return "cmag_gb300 0.1 (sm_103a)"; }
 
 size_t cmag_sph_params_size(void) { return sizeof(cmag_sph_params); }
 
-const char *cmag_last_error(void) { return g_last_error.c_str(); }
+const char *cmag_last_error(void) { return last_error().c_str(); }
 
 const char *cmag_system_last_error(const cmag_system *s)
 {
-    return s ? s->last_error.c_str() : g_last_error.c_str();
+    return s ? s->last_error.c_str() : last_error().c_str();
 }
 
 int cmag_dambreak_default_params(const uint32_t fluid_size[3], int32_t boundary_offset,
@@ -596,7 +629,7 @@ int cmag_system_create(const cmag_sph_params *params, uint32_t n, cmag_system **
         std::string msg = s->last_error;
         free_all(s);
         delete s;
-        g_last_error = msg;
+        set_last_error(msg);
         return rc;
     }
     s->host_phase.is_bc = params->is_boundary_configuration;
@@ -1074,21 +1107,21 @@ int cmag_system_autotune(cmag_system *s, int32_t reps)
     float4 *fa = s->p.system == CMAG_PERISTALSIS ? s->vforce : s->acc;
     float4 *fb = s->p.system == CMAG_PERISTALSIS ? s->pforce : nullptr;
     for (int k = 0; k < 3; ++k) {
-        launch_density(d, groups[k], s->spos, s->off, s->meas, s->aux, st);  // warm
+        launch_density(d, BatchView{}, groups[k], s->spos, s->off, s->meas, s->aux, st);  // warm
         cudaEventRecord(a, st);
-        for (int r = 0; r < reps; ++r) launch_density(d, groups[k], s->spos, s->off, s->meas, s->aux, st);
+        for (int r = 0; r < reps; ++r) launch_density(d, BatchView{}, groups[k], s->spos, s->off, s->meas, s->aux, st);
         cudaEventRecord(b, st);
         cudaEventSynchronize(b);
         float ms = 0;
         cudaEventElapsedTime(&ms, a, b);
         if (ms < best_d) { best_d = ms; gd = groups[k]; }
     }
-    launch_density(d, gd, s->spos, s->off, s->meas, s->aux, st);
+    launch_density(d, BatchView{}, gd, s->spos, s->off, s->meas, s->aux, st);
     for (int k = 0; k < 3; ++k) {
-        launch_force(d, groups[k], s->spos, s->svel, s->aux, sorted_idx(s), s->off, fa, fb, st);
+        launch_force(d, BatchView{}, groups[k], s->spos, s->svel, s->aux, sorted_idx(s), s->off, fa, fb, st);
         cudaEventRecord(a, st);
         for (int r = 0; r < reps; ++r)
-            launch_force(d, groups[k], s->spos, s->svel, s->aux, sorted_idx(s), s->off, fa, fb, st);
+            launch_force(d, BatchView{}, groups[k], s->spos, s->svel, s->aux, sorted_idx(s), s->off, fa, fb, st);
         cudaEventRecord(b, st);
         cudaEventSynchronize(b);
         float ms = 0;

@@ -9,6 +9,8 @@ Benchmark workloads (synthetic, seeded):
   * poiseuille_c1():   2-D Poiseuille, 64x64 fluid, 3 wall rows, periodic x
   * dambreak3d():      3-D dam break, 64x128x64 = 524,288 fluid, 3 wall layers
   * peristalsis_c3():  2-D peristaltic channel, 2048x512 = 1,048,576 fluid, 4 waves
+  * batched_scenes():  256 independent 2-D scenes (128 Poiseuille, 128 dam breaks),
+                       fluid counts log-uniform in [4096, 262144]
 """
 import ctypes
 import math
@@ -179,3 +181,55 @@ def peristalsis_c3(fluid=(2048, 512), amplitude_frac=0.3, waves=4, reynolds=10.0
                            off, (gx, gy, 4), r)
     p.wave_count = float(waves)
     return p
+
+
+def batched_scenes(scenes=256, seed=1973, lo=4096, hi=262144, nu_lo=1e-6, nu_hi=1e-4):
+    """Batch of independent 2-D scenes: the first half Poiseuille channels, the
+    second half dam breaks.  Fluid particle counts are drawn log-uniform in
+    [lo, hi] and the kinematic viscosity of each channel log-uniform in
+    [nu_lo, nu_hi] from `seed`.
+
+    Poiseuille (the reference channel, Poiseuille.Report/dump.h): fy rows across a
+    1 mm channel (fy = sqrt(count)), fx = count / fy columns along the periodic x
+    axis, 3 wall rows each side, grid (fx, fy + 12, 4); mu = 1000 nu and the body
+    force 1e-4 nu / 1e-6, so every channel has the reference's u_max = F l^2 / (8 nu)
+    = 1.25e-5 m/s; dt = min(1e-4, 0.125 h^2 / nu).
+    Dam break (the reference column, DamBreak.Report/XFrontTest.h:17-23): a num x
+    2num column (num = sqrt(count / 2)) in a 4num x 2num x 4 grid at radius
+    1/(2 num), gravity -9.8, reference artificial viscosity and walls.  The
+    reference's particle mass and dt (1e-4) belong to its num = 128 column
+    (fluidSystem.cpp:17-77); here the mass scales with the particle area,
+    (128 / num)^2, so every column has the reference's rest density, and dt with
+    the spacing at half the reference's CFL number, 1e-4 * 64 / num: the columns
+    are released at t = 0 without the reference's 1.5 s of settling.
+
+    Returns (params list, particle counts, fluid counts, per-scene description)."""
+    rng = np.random.default_rng(seed)
+    half = scenes // 2
+    out_p, out_n, out_f, desc = [], [], [], []
+    for k in range(scenes):
+        target = float(np.exp(rng.uniform(np.log(lo), np.log(hi))))
+        nu = float(np.exp(rng.uniform(np.log(nu_lo), np.log(nu_hi))))
+        if k < half:
+            off = 3
+            fy = max(16, int(round(math.sqrt(target))))
+            fx = max(16, int(round(target / fy)))
+            r = 1.0 / (2 * fy * 1000)
+            p = poiseuille_params((fx, fy, 1), off, (fx, fy + 2 * off + 6, 4), r)
+            p.mu = F32(1000.0 * nu)
+            p.gravity[0] = F32(1e-4 * nu / 1e-6)
+            h = float(p.smoothing_radius)
+            p.delta_time = F32(min(1e-4, 0.125 * h * h / nu))
+            fluid = fx * fy
+            desc.append(("poiseuille", fx, fy, nu))
+        else:
+            num = max(16, int(round(math.sqrt(target / 2))))
+            p = dambreak_params((num, 2 * num, 1), 1, (4 * num, 2 * num, 4), 1.0 / (2 * num))
+            p.particle_mass = F32(float(p.particle_mass) * (128.0 / num) ** 2)
+            p.delta_time = F32(1e-4 * 64 / num)
+            fluid = 2 * num * num
+            desc.append(("dambreak", num, 2 * num, nu))
+        out_p.append(p)
+        out_n.append(reference_count(p))
+        out_f.append(fluid)
+    return out_p, out_n, out_f, desc

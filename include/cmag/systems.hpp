@@ -14,6 +14,7 @@
 #include <stdexcept>
 #include <string>
 #include <utility>
+#include <vector>
 
 #include <vector_functions.h>
 #include <vector_types.h>
@@ -224,3 +225,60 @@ public:
     void *pressure_force() const { return cmag_system_device_array(h_, CMAG_PRESSUREFORCE); }
     void *getPredictedPos() const { return cmag_system_device_array(h_, CMAG_PREDICTEDPOSITION); }
 };
+
+namespace cmag {
+
+// Many independent scenes advanced together (cmag_batch_*); no reference
+// counterpart.  Scene indices are the positions in the constructor's vectors.
+class Batch {
+public:
+    Batch(const std::vector<cmag_sph_params> &params, const std::vector<uint32_t> &counts)
+    {
+        if (params.size() != counts.size()) throw Error(CMAG_ERR_INVALID, "one particle count per scene");
+        check(cmag_batch_create(params.data(), counts.data(), (uint32_t)params.size(), &h_));
+    }
+    Batch(const Batch &) = delete;
+    Batch &operator=(const Batch &) = delete;
+    ~Batch() { cmag_batch_destroy(h_); }
+
+    cmag_batch *handle() const { return h_; }
+    uint32_t numScenes() const { uint32_t v = 0; chk(cmag_batch_num_scenes(h_, &v)); return v; }
+    uint32_t numParticles() const { uint32_t v = 0; chk(cmag_batch_num_particles(h_, &v)); return v; }
+    std::pair<uint32_t, uint32_t> sceneRange(uint32_t scene) const
+    {
+        uint32_t a = 0, n = 0;
+        chk(cmag_batch_scene_range(h_, scene, &a, &n));
+        return {a, n};
+    }
+    void reset() { chk(cmag_batch_reset(h_)); }
+    void reset(uint32_t scene) { chk(cmag_batch_reset_scene(h_, scene)); }
+    void update() { chk(cmag_batch_update(h_)); }
+    void update(uint32_t steps) { chk(cmag_batch_update_n(h_, steps)); }
+    void setArray(uint32_t scene, int array, const float *data, int start, int count)
+    {
+        chk(cmag_batch_set_array(h_, scene, array, data, (uint32_t)start, (uint32_t)count));
+    }
+    void getArray(uint32_t scene, int array, float *data, int start, int count) const
+    {
+        chk(cmag_batch_get_array(h_, scene, array, data, (uint32_t)start, (uint32_t)count));
+    }
+    void *deviceArray(int array) const { return cmag_batch_device_array(h_, array); }
+    float elapsedTime(uint32_t scene) const { float t = 0; chk(cmag_batch_elapsed_time(h_, scene, &t)); return t; }
+    void removeRightBoundary(uint32_t scene) { chk(cmag_batch_dambreak_remove_right_boundary(h_, scene)); }
+    void changeRightBoundary(uint32_t scene) { chk(cmag_batch_dambreak_change_right_boundary(h_, scene)); }
+    void changeGravity(uint32_t scene) { chk(cmag_batch_poiseuille_change_gravity(h_, scene)); }
+    // fluid bounding boxes of every scene (scenes * 3 floats each)
+    void fluidExtents(float *lo, float *hi) const { chk(cmag_batch_fluid_extents(h_, lo, hi)); }
+    void setGraphs(bool enable, uint32_t stepsPerGraph = 1) { chk(cmag_batch_set_graphs(h_, enable ? 1 : 0, stepsPerGraph)); }
+    void autotune(int reps = 3) { chk(cmag_batch_autotune(h_, reps)); }
+    void synchronize() { chk(cmag_batch_synchronize(h_)); }
+
+private:
+    void chk(int rc) const
+    {
+        if (rc != CMAG_OK) throw Error(rc, cmag_batch_last_error(h_));
+    }
+    cmag_batch *h_ = nullptr;
+};
+
+}  // namespace cmag

@@ -342,6 +342,86 @@ int cmag_sort_particles_noalloc(uint32_t *d_hash, uint32_t *d_index, uint32_t n,
                                 uint32_t key_bits, void *cuda_stream);
 const char *cmag_sort_particles_noalloc_error(void);
 
+/* ---- batches of independent scenes -------------------------------------- */
+/* No counterpart in the reference, which runs one scene per process (its kernels
+ * read one global __constant__ parameter block per library: fluidSystem.cu:17-19,
+ * poiseuilleFlowSystem.cu:19-21, PeristalsisSystem.cu:21-23).  A batch advances
+ * S scenes of any families and sizes with one set of launches per step (one hash,
+ * scan, sort, gather and integration; one density and one force launch per launch
+ * group), captured as one CUDA graph.  Each scene follows exactly the arithmetic
+ * of a cmag_system with the same parameters and lanes, so its trajectory equals
+ * that system's bit for bit.
+ *  - Scenes are addressed by their index in the create call.  Particle arrays
+ *    are scene-local in set/get_array; the device arrays hold scene s at
+ *    [first, first + count) (cmag_batch_scene_range).
+ *  - A 2-D scene with zero z gravity and more than cell_count z layers is
+ *    planar: its particles must share one z and have no z velocity (set_array
+ *    refuses other data); its cell table covers that z layer only.
+ *  - Launch groups: scenes of one family, search shape and factor-4 size class;
+ *    each has its own lanes per particle (cmag_batch_autotune). */
+typedef struct cmag_batch cmag_batch;
+
+typedef struct cmag_batch_group {
+    int32_t system;          /* enum cmag_system_kind                     */
+    int32_t planar;          /* 1: single z layer search                  */
+    int32_t trim;            /* 1: rows trimmed to the support sphere     */
+    uint32_t size_bucket;    /* scenes with 2^(2k-1) < n <= 2^(2k+1)       */
+    uint32_t scenes;
+    uint32_t particles;
+    int32_t density_lanes;
+    int32_t force_lanes;
+} cmag_batch_group;
+
+int cmag_batch_create(const cmag_sph_params *params, const uint32_t *counts, uint32_t scenes,
+                      cmag_batch **out);
+int cmag_batch_destroy(cmag_batch *b);
+int cmag_batch_num_scenes(const cmag_batch *b, uint32_t *out);
+int cmag_batch_num_particles(const cmag_batch *b, uint32_t *out);
+int cmag_batch_scene_range(cmag_batch *b, uint32_t scene, uint32_t *first, uint32_t *count);
+/* every scene's / one scene's reference initial state (cmag_system_reset) */
+int cmag_batch_reset(cmag_batch *b);
+int cmag_batch_reset_scene(cmag_batch *b, uint32_t scene);
+int cmag_batch_set_array(cmag_batch *b, uint32_t scene, int32_t array, const float *host,
+                         uint32_t start, uint32_t count);
+int cmag_batch_get_array(cmag_batch *b, uint32_t scene, int32_t array, float *host,
+                         uint32_t start, uint32_t count);
+/* scene-local: HASH = the scene's reference hash, INDEX = scene-local original
+ * index, CELLOFFSET = offsets over the scene's table (scan_cells + 1 entries),
+ * CELLSTART / CELLEND = the reference arrays over the scene's grid */
+int cmag_batch_get_uint_array(cmag_batch *b, uint32_t scene, int32_t array, uint32_t *host,
+                              uint32_t start, uint32_t count);
+/* whole-batch device array (NULL for arrays the batch does not hold) */
+void *cmag_batch_device_array(cmag_batch *b, int32_t array);
+int cmag_batch_get_params(cmag_batch *b, uint32_t scene, cmag_sph_params *out);
+/* family, grid size and search shape are fixed at creation */
+int cmag_batch_set_params(cmag_batch *b, uint32_t scene, const cmag_sph_params *p);
+int cmag_batch_update(cmag_batch *b);
+int cmag_batch_update_n(cmag_batch *b, uint32_t steps);
+int cmag_batch_timed_update(cmag_batch *b, uint32_t steps, float *ms_out);
+int cmag_batch_run_stages(cmag_batch *b, int32_t last_stage);
+int cmag_batch_elapsed_time(cmag_batch *b, uint32_t scene, float *out);
+int cmag_batch_dambreak_change_right_boundary(cmag_batch *b, uint32_t scene);
+int cmag_batch_dambreak_remove_right_boundary(cmag_batch *b, uint32_t scene);
+int cmag_batch_poiseuille_change_gravity(cmag_batch *b, uint32_t scene);
+/* fluid extents of every scene from one reduction: lo/hi hold scenes*3 floats */
+int cmag_batch_fluid_extents(cmag_batch *b, float *lo, float *hi);
+int cmag_batch_set_stream(cmag_batch *b, void *cuda_stream);
+void *cmag_batch_stream(const cmag_batch *b);
+/* graphs on/off; steps_per_graph (1..1024) steps are captured in one graph */
+int cmag_batch_set_graphs(cmag_batch *b, int32_t enable, uint32_t steps_per_graph);
+int cmag_batch_synchronize(cmag_batch *b);
+int cmag_batch_device_error_bits(cmag_batch *b, uint32_t *bits);
+int cmag_batch_num_groups(const cmag_batch *b, uint32_t *out);
+int cmag_batch_group_info(cmag_batch *b, uint32_t group, cmag_batch_group *out);
+int cmag_batch_scene_group(cmag_batch *b, uint32_t scene, uint32_t *group);
+int cmag_batch_set_group_lanes(cmag_batch *b, uint32_t group, int32_t density_lanes,
+                               int32_t force_lanes);
+/* per launch group, the fastest lanes per particle for density and force */
+int cmag_batch_autotune(cmag_batch *b, int32_t reps);
+int cmag_batch_set_stage_timing(cmag_batch *b, int32_t enable);
+int cmag_batch_stage_times(cmag_batch *b, float ms_out[6], uint32_t *steps_out);
+const char *cmag_batch_last_error(const cmag_batch *b);
+
 /* Library version string. */
 const char *cmag_version(void);
 /* sizeof(cmag_sph_params) as compiled into the library (for FFI layout checks). */

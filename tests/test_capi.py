@@ -112,3 +112,34 @@ def test_create_reports_errors_without_exiting(built):
     p.grid_size[0] = 64
     rc = lib().cmag_system_create(ctypes.byref(p), 0, ctypes.byref(h))
     assert rc == _abi.CMAG_ERR_INVALID
+
+
+def test_batch_create_reports_errors_without_exiting(built):
+    """Batch creation checks every scene before touching the device."""
+    good = presets.dambreak_params((16, 32, 1), 1, (64, 64, 4), 1 / 256)
+    bad = presets.dambreak_params((16, 32, 1), 1, (64, 64, 4), 1 / 256)
+    bad.grid_size[1] = 3
+    arr = (_abi.SphParams * 2)(good, bad)
+    counts = (ctypes.c_uint32 * 2)(100, 100)
+    h = ctypes.c_void_p()
+    assert lib().cmag_batch_create(arr, counts, 2, ctypes.byref(h)) == _abi.CMAG_ERR_INVALID
+    assert lib().cmag_last_error().startswith(b"scene 1:")
+    assert lib().cmag_batch_create(arr, counts, 0, ctypes.byref(h)) == _abi.CMAG_ERR_INVALID
+    counts[0] = 0
+    assert lib().cmag_batch_create(arr, counts, 1, ctypes.byref(h)) == _abi.CMAG_ERR_INVALID
+    assert not h.value
+
+
+def test_batched_workload_sizes(built):
+    """The batched benchmark's scenes: counts log-uniform in the stated range,
+    families split in half, cell tables small enough for 32-bit sort keys."""
+    P, N, F, D = presets.batched_scenes()
+    assert len(P) == 256 and [d[0] for d in D] == ["poiseuille"] * 128 + ["dambreak"] * 128
+    assert min(F) >= 0.9 * 4096 and max(F) <= 1.1 * 262144
+    assert all(n > f for n, f in zip(N, F))  # walls on top of the fluid
+    cells = sum(int(p.grid_size[0]) * int(p.grid_size[1]) for p in P)
+    assert cells < 2 ** 32
+    for p, d in zip(P, D):
+        if d[0] == "poiseuille":
+            assert abs(float(p.mu) - 1000 * d[3]) <= 1e-6 * float(p.mu)
+            assert 1e-6 * 0.99 <= d[3] <= 1e-4 * 1.01
