@@ -347,6 +347,80 @@ def cpu_run_batched(run, threads, budget_s=20.0):
         rounds, picks)
 
 
+def run_learned(args):
+    """Learned closure (3-D dam break at 2x the spacing of the fine 64x128x64
+    column, 65,536 fluid particles): build training data from fine runs, train on
+    the GPU, then time fine, coarse and coarse + closure runs of a held-out seed to
+    t_end and compare their surge fronts."""
+    import torch
+    import cmag_gb300 as cm  # noqa: F401
+    from cmag_gb300.closure import (Closure, Pair, collect, normalization_from, output_limit_from,
+                                    rollout, train)
+    from oracle import closure_oracle as CO
+    t_end, width = args.t_end, 0.5
+    pair = Pair()
+    fine_dt = float(pair.pf.delta_time)
+    every = 2 * int(round(args.sample_every / (2 * fine_dt)))
+    snaps = int(round(args.t_train / args.sample_every))
+    seeds = list(range(2001, 2001 + args.train_seeds))
+    t0 = time.perf_counter()
+    feat, tgt = collect(pair, seeds, snaps, every)
+    t_data = time.perf_counter() - t0
+    c = Closure(CO.init_params(0))
+    mean, inv, scale = normalization_from(feat, tgt)
+    c.set_normalization(mean, inv, scale)
+    c.set_output_limit(output_limit_from(tgt, scale))
+    train_rows = int(feat.shape[0])
+    t0 = time.perf_counter()
+    losses = train(c, feat, tgt, steps=args.train_steps, batch=65536, lr=2e-3, lr_final=1e-4,
+                   log_every=max(1, args.train_steps // 5))
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    del feat, tgt
+
+    held = 999
+    runs = {}
+    for name in ("fine", "coarse", "coarse_closure"):
+        sysm = pair.fine if name == "fine" else pair.coarse
+        pair.coarse.set_closure(c if name == "coarse_closure" else None)
+        pair.start(held)
+        sysm.update_n(3)  # warm-up and graph capture (restarted below)
+        pair.start(held)
+        secs, times, fronts = rollout(sysm, t_end, 0.01, width)
+        runs[name] = {"device_s_to_t_end": secs, "steps": int(round(t_end / float(sysm.params.delta_time))),
+                      "fronts": fronts, "times": times}
+    pair.coarse.set_closure(None)
+    ff = runs["fine"]["fronts"]
+    tank_len = pair.tank_f[0] / pair.fluid_f[0]  # tank length over column width
+    judged = ff < 0.95 * tank_len   # before the surge meets the far wall
+    out = {}
+    for name in ("coarse", "coarse_closure"):
+        err = np.abs(runs[name]["fronts"] - ff) / ff
+        out[name] = {"front_err_max": float(err[judged].max()), "front_err_mean": float(err[judged].mean()),
+                     "device_s_to_t_end": runs[name]["device_s_to_t_end"],
+                     "speedup_vs_fine": runs["fine"]["device_s_to_t_end"] / runs[name]["device_s_to_t_end"]}
+    nfc = pair.nfluid_c
+    cl = runs["coarse_closure"]
+    value = nfc * cl["steps"] / cl["device_s_to_t_end"]
+    line = {"metric": METRIC, "value": value, "unit": "particle-updates/s", "n_gpus": 1,
+            "steps": cl["steps"], "warmup": 3, "ms_per_step": 1e3 * cl["device_s_to_t_end"] / cl["steps"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+bf16",
+            "data": "synthetic (seeded lattices + jitter)",
+            "config": {"workload": "learned_closure", "fine_fluid": list(pair.fluid_f),
+                       "coarse_fluid": list(pair.fluid_c), "t_end": t_end,
+                       "train_seeds": len(seeds), "snapshots_per_seed": snaps,
+                       "train_rows": train_rows, "train_steps": args.train_steps,
+                       "held_out_seed": held, "network": "16-64-64-64-3 SiLU, bf16 params/activations"},
+            "learned": {"fine_device_s_to_t_end": runs["fine"]["device_s_to_t_end"],
+                        "coarse": out["coarse"], "coarse_closure": out["coarse_closure"],
+                        "meets_2pct_front": out["coarse_closure"]["front_err_max"] <= 0.02,
+                        "data_s": t_data, "train_s": t_train, "losses": losses,
+                        "fronts": {k: [round(float(v), 4) for v in r["fronts"][::10]] for k, r in runs.items()}}}
+    pair.close()
+    c.close()
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -354,7 +428,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="own", choices=["own", "reference"])
     ap.add_argument("--workload", default="dambreak3d",
-                    choices=["dambreak3d", "peristalsis", "poiseuille", "batched"])
+                    choices=["dambreak3d", "peristalsis", "poiseuille", "batched", "learned"])
+    ap.add_argument("--t-end", type=float, default=1.0, help="learned: simulated time of the timed runs")
+    ap.add_argument("--t-train", type=float, default=1.0, help="learned: time span of the training runs")
+    ap.add_argument("--sample-every", type=float, default=0.025, help="learned: seconds between samples")
+    ap.add_argument("--train-seeds", type=int, default=3)
+    ap.add_argument("--train-steps", type=int, default=3000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-steps", type=int, default=1)
     args = ap.parse_args()
@@ -367,6 +446,9 @@ def main():
     from cmag_gb300 import build as B
     if not os.path.exists(B.LIB):
         B.build()
+    if args.workload == "learned":
+        run_learned(args)
+        return
     dist = dist_init(args.gpus)
     rank = int(os.environ.get("RANK", "0"))
     world = dist.get_world_size() if dist else 1

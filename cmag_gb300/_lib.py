@@ -112,6 +112,28 @@ SIGNATURES = {
     "cmag_batch_set_stage_timing": ([c_bat, c_i32], ctypes.c_int),
     "cmag_batch_stage_times": ([c_bat, c_f32p, c_u32p], ctypes.c_int),
     "cmag_batch_last_error": ([c_bat], ctypes.c_char_p),
+    # learned closure
+    "cmag_closure_param_count": ([], ctypes.c_size_t),
+    "cmag_closure_create": ([c_f32p, P(ctypes.c_void_p)], ctypes.c_int),
+    "cmag_closure_destroy": ([ctypes.c_void_p], ctypes.c_int),
+    "cmag_closure_set_params": ([ctypes.c_void_p, c_f32p], ctypes.c_int),
+    "cmag_closure_get_params": ([ctypes.c_void_p, c_f32p], ctypes.c_int),
+    "cmag_closure_get_bf16_params": ([ctypes.c_void_p, c_f32p], ctypes.c_int),
+    "cmag_closure_set_normalization": ([ctypes.c_void_p, c_f32p, c_f32p, ctypes.c_float], ctypes.c_int),
+    "cmag_closure_get_normalization": ([ctypes.c_void_p, c_f32p, c_f32p, c_f32p], ctypes.c_int),
+    "cmag_closure_set_output_limit": ([ctypes.c_void_p, ctypes.c_float], ctypes.c_int),
+    "cmag_closure_forward": ([ctypes.c_void_p, ctypes.c_void_p, c_u32, ctypes.c_void_p, ctypes.c_void_p],
+                             ctypes.c_int),
+    "cmag_closure_gradient": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, c_u32, c_f32p, c_f32p,
+                               ctypes.c_void_p], ctypes.c_int),
+    "cmag_closure_train_step": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, c_u32, ctypes.c_float,
+                                 c_f32p, ctypes.c_void_p], ctypes.c_int),
+    "cmag_closure_reset_optimizer": ([ctypes.c_void_p], ctypes.c_int),
+    "cmag_closure_synchronize": ([ctypes.c_void_p], ctypes.c_int),
+    "cmag_closure_last_error": ([ctypes.c_void_p], ctypes.c_char_p),
+    "cmag_system_set_closure": ([c_sys, ctypes.c_void_p], ctypes.c_int),
+    "cmag_system_closure_features": ([c_sys, ctypes.c_void_p], ctypes.c_int),
+    "cmag_system_interpolate": ([c_sys, c_i32, ctypes.c_void_p, c_u32, ctypes.c_void_p], ctypes.c_int),
 }
 
 
@@ -137,10 +159,12 @@ def lib():
     return _lib
 
 
-def check(rc, handle=None, batch=None):
+def check(rc, handle=None, batch=None, closure=None):
     if rc != 0:
         L = lib()
-        if batch:
+        if closure:
+            msg = L.cmag_closure_last_error(closure)
+        elif batch:
             msg = L.cmag_batch_last_error(batch)
         elif handle:
             msg = L.cmag_system_last_error(handle)

@@ -1,0 +1,154 @@
+// neighbor_walk.cuh -- the walk over a particle's neighbour cells as runs of
+// consecutive sorted particles, shared by the density/force loops
+// (neighbors.cu) and the learned closure's feature loop (closure.cu).
+//
+// The (2c+1)^2 rows of the cell box (only the particle's own z layer for planar
+// 2-D scenes) are walked as runs of consecutive cells: a run's particles are one
+// contiguous sorted range [off[a], off[b+1]) of the dense offset table.  A group
+// of G lanes shares a particle and splits its rows between them (row r goes to
+// lane r mod G).  Runs wrap at most once per row; a wrapped run carries the
+// periodic image shift of its unmasked cell coordinates, as the reference's
+// per-cell shift (poiseuilleFlowKernel.cu:121-127, PeristalsisUtil.cu:4-11).
+// With TRIM each row's run is trimmed to the support circle, in cell units from
+// the particle's fractional cell coordinates.
+#pragma once
+
+#include "sph_common.cuh"
+
+namespace cmag {
+namespace walk {
+
+constexpr float kMargin = 1e-3f;  // cells: covers rounding of the cell assignment
+
+template <bool PLANAR>
+__device__ __forceinline__ int rows_of(int c)
+{
+    return PLANAR ? (2 * c + 1) : (2 * c + 1) * (2 * c + 1);
+}
+
+__device__ __forceinline__ uint32_t wrap_axis(int v, uint32_t n)
+{
+    // one period away at most for particles inside the grid; any value for
+    // particles that left it
+    if ((uint32_t)v < n) return (uint32_t)v;
+    if (v < 0 && v >= -(int)n) return (uint32_t)(v + (int)n);
+    if (v >= (int)n && v < 2 * (int)n) return (uint32_t)(v - (int)n);
+    int m = v % (int)n;
+    return (uint32_t)(m < 0 ? m + (int)n : m);
+}
+
+// The runs of one row of the cell box: [b0, e0) with x image shift sx0 and,
+// when the row wraps in x, [b1, e1) with sx1 (empty otherwise); sy, sz: the
+// row's image shifts.
+struct RowRuns {
+    uint32_t b0, e0, b1, e1;
+    float sx0, sx1, sy, sz;
+};
+
+// Row (dy, dz) of particle (fx,fy,fz) (fractional cell coordinates) in cell g.
+// Returns false when the row holds no candidates.
+template <int SYS, bool PLANAR, bool TRIM>
+__device__ __forceinline__ bool row_runs(const DevParams &p, const uint32_t *__restrict__ off,
+                                         int dy, int dz, int3 g, float fx, float fy, float fz,
+                                         RowRuns &rr)
+{
+    const int c = p.cell_count;
+    const int yu = g.y + dy, zu = g.z + dz;
+    int xa = g.x - c, xb = g.x + c;
+    if (TRIM) {
+        float dym = 0.0f, dzm = 0.0f;
+        if (dy > 0) dym = (float)yu - fy;
+        if (dy < 0) dym = fy - (float)(yu + 1);
+        if (!PLANAR) {
+            if (dz > 0) dzm = (float)zu - fz;
+            if (dz < 0) dzm = fz - (float)(zu + 1);
+            dzm = fmaxf(dzm - kMargin, 0.0f);
+        }
+        dym = fmaxf(dym - kMargin, 0.0f);
+        const float r2 = p.support2_cells - dym * dym - dzm * dzm;
+        if (r2 <= 0.0f) return false;
+        // conservative half width: the approximate square root errs by far less
+        // than the margin
+        const float R = r2 * rsqrtf(r2) + kMargin;
+        xa = max(xa, __float2int_rd(fx - R));
+        xb = min(xb, __float2int_rd(fx + R));
+        if (xa > xb) return false;
+    }
+    const uint32_t zm = PLANAR ? p.planar_layer : wrap_axis(zu, p.gz);
+    const uint32_t row = (zm * p.gy + wrap_axis(yu, p.gy)) * p.gx - p.scan_base;
+    if (row >= p.scan_cells) return false;  // outside the offset table: no particles
+    rr.sy = (SYS == CMAG_PERISTALSIS) ? (float)eval_shift(yu, p.gy) * p.wsy : 0.0f;
+    rr.sz = (SYS == CMAG_PERISTALSIS && !PLANAR) ? (float)eval_shift(zu, p.gz) * p.wsz : 0.0f;
+    const uint32_t xma = wrap_axis(xa, p.gx);
+    const uint32_t len = (uint32_t)(xb - xa);
+    rr.sx0 = (SYS == CMAG_DAMBREAK) ? 0.0f : (float)eval_shift(xa, p.gx) * p.wsx;
+    rr.b0 = __ldg(off + row + xma);
+    if (xma + len < p.gx) {
+        rr.e0 = __ldg(off + row + xma + len + 1);
+        rr.b1 = rr.e1 = 0;
+        rr.sx1 = 0.0f;
+    } else {
+        rr.e0 = __ldg(off + row + p.gx);
+        rr.b1 = __ldg(off + row);
+        rr.e1 = __ldg(off + row + (xma + len - p.gx) + 1);
+        rr.sx1 = (SYS == CMAG_DAMBREAK) ? 0.0f : (float)eval_shift(xb, p.gx) * p.wsx;
+    }
+    return true;
+}
+
+// Calls visit_run(b, e, sx, sy, sz) for every run of the rows this lane owns
+// (rows r = lane, lane + G, ... of the (2c+1)^2 box, dy fastest).
+template <int SYS, bool PLANAR, bool TRIM, int G, class VisitRun>
+__device__ __forceinline__ void for_each_run(const DevParams &p, const uint32_t *__restrict__ off,
+                                             int lane, int3 g, float3 f, VisitRun &&visit_run)
+{
+    const int c = p.cell_count;
+    const int w = 2 * c + 1;
+    int dy = (G == 1) ? -c : (lane % w) - c;
+    int dz = PLANAR ? 0 : ((G == 1) ? -c : (lane / w) - c);
+    const int nrows = rows_of<PLANAR>(c);
+    for (int r = lane; r < nrows; r += G) {
+        RowRuns rr;
+        if (row_runs<SYS, PLANAR, TRIM>(p, off, dy, dz, g, f.x, f.y, f.z, rr)) {
+            visit_run(rr.b0, rr.e0, rr.sx0, rr.sy, rr.sz);
+            if (rr.e1 > rr.b1) visit_run(rr.b1, rr.e1, rr.sx1, rr.sy, rr.sz);
+        }
+        dy += G;
+        while (dy > c) {
+            dy -= w;
+            ++dz;
+        }
+    }
+}
+
+// Calls visit(j, sx, sy, sz) for every candidate of the rows this lane owns.
+template <int SYS, bool PLANAR, bool TRIM, int G, class Visit>
+__device__ __forceinline__ void for_each_candidate(const DevParams &p,
+                                                   const uint32_t *__restrict__ off, int lane,
+                                                   int3 g, float3 f, Visit &&visit)
+{
+    for_each_run<SYS, PLANAR, TRIM, G>(p, off, lane, g, f,
+                                       [&](uint32_t b, uint32_t e, float sx, float sy, float sz) {
+#pragma unroll 2
+                                           for (uint32_t j = b; j < e; ++j) visit(j, sx, sy, sz);
+                                       });
+}
+
+// Relative position of candidate j seen through its image shift.  Only the
+// families with periodic images add the shift (DamBreak none, Poiseuille x only);
+// the compiler cannot drop an added 0.0f by itself (signed zeros).
+template <int SYS>
+__device__ __forceinline__ float3 rel(float4 pi, float4 pj, float sx, float sy, float sz)
+{
+    if (SYS == CMAG_DAMBREAK) return make_float3(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z);
+    if (SYS == CMAG_POISEUILLE) return make_float3(pi.x - (pj.x + sx), pi.y - pj.y, pi.z - pj.z);
+    return make_float3(pi.x - (pj.x + sx), pi.y - (pj.y + sy), pi.z - (pj.z + sz));
+}
+
+__device__ __forceinline__ float3 frac_cell(const DevParams &p, float4 q)
+{
+    return make_float3((q.x - p.ox) * p.inv_csx, (q.y - p.oy) * p.inv_csy, (q.z - p.oz) * p.inv_csz);
+}
+
+}  // namespace walk
+}  // namespace cmag

@@ -14,6 +14,7 @@
 #include <string>
 #include <vector>
 
+#include "closure.h"
 #include "host_common.h"
 #include "host_scenes.h"
 #include "kernels.h"
@@ -58,6 +59,7 @@ struct cmag_system {
     int last_stage = CMAG_STAGE_INTEGRATE;
 
     int g_density = 1, g_force = 1;  // lanes per particle (cmag_system_autotune)
+    cmag_closure *closure = nullptr;   // learned correction added after the force stage
 
     bool use_graphs = true;
     cudaGraphExec_t gexec = nullptr;
@@ -341,6 +343,9 @@ int record_step(cmag_system *s, int last, bool timed)
         else
             launch_force(d, BatchView{}, s->g_force, s->spos, s->svel, s->aux, sorted_idx(s), s->off, s->acc,
                          nullptr, st);
+        if (s->closure)
+            launch_closure_apply(d, s->closure->view(), s->spos, s->svel, s->aux, s->meas,
+                                 sorted_idx(s), s->off, s->acc, st);
     }
     mark(5);
     if (last >= CMAG_STAGE_INTEGRATE)
@@ -1135,6 +1140,52 @@ int cmag_system_autotune(cmag_system *s, int32_t reps)
     s->g_force = gf;
     s->last_stage = CMAG_STAGE_FORCE;
     invalidate_graph(s);
+    return CMAG_OK;
+}
+
+int cmag_system_set_closure(cmag_system *s, cmag_closure *c)
+{
+    if (!s) return fail(nullptr, CMAG_ERR_INVALID, "null handle");
+    if (c && s->p.system != CMAG_DAMBREAK)
+        return fail(s, CMAG_ERR_STATE, "the learned closure corrects DamBreak scenes only");
+    s->closure = c;
+    invalidate_graph(s);
+    return CMAG_OK;
+}
+
+int cmag_system_closure_features(cmag_system *s, float *d_features)
+{
+    if (!s || !d_features) return fail(s, CMAG_ERR_INVALID, "null argument");
+    if (s->p.system != CMAG_DAMBREAK) return fail(s, CMAG_ERR_STATE, "not a dam-break system");
+    if (s->last_stage < CMAG_STAGE_FORCE)
+        return fail(s, CMAG_ERR_STATE, "features need this step's density and forces (run_stages FORCE)");
+    launch_closure_features(make_dev(s), s->spos, s->svel, s->aux, s->meas, sorted_idx(s), s->off,
+                            s->acc, d_features, st_of(s));
+    CM_CUDA(s, cudaGetLastError());
+    CM_CUDA(s, cudaStreamSynchronize(st_of(s)));
+    return CMAG_OK;
+}
+
+int cmag_system_interpolate(cmag_system *s, int32_t array, const float *d_points, uint32_t n,
+                            float *d_out)
+{
+    if (!s || (n && (!d_points || !d_out))) return fail(s, CMAG_ERR_INVALID, "null argument");
+    if (s->p.system != CMAG_DAMBREAK) return fail(s, CMAG_ERR_STATE, "not a dam-break system");
+    if (s->last_stage < CMAG_STAGE_DENSITY)
+        return fail(s, CMAG_ERR_STATE, "interpolation needs this step's densities (run_stages DENSITY)");
+    const float4 *a = nullptr;
+    switch (array) {
+    case CMAG_POSITION: a = s->pos; break;
+    case CMAG_VELOCITY: a = s->vel; break;
+    case CMAG_ACCELERATION: a = s->acc; break;
+    case CMAG_VELOCITYLEAPFROG: a = s->vlf; break;
+    default: return fail(s, CMAG_ERR_INVALID, "not an original-order float4 array: " + std::to_string(array));
+    }
+    launch_interpolate(make_dev(s), s->spos, s->aux, sorted_idx(s), s->off, a,
+                       reinterpret_cast<const float4 *>(d_points), n, reinterpret_cast<float4 *>(d_out),
+                       st_of(s));
+    CM_CUDA(s, cudaGetLastError());
+    CM_CUDA(s, cudaStreamSynchronize(st_of(s)));
     return CMAG_OK;
 }
 

@@ -225,6 +225,24 @@ class _System:
         self._chk(lib().cmag_system_fluid_sum(self._h, int(array), s, ctypes.byref(c)))
         return tuple(s), c.value
 
+    # -- learned closure (DamBreak) --
+    def set_closure(self, closure):
+        """Attach a cmag_gb300.closure.Closure (None detaches); it must outlive the
+        attachment."""
+        self._closure = closure
+        self._chk(lib().cmag_system_set_closure(self._h, closure._h if closure is not None else None))
+
+    def closure_features(self, dev_ptr):
+        """Raw closure features of the last run_stages(FORCE) state into the device
+        array at dev_ptr (num_particles x 16 floats, original order)."""
+        self._chk(lib().cmag_system_closure_features(self._h, ctypes.c_void_p(int(dev_ptr))))
+
+    def interpolate(self, array, points_ptr, n, out_ptr):
+        """SPH interpolation of `array` over the fluid at n device points (n x 4
+        floats at points_ptr) into out_ptr (n x 4: value, Shepard sum)."""
+        self._chk(lib().cmag_system_interpolate(self._h, int(array), ctypes.c_void_p(int(points_ptr)),
+                                                int(n), ctypes.c_void_p(int(out_ptr))))
+
     def set_elapsed_time(self, t):
         self._chk(lib().cmag_system_set_elapsed_time(self._h, float(t)))
 

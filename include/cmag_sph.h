@@ -422,6 +422,64 @@ int cmag_batch_set_stage_timing(cmag_batch *b, int32_t enable);
 int cmag_batch_stage_times(cmag_batch *b, float ms_out[6], uint32_t *steps_out);
 const char *cmag_batch_last_error(const cmag_batch *b);
 
+/* ---- learned closure ----------------------------------------------------- */
+/* No counterpart in the reference.  A 16-64-64-64-3 SiLU network that adds a
+ * learned correction to the pressure + viscous + wall acceleration of every fluid
+ * particle of a (coarse) DamBreak scene, right after the force stage.  BF16
+ * parameters and activations, FP32 accumulation; trained on the GPU by the
+ * library's own forward/backward kernels and Adam (FP32 master copy).
+ *  - Parameters: cmag_closure_param_count() floats, order W1[64][16] b1[64]
+ *    W2[64][64] b2[64] W3[64][64] b3[64] W4[3][64] b4[3] (W[out][in]).
+ *  - Features (16 per fluid particle, raw): cmag_system_closure_features writes
+ *    them for the state of the last run_stages(CMAG_STAGE_FORCE) into a device
+ *    array of num_particles x 16 floats (original order; wall rows untouched).
+ *    The network sees bf16((f - mean) * inv_std); the correction is out_scale * y.
+ *  - Device arrays (features n x 16, targets / outputs n x 3, row-major floats)
+ *    are the caller's; stream NULL means the closure's own stream. */
+typedef struct cmag_closure cmag_closure;
+
+size_t cmag_closure_param_count(void);
+/* params: FP32 initial parameters, or NULL for zeros */
+int cmag_closure_create(const float *params, cmag_closure **out);
+int cmag_closure_destroy(cmag_closure *c);
+int cmag_closure_set_params(cmag_closure *c, const float *params);
+int cmag_closure_get_params(cmag_closure *c, float *params);
+/* the BF16 values the kernels use, widened to float */
+int cmag_closure_get_bf16_params(cmag_closure *c, float *params);
+int cmag_closure_set_normalization(cmag_closure *c, const float mean[16], const float inv_std[16],
+                                   float out_scale);
+int cmag_closure_get_normalization(cmag_closure *c, float mean[16], float inv_std[16],
+                                   float *out_scale);
+/* inside a step the correction is out_scale * clamp(y, -limit, limit) per
+ * component (default: no limit); cmag_closure_forward is not clamped */
+int cmag_closure_set_output_limit(cmag_closure *c, float limit);
+/* network outputs y (unscaled) for n feature rows */
+int cmag_closure_forward(cmag_closure *c, const float *d_features, uint32_t n, float *d_out,
+                         void *stream);
+/* loss 0.5/n sum |y - t|^2 and its gradient with respect to the (BF16) parameters,
+ * copied to the host (grad_out: param_count floats); parameters unchanged */
+int cmag_closure_gradient(cmag_closure *c, const float *d_features, const float *d_targets,
+                          uint32_t n, float *grad_out, float *loss_out, void *stream);
+/* one Adam step (beta 0.9 / 0.999, eps 1e-8) on the loss over the n rows; the loss
+ * before the step is returned when loss_out is given (that call waits) */
+int cmag_closure_train_step(cmag_closure *c, const float *d_features, const float *d_targets,
+                            uint32_t n, float lr, float *loss_out, void *stream);
+int cmag_closure_reset_optimizer(cmag_closure *c);
+int cmag_closure_synchronize(cmag_closure *c);
+const char *cmag_closure_last_error(const cmag_closure *c);
+/* attach (or with NULL detach) a closure to a DamBreak system: every later step
+ * adds its correction after the force stage; the closure must outlive the
+ * attachment */
+int cmag_system_set_closure(cmag_system *s, cmag_closure *c);
+int cmag_system_closure_features(cmag_system *s, float *d_features);
+/* Shepard-normalised SPH interpolation of a float4 array (POSITION, VELOCITY,
+ * ACCELERATION or VELOCITYLEAPFROG) over the fluid particles of a DamBreak system,
+ * at n points (device, n x 4 floats; .w ignored): d_out (device, n x 4) gets
+ * sum V_j W a_j / sum V_j W in xyz and sum V_j W in w (0: no fluid in reach).
+ * Uses the sorted state and densities of the last run_stages (>= DENSITY). */
+int cmag_system_interpolate(cmag_system *s, int32_t array, const float *d_points, uint32_t n,
+                            float *d_out);
+
 /* Library version string. */
 const char *cmag_version(void);
 /* sizeof(cmag_sph_params) as compiled into the library (for FFI layout checks). */
