@@ -254,10 +254,12 @@ def train(closure, feat_dev, target_dev, steps, batch=65536, lr=2e-3, lr_final=2
 # ------------------------------------------------------------------ rollouts ---
 
 def front(system, column_width):
-    """Surge front: the largest x of a fluid particle over the initial column
-    width (DamBreak.Report/XFrontTest.h:64,79-86, reduced on the device)."""
+    """Surge front over the initial column width: the largest x of a fluid
+    particle (DamBreak.Report/XFrontTest.h:64,79-86, reduced on the device) plus
+    the particle radius, i.e. the free surface, so that runs at different spacings
+    compare (at t = 0 both give the column's face)."""
     _, hi = system.fluid_extent()
-    return hi[0] / column_width
+    return (hi[0] + float(system.params.particle_radius)) / column_width
 
 
 def rollout(system, t_end, sample_dt, column_width, steps_per_call=None):

@@ -98,27 +98,6 @@ __device__ __forceinline__ void load_row(const float *src, float (&v)[N])
     }
 }
 
-// network output for one normalised, BF16-rounded input row; rows a/b: this
-// thread's scratch rows (kRow floats each)
-__device__ __forceinline__ void forward_row(const float *sw, const float (&x)[kFeat], float *ra,
-                                            float *rb, float (&y)[kOut])
-{
-    dense_row<kFeat, kHidden, false>(sw, kOffW1, kOffB1, x, ra);
-    float h[kHidden];
-    load_row(ra, h);
-    dense_row<kHidden, kHidden, false>(sw, kOffW2, kOffB2, h, rb);
-    load_row(rb, h);
-    dense_row<kHidden, kHidden, false>(sw, kOffW3, kOffB3, h, ra);
-    load_row(ra, h);
-#pragma unroll
-    for (int o = 0; o < kOut; ++o) {
-        float z = sw[kOffB4 + o];
-#pragma unroll
-        for (int k = 0; k < kHidden; ++k) z = __fmaf_rn(sw[kOffW4 + o * kHidden + k], h[k], z);
-        y[o] = z;
-    }
-}
-
 __device__ __forceinline__ void normalise(const float *mean, const float *inv_std,
                                           const float (&f)[kFeat], float (&x)[kFeat])
 {
@@ -176,63 +155,220 @@ __device__ __forceinline__ void features(const DevParams &p, const float4 *__res
     f[15] = sqrtf(vi.x * vi.x + vi.y * vi.y + vi.z * vi.z) * ic;
 }
 
-// MODE 0: write the raw features of every fluid particle (original order);
-// MODE 1: features, network, acc += correction.
-template <bool PLANAR, bool TRIM, int MODE>
-__global__ void __launch_bounds__(kTile)
-    k_closure(DevParams p, ClosureView c, const float4 *__restrict__ spos,
-              const float4 *__restrict__ svel, const float2 *__restrict__ aux,
-              const float4 *__restrict__ meas, const uint32_t *__restrict__ idx,
-              const uint32_t *__restrict__ off, float4 *acc, float *feat)
+// NORM false: the raw features of every fluid particle to feat[o * 16] (original
+// order o); NORM true: the normalised BF16 network input of every sorted particle
+// to xb[i * 16] (zeros for walls).
+template <bool PLANAR, bool TRIM, bool NORM>
+__global__ void __launch_bounds__(256)
+    k_closure_features(DevParams p, ClosureView c, const float4 *__restrict__ spos,
+                       const float4 *__restrict__ svel, const float2 *__restrict__ aux,
+                       const float4 *__restrict__ meas, const uint32_t *__restrict__ idx,
+                       const uint32_t *__restrict__ off, const float4 *__restrict__ acc,
+                       float *feat, __nv_bfloat16 *xb)
 {
-    extern __shared__ float4 smem4[];
-    float *sw = reinterpret_cast<float *>(smem4);
-    float *rows = sw + kWPad;
-    if (MODE == 1) {
-        load_weights(sw, c.w);
-        __syncthreads();
-    }
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
     const float4 pi = spos[i];
-    if (pi.w != (float)CMAG_FLUID) return;
     const uint32_t o = idx[i];
-    if (o >= p.n) return;  // only after a failed sort (reported by the sort itself)
-    float4 a = acc[o];
+    const bool fluid = pi.w == (float)CMAG_FLUID && o < p.n;  // o < n unless the sort failed
+    if (NORM && !fluid) {
+        uint4 *dst = reinterpret_cast<uint4 *>(xb + (size_t)i * kFeat);
+        dst[0] = dst[1] = make_uint4(0, 0, 0, 0);
+    }
+    if (!fluid) return;
     float f[kFeat];
-    features<PLANAR, TRIM>(p, spos, svel, aux, meas[i], off, i, pi, a, f);
-    if (MODE == 0) {
+    features<PLANAR, TRIM>(p, spos, svel, aux, meas[i], off, i, pi, acc[o], f);
+    if (!NORM) {
         float4 *dst = reinterpret_cast<float4 *>(feat + (size_t)o * kFeat);
 #pragma unroll
         for (int q = 0; q < kFeat / 4; ++q) dst[q] = make_float4(f[4 * q], f[4 * q + 1], f[4 * q + 2], f[4 * q + 3]);
         return;
     }
-    float x[kFeat], y[kOut];
+    float x[kFeat];
     normalise(c.mean, c.inv_std, f, x);
-    forward_row(sw, x, rows + threadIdx.x * 2 * kRow, rows + threadIdx.x * 2 * kRow + kRow, y);
-    const float s = *c.out_scale, lim = *c.out_limit;
-    a.x += s * fminf(fmaxf(y[0], -lim), lim);
-    a.y += s * fminf(fmaxf(y[1], -lim), lim);
-    a.z += s * fminf(fmaxf(y[2], -lim), lim);
-    acc[o] = a;
+    uint32_t w[kFeat / 2];
+#pragma unroll
+    for (int k = 0; k < kFeat / 2; ++k) {
+        const __nv_bfloat162 v = __floats2bfloat162_rn(x[2 * k], x[2 * k + 1]);
+        w[k] = *reinterpret_cast<const uint32_t *>(&v);
+    }
+    uint4 *dst = reinterpret_cast<uint4 *>(xb + (size_t)i * kFeat);
+    dst[0] = make_uint4(w[0], w[1], w[2], w[3]);
+    dst[1] = make_uint4(w[4], w[5], w[6], w[7]);
 }
 
-__global__ void __launch_bounds__(kTile)
-    k_forward(ClosureView c, const float *__restrict__ feat, uint32_t n, float *__restrict__ out)
+// raw FP32 feature rows -> normalised BF16 network input rows
+__global__ void k_normalise(ClosureView c, const float *__restrict__ feat, uint32_t n,
+                            __nv_bfloat16 *__restrict__ xb)
 {
-    extern __shared__ float4 smem4[];
-    float *sw = reinterpret_cast<float *>(smem4);
-    float *rows = sw + kWPad;
-    load_weights(sw, c.w);
-    __syncthreads();
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
-    float f[kFeat], x[kFeat], y[kOut];
+    float f[kFeat], x[kFeat];
     load_row(feat + (size_t)s * kFeat, f);
     normalise(c.mean, c.inv_std, f, x);
-    forward_row(sw, x, rows + threadIdx.x * 2 * kRow, rows + threadIdx.x * 2 * kRow + kRow, y);
 #pragma unroll
-    for (int o = 0; o < kOut; ++o) out[(size_t)s * kOut + o] = y[o];
+    for (int k = 0; k < kFeat / 2; ++k)
+        reinterpret_cast<__nv_bfloat162 *>(xb + (size_t)s * kFeat)[k] = __floats2bfloat162_rn(x[2 * k], x[2 * k + 1]);
+}
+
+// ---- the network on the tensor cores: mma.sync m16n8k16, BF16 in, FP32 accumulate.
+// A warp evaluates 16 rows at a time; a layer's FP32 accumulator fragments become
+// the next layer's BF16 A fragments in registers (the C layout of n-tiles 2j and
+// 2j+1 is the A layout of k-tile j), so activations never leave the registers.
+
+constexpr int kW1Stride = 24;   // BF16 per shared row of W1 (16 + 8: conflict-free fragment loads)
+constexpr int kWStride = 72;    // BF16 per shared row of W2, W3, W4 (64 + 8)
+constexpr int kSW1 = 0, kSW2 = kSW1 + kHidden * kW1Stride, kSW3 = kSW2 + kHidden * kWStride,
+              kSW4 = kSW3 + kHidden * kWStride, kSWEnd = kSW4 + 8 * kWStride;
+constexpr int kSB1 = 0, kSB2 = kSB1 + kHidden, kSB3 = kSB2 + kHidden, kSB4 = kSB3 + kHidden,
+              kSBEnd = kSB4 + 8;
+
+__device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1)
+{
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+        "{%8,%9}, {%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ uint32_t pack_silu(float lo, float hi)
+{
+    const __nv_bfloat162 v = __floats2bfloat162_rn(lo * sigmoid(lo), hi * sigmoid(hi));
+    return *reinterpret_cast<const uint32_t *>(&v);
+}
+
+__device__ __forceinline__ uint32_t lds32(const __nv_bfloat16 *p)
+{
+    return *reinterpret_cast<const uint32_t *>(p);
+}
+
+// one hidden layer: c[nt] = bias + A x W^T over KT k-tiles; W rows of `stride` BF16
+template <int KT>
+__device__ __forceinline__ void hidden_layer(const __nv_bfloat16 *W, int stride, const float *b,
+                                             const uint32_t (&a)[KT][4], float (&c)[8][4], int g, int t)
+{
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt) {
+        c[nt][0] = c[nt][2] = b[nt * 8 + 2 * t];
+        c[nt][1] = c[nt][3] = b[nt * 8 + 2 * t + 1];
+    }
+#pragma unroll
+    for (int kt = 0; kt < KT; ++kt)
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt) {
+            const __nv_bfloat16 *row = W + (nt * 8 + g) * stride + kt * 16 + 2 * t;
+            mma16816(c[nt], a[kt], lds32(row), lds32(row + 8));
+        }
+}
+
+__device__ __forceinline__ void to_a(const float (&c)[8][4], uint32_t (&a)[4][4])
+{
+#pragma unroll
+    for (int kt = 0; kt < 4; ++kt) {
+        a[kt][0] = pack_silu(c[2 * kt][0], c[2 * kt][1]);
+        a[kt][1] = pack_silu(c[2 * kt][2], c[2 * kt][3]);
+        a[kt][2] = pack_silu(c[2 * kt + 1][0], c[2 * kt + 1][1]);
+        a[kt][3] = pack_silu(c[2 * kt + 1][2], c[2 * kt + 1][3]);
+    }
+}
+
+// APPLY false: out[r * 3 ..] = network(xb row r) for r < n.
+// APPLY true: rows are sorted particles; acc[idx[r]] += out_scale * clamp(y) for
+// fluid rows.
+template <bool APPLY>
+__global__ void __launch_bounds__(128)
+    k_mlp(ClosureView c, const __nv_bfloat16 *__restrict__ xb, uint32_t n,
+          const float4 *__restrict__ spos, const uint32_t *__restrict__ idx, float4 *acc,
+          float *__restrict__ out)
+{
+    __shared__ __align__(16) __nv_bfloat16 sw[kSWEnd];
+    __shared__ float sb[kSBEnd];
+    for (int k = threadIdx.x; k < kSWEnd; k += blockDim.x) {
+        float v = 0.0f;
+        if (k < kSW2) {
+            const int o = k / kW1Stride, i = k % kW1Stride;
+            if (i < kFeat) v = __bfloat162float(c.w[kOffW1 + o * kFeat + i]);
+        } else {
+            const int base = k < kSW3 ? kSW2 : (k < kSW4 ? kSW3 : kSW4);
+            const int off = k < kSW3 ? kOffW2 : (k < kSW4 ? kOffW3 : kOffW4);
+            const int o = (k - base) / kWStride, i = (k - base) % kWStride;
+            if (i < kHidden && (base != kSW4 || o < kOut)) v = __bfloat162float(c.w[off + o * kHidden + i]);
+        }
+        sw[k] = __float2bfloat16_rn(v);  // exact: v is a BF16 value
+    }
+    for (int k = threadIdx.x; k < kSBEnd; k += blockDim.x) {
+        float v = 0.0f;
+        if (k < kSB2) v = __bfloat162float(c.w[kOffB1 + k]);
+        else if (k < kSB3) v = __bfloat162float(c.w[kOffB2 + k - kSB2]);
+        else if (k < kSB4) v = __bfloat162float(c.w[kOffB3 + k - kSB3]);
+        else if (k - kSB4 < kOut) v = __bfloat162float(c.w[kOffB4 + k - kSB4]);
+        sb[k] = v;
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+    const uint32_t tiles = (n + 15) / 16;
+    const float scale = APPLY ? *c.out_scale : 0.0f, lim = APPLY ? *c.out_limit : 0.0f;
+    for (uint32_t tile = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); tile < tiles; tile += warps) {
+        const uint32_t r0 = tile * 16 + g, r1 = r0 + 8;
+        if (APPLY) {  // sorted order keeps wall cells together: skip tiles without fluid
+            const bool f = (r0 < n && spos[r0].w == (float)CMAG_FLUID) ||
+                           (r1 < n && spos[r1].w == (float)CMAG_FLUID);
+            if (!__any_sync(0xffffffffu, f)) continue;
+        }
+        uint32_t a1[1][4];
+        {
+            const uint32_t *x0 = reinterpret_cast<const uint32_t *>(xb + (size_t)r0 * kFeat);
+            const uint32_t *x1 = reinterpret_cast<const uint32_t *>(xb + (size_t)r1 * kFeat);
+            a1[0][0] = r0 < n ? x0[t] : 0u;
+            a1[0][1] = r1 < n ? x1[t] : 0u;
+            a1[0][2] = r0 < n ? x0[t + 4] : 0u;
+            a1[0][3] = r1 < n ? x1[t + 4] : 0u;
+        }
+        float cc[8][4];
+        uint32_t a[4][4];
+        hidden_layer<1>(sw + kSW1, kW1Stride, sb + kSB1, a1, cc, g, t);
+        to_a(cc, a);
+        hidden_layer<4>(sw + kSW2, kWStride, sb + kSB2, a, cc, g, t);
+        to_a(cc, a);
+        hidden_layer<4>(sw + kSW3, kWStride, sb + kSB3, a, cc, g, t);
+        to_a(cc, a);
+        // output layer (3 of 8 columns used)
+        float y[4] = {sb[kSB4 + 2 * t], sb[kSB4 + 2 * t + 1], sb[kSB4 + 2 * t], sb[kSB4 + 2 * t + 1]};
+#pragma unroll
+        for (int kt = 0; kt < 4; ++kt) {
+            const __nv_bfloat16 *row = sw + kSW4 + g * kWStride + kt * 16 + 2 * t;
+            mma16816(y, a[kt], lds32(row), lds32(row + 8));
+        }
+        // lane (g, 0) holds columns 0, 1 of rows r0 (y[0..1]) and r1 (y[2..3]);
+        // column 2 sits in lane (g, 1)
+        const float y2r0 = __shfl_down_sync(0xffffffffu, y[0], 1);
+        const float y2r1 = __shfl_down_sync(0xffffffffu, y[2], 1);
+        if (t == 0) {
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const uint32_t r = h ? r1 : r0;
+                const float o0 = h ? y[2] : y[0], o1 = h ? y[3] : y[1], o2 = h ? y2r1 : y2r0;
+                if (r < n && !APPLY) {
+                    out[(size_t)r * kOut + 0] = o0;
+                    out[(size_t)r * kOut + 1] = o1;
+                    out[(size_t)r * kOut + 2] = o2;
+                }
+                if (r < n && APPLY && spos[r].w == (float)CMAG_FLUID) {
+                    const uint32_t o = idx[r];
+                    if (o < n) {  // o >= n only after a failed sort
+                        float4 av = acc[o];
+                        av.x += scale * fminf(fmaxf(o0, -lim), lim);
+                        av.y += scale * fminf(fmaxf(o1, -lim), lim);
+                        av.z += scale * fminf(fmaxf(o2, -lim), lim);
+                        acc[o] = av;
+                    }
+                }
+            }
+        }
+        __syncwarp();
+    }
 }
 
 // dW[o][k] += sum_s D[s][o] A[s][k], db[o] += sum_s D[s][o] over the block's
@@ -441,7 +577,6 @@ __global__ void __launch_bounds__(128)
     out[t] = make_float4(sx * inv, sy * inv, sz * inv, sw);
 }
 
-constexpr size_t kSmemForward = sizeof(float) * (kWPad + kTile * 2 * kRow);
 constexpr size_t kSmemBackward =
     sizeof(float) * (kWPad + kTile * kXRow + 4 * kTile * kRow + kTile * 4);
 
@@ -451,33 +586,31 @@ void allow_smem(K kernel, size_t bytes)
     cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
-template <bool PLANAR, bool TRIM, int MODE>
-void launch_closure_t(const DevParams &p, const ClosureView &c, const float4 *spos,
-                      const float4 *svel, const float2 *aux, const float4 *meas,
-                      const uint32_t *idx, const uint32_t *off, float4 *acc, float *feat,
-                      cudaStream_t st)
-{
-    const size_t smem = MODE == 1 ? kSmemForward : 0;
-    if (MODE == 1) allow_smem(k_closure<PLANAR, TRIM, MODE>, smem);
-    const uint32_t blocks = (p.n + kTile - 1) / kTile;
-    k_closure<PLANAR, TRIM, MODE><<<blocks, kTile, smem, st>>>(p, c, spos, svel, aux, meas, idx,
-                                                               off, acc, feat);
-}
-
-template <int MODE>
-void dispatch_closure(const DevParams &p, const ClosureView &c, const float4 *spos,
-                      const float4 *svel, const float2 *aux, const float4 *meas,
-                      const uint32_t *idx, const uint32_t *off, float4 *acc, float *feat,
-                      cudaStream_t st)
+template <bool NORM>
+void dispatch_features(const DevParams &p, const ClosureView &c, const float4 *spos,
+                       const float4 *svel, const float2 *aux, const float4 *meas,
+                       const uint32_t *idx, const uint32_t *off, const float4 *acc, float *feat,
+                       __nv_bfloat16 *xb, cudaStream_t st)
 {
     if (p.n == 0) return;
+    const uint32_t blocks = (p.n + 255) / 256;
+#define CMAG_FEAT(PL, TR) \
+    k_closure_features<PL, TR, NORM><<<blocks, 256, 0, st>>>(p, c, spos, svel, aux, meas, idx, off, acc, feat, xb)
     if (p.planar) {
-        if (p.trim) launch_closure_t<true, true, MODE>(p, c, spos, svel, aux, meas, idx, off, acc, feat, st);
-        else launch_closure_t<true, false, MODE>(p, c, spos, svel, aux, meas, idx, off, acc, feat, st);
+        if (p.trim) CMAG_FEAT(true, true);
+        else CMAG_FEAT(true, false);
     } else {
-        if (p.trim) launch_closure_t<false, true, MODE>(p, c, spos, svel, aux, meas, idx, off, acc, feat, st);
-        else launch_closure_t<false, false, MODE>(p, c, spos, svel, aux, meas, idx, off, acc, feat, st);
+        if (p.trim) CMAG_FEAT(false, true);
+        else CMAG_FEAT(false, false);
     }
+#undef CMAG_FEAT
+}
+
+uint32_t mlp_blocks(uint32_t n)
+{
+    const uint32_t tiles = (n + 15) / 16;
+    uint32_t b = (tiles + 3) / 4;  // 4 warps per block, one 16-row tile each
+    return b < 1 ? 1 : (b > 152 * 16 ? 152 * 16 : b);
 }
 
 }  // namespace
@@ -486,15 +619,25 @@ void launch_closure_features(const DevParams &p, const float4 *spos, const float
                              const float2 *aux, const float4 *meas, const uint32_t *idx,
                              const uint32_t *off, const float4 *acc, float *feat, cudaStream_t st)
 {
-    dispatch_closure<0>(p, ClosureView{}, spos, svel, aux, meas, idx, off,
-                        const_cast<float4 *>(acc), feat, st);
+    dispatch_features<false>(p, ClosureView{}, spos, svel, aux, meas, idx, off, acc, feat, nullptr, st);
 }
 
 void launch_closure_apply(const DevParams &p, const ClosureView &c, const float4 *spos,
                           const float4 *svel, const float2 *aux, const float4 *meas,
-                          const uint32_t *idx, const uint32_t *off, float4 *acc, cudaStream_t st)
+                          const uint32_t *idx, const uint32_t *off, float4 *acc,
+                          __nv_bfloat16 *xb, cudaStream_t st)
 {
-    dispatch_closure<1>(p, c, spos, svel, aux, meas, idx, off, acc, nullptr, st);
+    if (p.n == 0) return;
+    dispatch_features<true>(p, c, spos, svel, aux, meas, idx, off, acc, nullptr, xb, st);
+    k_mlp<true><<<mlp_blocks(p.n), 128, 0, st>>>(c, xb, p.n, spos, idx, acc, nullptr);
+}
+
+void launch_closure_forward(const ClosureView &c, const float *feat, uint32_t n,
+                            __nv_bfloat16 *xb, float *out, cudaStream_t st)
+{
+    if (n == 0) return;
+    k_normalise<<<(n + 255) / 256, 256, 0, st>>>(c, feat, n, xb);
+    k_mlp<false><<<mlp_blocks(n), 128, 0, st>>>(c, xb, n, nullptr, nullptr, nullptr, out);
 }
 
 void launch_interpolate(const DevParams &p, const float4 *spos, const float2 *aux,
@@ -510,14 +653,6 @@ void launch_interpolate(const DevParams &p, const float4 *spos, const float2 *au
         if (p.trim) k_interp<false, true><<<blocks, 128, 0, st>>>(p, spos, aux, idx, off, arr, pts, n, out);
         else k_interp<false, false><<<blocks, 128, 0, st>>>(p, spos, aux, idx, off, arr, pts, n, out);
     }
-}
-
-void launch_closure_forward(const ClosureView &c, const float *feat, uint32_t n, float *out,
-                            cudaStream_t st)
-{
-    if (n == 0) return;
-    allow_smem(k_forward, kSmemForward);
-    k_forward<<<(n + kTile - 1) / kTile, kTile, kSmemForward, st>>>(c, feat, n, out);
 }
 
 void launch_closure_backward(const ClosureView &c, const float *feat, const float *target,

@@ -40,19 +40,20 @@ void launch_closure_features(const DevParams &p, const float4 *spos, const float
                              const float2 *aux, const float4 *meas, const uint32_t *idx,
                              const uint32_t *off, const float4 *acc, float *feat,
                              cudaStream_t st);
-// Features, network and acc[idx[i]] += correction for every fluid particle.
+// Features (normalised BF16 rows in xb, n x 16, sorted order), network on the
+// tensor cores and acc[idx[i]] += correction for every fluid particle.
 void launch_closure_apply(const DevParams &p, const ClosureView &c, const float4 *spos,
                           const float4 *svel, const float2 *aux, const float4 *meas,
                           const uint32_t *idx, const uint32_t *off, float4 *acc,
-                          cudaStream_t st);
+                          __nv_bfloat16 *xb, cudaStream_t st);
 // Shepard-normalised SPH interpolation of arr (original order) over the fluid
 // particles of a DamBreak scene at n points: out = (value, sum of V_j W).
 void launch_interpolate(const DevParams &p, const float4 *spos, const float2 *aux,
                         const uint32_t *idx, const uint32_t *off, const float4 *arr,
                         const float4 *pts, uint32_t n, float4 *out, cudaStream_t st);
-// Network outputs (unscaled) for n feature rows.
-void launch_closure_forward(const ClosureView &c, const float *feat, uint32_t n, float *out,
-                            cudaStream_t st);
+// Network outputs (unscaled) for n raw feature rows (xb: n x 16 BF16 scratch).
+void launch_closure_forward(const ClosureView &c, const float *feat, uint32_t n,
+                            __nv_bfloat16 *xb, float *out, cudaStream_t st);
 // Loss 0.5/n sum |y - t|^2 over n rows (t: targets, n x 3) added to *loss and its
 // gradient with respect to the BF16 parameters added to grad (FP32).
 void launch_closure_backward(const ClosureView &c, const float *feat, const float *target,
@@ -72,6 +73,8 @@ struct cmag_closure {
     __nv_bfloat16 *w = nullptr;                                            // BF16 copy used by kernels
     float *norm = nullptr;   // mean[16], inv_std[16], out_scale, loss, out_limit
     uint32_t adam_steps = 0;
+    __nv_bfloat16 *xb = nullptr;   // forward() scratch: normalised input rows
+    size_t xb_rows = 0;
     cudaStream_t stream = nullptr;
     std::string last_error;
     cmag::ClosureView view() const

@@ -36,7 +36,7 @@ cudaStream_t stream_of(cmag_closure *c, void *stream)
 
 void free_all(cmag_closure *c)
 {
-    void *ptrs[] = {c->master, c->m, c->v, c->grad, c->w, c->norm};
+    void *ptrs[] = {c->master, c->m, c->v, c->grad, c->w, c->norm, c->xb};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -179,7 +179,15 @@ int cmag_closure_forward(cmag_closure *c, const float *d_features, uint32_t n, f
 {
     if (!c || (n && (!d_features || !d_out))) return cfail(c, CMAG_ERR_INVALID, "null argument");
     cudaStream_t st = stream_of(c, stream);
-    launch_closure_forward(c->view(), d_features, n, d_out, st);
+    if (c->xb_rows < n) {
+        CC_CUDA(c, cudaStreamSynchronize(st));
+        if (c->xb) cudaFree(c->xb);
+        c->xb = nullptr;
+        c->xb_rows = 0;
+        CC_CUDA(c, cudaMalloc((void **)&c->xb, sizeof(__nv_bfloat16) * kFeat * (size_t)n));
+        c->xb_rows = n;
+    }
+    launch_closure_forward(c->view(), d_features, n, c->xb, d_out, st);
     CC_CUDA(c, cudaGetLastError());
     CC_CUDA(c, cudaStreamSynchronize(st));
     return CMAG_OK;

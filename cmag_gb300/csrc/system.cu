@@ -60,6 +60,7 @@ struct cmag_system {
 
     int g_density = 1, g_force = 1;  // lanes per particle (cmag_system_autotune)
     cmag_closure *closure = nullptr;   // learned correction added after the force stage
+    __nv_bfloat16 *closure_x = nullptr;  // its normalised input rows (n x 16)
 
     bool use_graphs = true;
     cudaGraphExec_t gexec = nullptr;
@@ -345,7 +346,7 @@ int record_step(cmag_system *s, int last, bool timed)
                          nullptr, st);
         if (s->closure)
             launch_closure_apply(d, s->closure->view(), s->spos, s->svel, s->aux, s->meas,
-                                 sorted_idx(s), s->off, s->acc, st);
+                                 sorted_idx(s), s->off, s->acc, s->closure_x, st);
     }
     mark(5);
     if (last >= CMAG_STAGE_INTEGRATE)
@@ -452,7 +453,8 @@ void free_all(cmag_system *s)
     s->events.clear();
     void *ptrs[] = {s->pos, s->vel, s->vlf, s->meas, s->acc, s->vforce, s->pforce, s->pred,
                     s->spos, s->svel, s->hash[0], s->hash[1], s->idx[0], s->idx[1], s->cnt,
-                    s->off, s->aux, s->ws, s->err, s->phase, s->view_cs, s->view_ce, s->red};
+                    s->off, s->aux, s->ws, s->err, s->phase, s->view_cs, s->view_ce, s->red,
+                    s->closure_x};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (s->own_stream) cudaStreamDestroy(s->own_stream);
@@ -1148,6 +1150,8 @@ int cmag_system_set_closure(cmag_system *s, cmag_closure *c)
     if (!s) return fail(nullptr, CMAG_ERR_INVALID, "null handle");
     if (c && s->p.system != CMAG_DAMBREAK)
         return fail(s, CMAG_ERR_STATE, "the learned closure corrects DamBreak scenes only");
+    if (c && !s->closure_x)
+        CM_CUDA(s, cudaMalloc((void **)&s->closure_x, sizeof(__nv_bfloat16) * 16 * (size_t)s->n));
     s->closure = c;
     invalidate_graph(s);
     return CMAG_OK;
