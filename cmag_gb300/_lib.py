@@ -76,6 +76,8 @@ SIGNATURES = {
     "cmag_sort_particles_noalloc": ([c_u32p, c_u32p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_void_p],
                                     ctypes.c_int),
     "cmag_sort_particles_noalloc_error": ([], ctypes.c_char_p),
+    "cmag_system_colors": ([c_sys, c_f32p], ctypes.c_int),
+    "cmag_system_render_ppm": ([c_sys, ctypes.c_char_p, c_u32, c_u32], ctypes.c_int),
     # batches
     "cmag_batch_create": ([P(SphParams), c_u32p, c_u32, P(c_bat)], ctypes.c_int),
     "cmag_batch_destroy": ([c_bat], ctypes.c_int),

@@ -606,11 +606,13 @@ void dispatch_features(const DevParams &p, const ClosureView &c, const float4 *s
 #undef CMAG_FEAT
 }
 
+// Each block stages the weights once and its 4 warps loop over 16-row tiles, so
+// the grid stays at a few blocks per SM (152 SMs) however many rows there are.
 uint32_t mlp_blocks(uint32_t n)
 {
     const uint32_t tiles = (n + 15) / 16;
-    uint32_t b = (tiles + 3) / 4;  // 4 warps per block, one 16-row tile each
-    return b < 1 ? 1 : (b > 152 * 16 ? 152 * 16 : b);
+    uint32_t b = (tiles + 3) / 4;
+    return b < 1 ? 1 : (b > 152 * 4 ? 152 * 4 : b);
 }
 
 }  // namespace

@@ -92,4 +92,13 @@ void launch_fluid_extents_batch(const BatchView &bv, const float4 *pos, uint32_t
 void launch_fluid_sum(int32_t system, const float4 *type_src, const float4 *a, uint32_t n,
                       double *sums4, unsigned long long *count, cudaStream_t st);
 
+// ---- headless colours and point view (render.cu) -------------------------------
+// the reference's colour buffer values per particle (original order)
+void launch_colors(const DevParams &p, const float4 *pos, uint32_t fluid, uint32_t type_one,
+                   float4 *out, cudaStream_t st);
+// x-y point image (w x h RGB bytes, row 0 at the top) of n particles
+void launch_render(const float4 *pos, const float4 *color, uint32_t n, float x0, float y0,
+                   float inv_px, uint32_t w, uint32_t h, float scale, uint32_t *owner,
+                   uint8_t *rgb, cudaStream_t st);
+
 }  // namespace cmag

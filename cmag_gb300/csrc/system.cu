@@ -1193,6 +1193,74 @@ int cmag_system_interpolate(cmag_system *s, int32_t array, const float *d_points
     return CMAG_OK;
 }
 
+namespace {
+int color_buffer(cmag_system *s, float4 *d_out)
+{
+    const cmag_sph_params &p = s->p;
+    const uint32_t fluid = p.fluid_size[0] * p.fluid_size[1] * p.fluid_size[2];
+    // fluidSystem.cpp:169-170
+    const uint32_t type_one = fluid + (p.grid_size[0] - p.boundary_offset + 1) + 2 * (p.grid_size[1] - p.boundary_offset);
+    launch_colors(make_dev(s), s->pos, fluid, type_one, d_out, st_of(s));
+    CM_CUDA(s, cudaGetLastError());
+    return CMAG_OK;
+}
+}  // namespace
+
+int cmag_system_colors(cmag_system *s, float *rgba)
+{
+    if (!s || !rgba) return fail(s, CMAG_ERR_INVALID, "null argument");
+    float4 *d = nullptr;
+    CM_CUDA(s, cudaMalloc((void **)&d, sizeof(float4) * (size_t)s->n));
+    int rc = color_buffer(s, d);
+    cudaError_t e = cudaSuccess;
+    if (rc == CMAG_OK) e = cudaMemcpyAsync(rgba, d, sizeof(float4) * (size_t)s->n, cudaMemcpyDeviceToHost, st_of(s));
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st_of(s));
+    cudaFree(d);
+    if (rc != CMAG_OK) return rc;
+    CM_CUDA(s, e);
+    return CMAG_OK;
+}
+
+int cmag_system_render_ppm(cmag_system *s, const char *path, uint32_t width, uint32_t height)
+{
+    if (!s || !path) return fail(s, CMAG_ERR_INVALID, "null argument");
+    const cmag_sph_params &p = s->p;
+    const float wx = p.grid_size[0] * p.cell_size[0], wy = p.grid_size[1] * p.cell_size[1];
+    if (width == 0 || width > 16384) return fail(s, CMAG_ERR_INVALID, "width must be in [1, 16384]");
+    if (height == 0) height = (uint32_t)std::lround(width * (double)wy / wx);
+    if (height == 0 || height > 16384) return fail(s, CMAG_ERR_INVALID, "height must be in [1, 16384]");
+    const size_t npix = (size_t)width * height;
+    float4 *color = nullptr;
+    uint32_t *owner = nullptr;
+    uint8_t *rgb = nullptr;
+    std::vector<uint8_t> host(3 * npix);
+    cudaError_t e = cudaMalloc((void **)&color, sizeof(float4) * (size_t)s->n);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&owner, sizeof(uint32_t) * npix);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&rgb, 3 * npix);
+    int rc = CMAG_OK;
+    if (e == cudaSuccess) rc = color_buffer(s, color);
+    if (e == cudaSuccess && rc == CMAG_OK) {
+        const float scale = p.system == CMAG_PERISTALSIS ? 1.0f : 255.0f;
+        launch_render(s->pos, color, s->n, p.world_origin[0], p.world_origin[1], width / wx, width,
+                      height, scale, owner, rgb, st_of(s));
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaMemcpyAsync(host.data(), rgb, 3 * npix, cudaMemcpyDeviceToHost, st_of(s));
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st_of(s));
+    }
+    cudaFree(color);
+    cudaFree(owner);
+    cudaFree(rgb);
+    if (rc != CMAG_OK) return rc;
+    CM_CUDA(s, e);
+    FILE *f = std::fopen(path, "wb");
+    if (!f) return fail(s, CMAG_ERR_INVALID, std::string("cannot open ") + path);
+    std::fprintf(f, "P6\n%u %u\n255\n", width, height);
+    const size_t wrote = std::fwrite(host.data(), 1, host.size(), f);
+    std::fclose(f);
+    if (wrote != host.size()) return fail(s, CMAG_ERR_INVALID, std::string("short write to ") + path);
+    return CMAG_OK;
+}
+
 int cmag_system_set_stage_timing(cmag_system *s, int32_t enable)
 {
     if (!s) return fail(nullptr, CMAG_ERR_INVALID, "null handle");

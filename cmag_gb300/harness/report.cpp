@@ -5,6 +5,10 @@
 //   report poiseuille [dir]  Poiseuille.Report/dump.h:15-86      -> XVelocityYPosition<t>.dat
 //   report density [dir] [T] Peristalsis.Report/density.h:12-70  -> density.dat
 //   report forces  [dir] [T] Peristalsis.Report/forces.h:13-88   -> press_{x,y}.dat, visc_{x,y}.dat
+//   report velocityfield [dir]  Peristalsis.Report/velocityfield.h:16-91
+//                                                 -> velocity_field0x3.dat, velocity_field0x4.dat
+//   report pvprofile [dir]   Peristalsis.Report/poiseuille_velocity_profile.h:13-94
+//                                                 -> velocity_profile<t>.dat
 //
 // Same scenes, time frames and output formats as the reference.  The front,
 // height and per-step averages come from device reductions over the fluid
@@ -161,12 +165,82 @@ int forces(const std::string &dir, float until)
     return 0;
 }
 
+// the reference's file-name rule: ostream << t, then character 1 replaced by "x"
+// (appended when the number has a single character): 0.3 -> 0x3, 1 -> 1x
+std::string frame_name(const char *stem, float t)
+{
+    char num[32];
+    std::snprintf(num, sizeof(num), "%g", t);
+    std::string s(num);
+    s.replace(1, 1, "x");
+    return std::string(stem) + s + ".dat";
+}
+
+// every fourth particle's position and velocity at t = 0.3 and 0.4 s
+int velocityfield(const std::string &dir)
+{
+    PeristalsisSystem *s = channel();
+    s->Reset();
+    const int n = s->getNumParticles();
+    std::vector<float> pos(4 * (size_t)n), vel(4 * (size_t)n);
+    for (float t : {0.3f, 0.4f}) {
+        while (s->GetElapsedTime() < t) s->Update();
+        s->getArray(CMAG_POSITION, pos.data(), 0, n);
+        s->getArray(CMAG_VELOCITY, vel.data(), 0, n);
+        FILE *f = std::fopen(path(dir, frame_name("velocity_field", t)).c_str(), "w");
+        for (int i = 0; i < n; i += 4)
+            std::fprintf(f, "%g %g %g %g\n", pos[4 * (size_t)i], pos[4 * (size_t)i + 1],
+                         vel[4 * (size_t)i], vel[4 * (size_t)i + 1]);
+        std::fclose(f);
+    }
+    delete s;
+    return 0;
+}
+
+// The Peristalsis solver as a plain channel (amplitude 0, body force 1e-4):
+// leap-frog u_x against height in the first column of cells, in sorted order.
+int pvprofile(const std::string &dir)
+{
+    const int off = 3, sizex = 64;
+    const float c = std::pow(10.0f, -4.0f);
+    const float radius = 1.0f / (2 * (sizex - 2 * off) * 1000);
+    const uint3 grid = make_uint3(sizex, 64, 4);
+    const uint3 fluid = make_uint3(grid.x, grid.y - 2 * off, 1);
+    PeristalsisSystem *s = new PeristalsisSystem(std::pow(10.0f, -4.0f), fluid, 0, 0, c,
+                                                 make_float3(std::pow(10.0f, -4.0f), 0, 0), off,
+                                                 grid, radius, false);
+    s->Reset();
+    const int n = s->getNumParticles();
+    std::vector<float> pos(4 * (size_t)n), vlf(4 * (size_t)n);
+    std::vector<uint32_t> index(n);
+    for (float t : {0.0225f, 0.045f, 0.1125f, 0.225f, 1.0f}) {
+        while (s->GetElapsedTime() < t) s->Update();
+        s->getArray(CMAG_POSITION, pos.data(), 0, n);
+        s->getArray(CMAG_VELOCITYLEAPFROG, vlf.data(), 0, n);
+        cmag::check(cmag_system_get_uint_array(s->handle(), CMAG_INDEX, index.data(), 0, n), s->handle());
+        const float bottom = s->getWorldOrigin().y + 2 * s->getradius() * off;
+        FILE *f = std::fopen(path(dir, frame_name("velocity_profile", t)).c_str(), "w");
+        std::fprintf(f, "0 0\n");
+        for (int i = 0; i < n; ++i) {
+            const float *p = &pos[4 * (size_t)index[i]];
+            if (p[0] > 0 && p[0] < 2 * s->getradius() && p[1] > bottom &&
+                p[1] < bottom + fluid.y * 2.0f * radius)
+                std::fprintf(f, "%g %g\n", vlf[4 * (size_t)index[i]],
+                             p[1] - s->getWorldOrigin().y - off * 2 * s->getradius());
+        }
+        std::fprintf(f, "0 0.001\n");
+        std::fclose(f);
+    }
+    delete s;
+    return 0;
+}
+
 }  // namespace
 
 int main(int argc, char **argv)
 {
     if (argc < 2) {
-        std::fprintf(stderr, "usage: report xfront|yfront|poiseuille|density|forces [dir] [until]\n");
+        std::fprintf(stderr, "usage: report xfront|yfront|poiseuille|density|forces|velocityfield|pvprofile [dir] [until]\n");
         return 2;
     }
     const std::string what = argv[1], dir = argc > 2 ? argv[2] : ".";
@@ -177,6 +251,8 @@ int main(int argc, char **argv)
         if (what == "poiseuille") return poiseuille(dir);
         if (what == "density") return density(dir, until);
         if (what == "forces") return forces(dir, until);
+        if (what == "velocityfield") return velocityfield(dir);
+        if (what == "pvprofile") return pvprofile(dir);
     } catch (const cmag::Error &e) {
         std::fprintf(stderr, "cmag error %d: %s\n", e.code, e.what());
         return 1;

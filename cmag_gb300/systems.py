@@ -225,6 +225,15 @@ class _System:
         self._chk(lib().cmag_system_fluid_sum(self._h, int(array), s, ctypes.byref(c)))
         return tuple(s), c.value
 
+    # -- headless colours and point view (the Demo programs' VBOs) --
+    def colors(self):
+        out = np.empty((self.numParticles, 4), np.float32)
+        self._chk(lib().cmag_system_colors(self._h, _fp(out)))
+        return out
+
+    def render_ppm(self, path, width=512, height=0):
+        self._chk(lib().cmag_system_render_ppm(self._h, str(path).encode(), int(width), int(height)))
+
     # -- learned closure (DamBreak) --
     def set_closure(self, closure):
         """Attach a cmag_gb300.closure.Closure (None detaches); it must outlive the

@@ -342,6 +342,18 @@ int cmag_sort_particles_noalloc(uint32_t *d_hash, uint32_t *d_index, uint32_t n,
                                 uint32_t key_bits, void *cuda_stream);
 const char *cmag_sort_particles_noalloc_error(void);
 
+/* ---- headless colours and point view ----------------------------------- */
+/* The Demo programs' colour buffers without OpenGL: per particle (original
+ * order) the RGBA values the reference writes into its colour VBO -- DamBreak
+ * colorRamp by index (fluidSystem.cpp:97-114, 165-181), Poiseuille likewise
+ * (poiseuilleFlowSystem.cpp:152-166), Peristalsis Coloring by type and x
+ * (PeristalsisSystem.cpp:409-442, values 0/255).  rgba: host, num_particles x 4. */
+int cmag_system_colors(cmag_system *s, float *rgba);
+/* The point view as a binary PPM image: particles projected on x-y over the
+ * grid's extent, each pixel coloured by the last particle (highest index) in it.
+ * height 0: from the grid's aspect ratio. */
+int cmag_system_render_ppm(cmag_system *s, const char *path, uint32_t width, uint32_t height);
+
 /* ---- batches of independent scenes -------------------------------------- */
 /* No counterpart in the reference, which runs one scene per process (its kernels
  * read one global __constant__ parameter block per library: fluidSystem.cu:17-19,

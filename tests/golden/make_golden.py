@@ -6,7 +6,7 @@ and stores the state before and after one step.  Scenes and parameters come from
 the reference constructors and reset() (restated, since the reference host
 classes need OpenGL).  Run where the reference tree exists:
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [scene ... | channel]
 """
 import os
 import sys
@@ -60,10 +60,44 @@ def make(name, p, warm, release):
     return n
 
 
+CHANNEL_TIMES = (0.0225, 0.045, 0.1125, 0.225)
+
+
+def channel_profile():
+    """Peristalsis.Report/poiseuille_velocity_profile.h:13-94 on the reference
+    kernels: the Peristalsis solver with wall amplitude 0 and body force 1e-4 in
+    x; leap-frog u_x and height above the lower wall of the fluid particles in the
+    first column of cells at each report time (about 2,250 reference steps)."""
+    off, sizex, c = 3, 64, 1e-4
+    r = 1.0 / (2 * (sizex - 2 * off) * 1000)
+    p = O.peristalsis_params(1e-4, (64, 58, 1), 0.0, 0.0, c, (1e-4, 0.0, 0.0), off, (64, 64, 4), r)
+    n = O.particle_count(p)
+    ref = O.RefState(p, n)
+    ref.reset_reference()
+    out = {"times": np.array(CHANNEL_TIMES)}
+    bottom = np.float32(p.world_origin[1]) + np.float32(2 * r * off)
+    for k, t in enumerate(CHANNEL_TIMES):
+        while ref.elapsed < t:
+            ref.step()
+        pos = ref.pos
+        m = (pos[:, 0] > 0) & (pos[:, 0] < 2 * r) & (pos[:, 1] > bottom) & (pos[:, 1] < bottom + 58 * 2 * r)
+        y = pos[m, 1] - np.float32(p.world_origin[1]) - np.float32(off * 2 * r)
+        order = np.argsort(y)
+        out["y%d" % k] = y[order].astype(np.float32)
+        out["u%d" % k] = ref.vlf[m, 0][order].astype(np.float32)
+    np.savez_compressed(os.path.join(HERE, "peristalsis_channel_profile.npz"), **out)
+    return n
+
+
 if __name__ == "__main__":
     if not O.ref_available():
         if not O.build_ref():
             sys.exit("the reference tree is needed to build oracle/_ref")
+    only = sys.argv[1:]
     for name, p, warm, release in scenes():
+        if only and name not in only:
+            continue
         n = make(name, p, warm, release)
         print("%-20s %6d particles, step %d" % (name, n, warm + 1))
+    if not only or "channel" in only:
+        print("peristalsis channel profile: %d particles" % channel_profile())

@@ -99,3 +99,40 @@ def test_fluid_reductions_match_host(gpu):
     assert count == sel.sum() == 32 * 64
     assert np.allclose(sums[:2], meas[sel, :2].astype(np.float64).sum(axis=0), rtol=1e-9)
     s.close()
+
+
+def test_peristalsis_channel_profile_matches_reference(harness, tmp_path):
+    """Peristalsis.Report/poiseuille_velocity_profile.h: the Peristalsis solver with
+    wall amplitude 0 and body force 1e-4 as a channel.  Its leap-frog u_x(y) follows
+    the reference kernels' own profile (tests/golden/peristalsis_channel_profile.npz,
+    made by tests/golden/make_golden.py).  The reference method itself leaves the
+    Poiseuille series once the walls are released after the 0.1 s relaxation (its
+    moving-wall viscous term has no no-slip extrapolation): the flow then
+    accelerates, in the reference and here alike."""
+    run(harness, "pvprofile", tmp_path)
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "peristalsis_channel_profile.npz"))
+    names = {0.0225: "0x0225", 0.045: "0x045", 0.1125: "0x1125", 0.225: "0x225"}
+    for k, t in enumerate(g["times"]):
+        d = np.loadtxt(tmp_path / ("velocity_profile%s.dat" % names[float(t)]))[1:-1]
+        d = d[np.argsort(d[:, 1])]
+        u, y = d[:, 0], d[:, 1]
+        uref, yref = g["u%d" % k].astype(np.float64), g["y%d" % k].astype(np.float64)
+        assert u.shape == uref.shape, (t, u.shape, uref.shape)
+        assert np.abs(y - yref).max() < 1e-3 * 1e-3
+        err = float(np.abs(u - uref).max() / np.abs(uref).max())
+        series = float(np.abs(u - poiseuille_series(y, t)).max() / np.abs(poiseuille_series(y, t)).max())
+        print("t=%g: |u - reference| / max|reference| = %.2e; |u - series| / max|series| = %.3f"
+              % (t, err, series))
+        assert err < (0.02 if t < 0.2 else 0.1), (t, err)
+
+
+def test_peristalsis_velocity_field_dump(harness, tmp_path):
+    """Peristalsis.Report/velocityfield.h: every fourth particle at t = 0.3, 0.4 s."""
+    run(harness, "velocityfield", tmp_path)
+    for name in ("velocity_field0x3.dat", "velocity_field0x4.dat"):
+        d = np.loadtxt(tmp_path / name)
+        assert d.shape[1] == 4 and d.shape[0] > 1000
+        assert np.isfinite(d).all()
+    a = np.loadtxt(tmp_path / "velocity_field0x3.dat")
+    b = np.loadtxt(tmp_path / "velocity_field0x4.dat")
+    assert a.shape == b.shape and not np.array_equal(a, b)  # the walls moved the fluid
