@@ -78,7 +78,9 @@ class SphParams(ctypes.Structure):
         ("clamp_z", ctypes.c_int32),
         ("z_min_border", ctypes.c_float),
         ("z_max_border", ctypes.c_float),
-        ("reserved", ctypes.c_int32 * 5),
+        ("wall_noslip", ctypes.c_int32),
+        ("wall_beta_max", ctypes.c_float),
+        ("reserved", ctypes.c_int32 * 3),
     ]
 
     def copy(self):

@@ -214,7 +214,7 @@ int launch_groups(cmag_batch *b, bool force)
         if (force) {
             const bool per = lg.system == CMAG_PERISTALSIS;
             launch_force(rep, v, lg.g_force, b->spos, b->svel, b->aux, sorted_idx(b), b->off,
-                         per ? b->vforce : b->acc, per ? b->pforce : nullptr, gs);
+                         per ? b->vforce : b->acc, per ? b->pforce : nullptr, b->phase, gs);
         } else {
             launch_density(rep, v, lg.g_density, b->spos, b->off, b->meas, b->aux, gs);
         }
@@ -1073,7 +1073,8 @@ int cmag_batch_autotune(cmag_batch *b, int32_t reps)
             for (int k = 0; k < 3; ++k) {
                 auto run = [&]() {
                     if (pass == 0) launch_density(rep, v, lanes[k], b->spos, b->off, b->meas, b->aux, st);
-                    else launch_force(rep, v, lanes[k], b->spos, b->svel, b->aux, sorted_idx(b), b->off, fa, fb, st);
+                    else launch_force(rep, v, lanes[k], b->spos, b->svel, b->aux, sorted_idx(b), b->off, fa, fb,
+                                      b->phase, st);
                 };
                 run();
                 cudaEventRecord(e0, st);

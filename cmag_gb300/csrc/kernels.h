@@ -63,9 +63,10 @@ void launch_cell_view(const uint32_t *off, uint32_t scan_base, uint32_t scan_cel
 // (p = the parameters of any of the group's scenes).
 void launch_density(const DevParams &p, const BatchView &bv, int group, const float4 *spos,
                     const uint32_t *off, float4 *meas, float2 *aux, cudaStream_t st);
+// ph: the Peristalsis phase (one per scene in a batch; read with wall_noslip only)
 void launch_force(const DevParams &p, const BatchView &bv, int group, const float4 *spos,
                   const float4 *svel, const float2 *aux, const uint32_t *idx, const uint32_t *off,
-                  float4 *out_a, float4 *out_b, cudaStream_t st);
+                  float4 *out_a, float4 *out_b, const PhaseState *ph, cudaStream_t st);
 
 // ---- integration and wall motion (integrate.cu) ------------------------------
 // bv empty: one scene; otherwise every particle of the batch with its scene's

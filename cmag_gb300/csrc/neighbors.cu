@@ -144,6 +144,52 @@ __global__ void __launch_bounds__(256, 6)
     }
 }
 
+// ---------------------------------------------- no-slip into moving walls --
+// The closest point (xa, ya) of one Peristalsis wall interface
+// y_w(x) = base + sgn A sin(K ((x - ox) - c t)) to a fluid particle at (x0, y0),
+// by Newton's method on f(x) = (x0 - x) + (y0 - y_w(x)) y_w'(x) (the reference's
+// commented-out BottomF/TopF + rtnewt, PeristalsisViscousForce.cu:4-66), with the
+// interface's slope there, 1 / (distance of the particle) and the wall's vertical
+// velocity.  Each wall particle's velocity is then extrapolated so that the fluid
+// velocity relative to the wall vanishes on the interface:
+// v_i - v_j -> beta (v_i - v_w), beta = min(beta_max, 1 + d_j / d_i), d_j the wall
+// particle's distance from the interface's tangent (the commented-out
+// getVelocityDiff, PeristalsisViscousForce.cu:68-138, which took v_w = 0).
+struct WallSide {
+    float xa, ya, slope, inv_norm, inv_da, vw;
+};
+
+__device__ __forceinline__ WallSide wall_side(const DevParams &p, float amp, float t, bool moving,
+                                              float sgn, float base, float x0, float y0)
+{
+    const float K = p.wave_k;
+    float x = x0;
+#pragma unroll 1
+    for (int it = 0; it < 8; ++it) {
+        float s, c;
+        sincosf(K * ((x - p.ox) - p.wave_speed * t), &s, &c);
+        const float yw = base + sgn * amp * s;
+        const float d1 = sgn * amp * K * c, d2 = -sgn * amp * K * K * s;
+        const float f = (x0 - x) + (y0 - yw) * d1;
+        const float df = -1.0f - d1 * d1 + (y0 - yw) * d2;
+        const float dx = f / df;
+        x -= dx;
+        if (!(fabsf(dx) >= 1e-3f * p.r)) break;
+    }
+    if (!(fabsf(x - x0) < 4.0f * p.h)) x = x0;  // no convergence: the vertical distance
+    float s, c;
+    sincosf(K * ((x - p.ox) - p.wave_speed * t), &s, &c);
+    WallSide w;
+    w.xa = x;
+    w.ya = base + sgn * amp * s;
+    w.slope = sgn * amp * K * c;
+    w.inv_norm = rsqrtf(1.0f + w.slope * w.slope);
+    const float da = sqrtf((x0 - x) * (x0 - x) + (y0 - w.ya) * (y0 - w.ya));
+    w.inv_da = 1.0f / fmaxf(da, 1e-6f * p.r);
+    w.vw = moving ? -sgn * amp * K * p.wave_speed * c : 0.0f;  // d y_w / dt
+    return w;
+}
+
 // ------------------------------------------------------------------ force --
 // 256 threads, 4 blocks per SM: at most 64 registers
 template <int SYS, bool PLANAR, bool TRIM, int G, bool BATCH>
@@ -151,7 +197,8 @@ __global__ void __launch_bounds__(256, 4)
     k_force(DevParams pv, BatchView bv, const float4 *__restrict__ spos,
             const float4 *__restrict__ svel, const float2 *__restrict__ aux,
             const uint32_t *__restrict__ idx, const uint32_t *__restrict__ off_all,
-            float4 *__restrict__ out_a, float4 *__restrict__ out_b)
+            float4 *__restrict__ out_a, float4 *__restrict__ out_b,
+            const PhaseState *__restrict__ ph_all)
 {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t i = (BATCH ? bv.first : 0u) + t / G;
@@ -169,6 +216,16 @@ __global__ void __launch_bounds__(256, 4)
         const float2 ai = aux[i];
         const float pterm = ai.x;
         const int3 g = grid_pos(p, pi.x, pi.y, pi.z);
+        // Peristalsis no-slip walls: the interfaces as seen by this fluid particle
+        const bool noslip = SYS == CMAG_PERISTALSIS && p.wall_noslip && pi.w == 0.0f;
+        WallSide wb{}, wt{};
+        if (noslip) {
+            const PhaseState &ph = ph_all[BATCH ? bv.scene_of[i] : 0u];
+            const float amp = ph.is_bc ? ph.configure_height : p.amplitude;
+            const float tw = ph.is_bc ? 0.0f : ph.t;
+            wb = wall_side(p, amp, tw, !ph.is_bc, 1.0f, -p.half_fluid_h, pi.x, pi.y);
+            wt = wall_side(p, amp, tw, !ph.is_bc, -1.0f, p.half_fluid_h, pi.x, pi.y);
+        }
         for_each_candidate<SYS, PLANAR, TRIM, G>(
             p, off, lane, g, frac_cell(p, pi), [&](uint32_t j, float sx, float sy, float sz) {
                 if (j == i) return;
@@ -237,9 +294,18 @@ __global__ void __launch_bounds__(256, 4)
                     const float2 aj = __ldg(aux + j);
                     const float4 vj = __ldg(svel + j);
                     const float sv = p.visc_coeff * temp * ai.y * aj.y * inv_d;
-                    ax = __fmaf_rn(sv, vi.x - vj.x, ax);
-                    ay = __fmaf_rn(sv, vi.y - vj.y, ay);
-                    az = __fmaf_rn(sv, vi.z - vj.z, az);
+                    float dvx = vi.x - vj.x, dvy = vi.y - vj.y, dvz = vi.z - vj.z;
+                    if (noslip && pj.w != 0.0f) {
+                        const WallSide &w = pj.w > 0.0f ? wb : wt;
+                        const float db = fabsf(w.slope * (pj.x + sx - w.xa) - (pj.y + sy - w.ya)) * w.inv_norm;
+                        const float beta = fminf(p.wall_beta_max, 1.0f + db * w.inv_da);
+                        dvx = beta * vi.x;
+                        dvy = beta * (vi.y - w.vw);
+                        dvz = beta * vi.z;
+                    }
+                    ax = __fmaf_rn(sv, dvx, ax);
+                    ay = __fmaf_rn(sv, dvy, ay);
+                    az = __fmaf_rn(sv, dvz, az);
                     const float sp = -p.mass * temp * (pterm + aj.x) * inv_d;
                     bx = __fmaf_rn(sp, rx, bx); by = __fmaf_rn(sp, ry, by); bz = __fmaf_rn(sp, rz, bz);
                 }
@@ -262,18 +328,18 @@ __global__ void __launch_bounds__(256, 4)
 template <int SYS, bool PLANAR, bool TRIM, int G>
 void launch_pair(bool force, const DevParams &p, const BatchView &bv, const float4 *spos,
                  const float4 *svel, float4 *meas, float2 *aux, const uint32_t *idx,
-                 const uint32_t *off, float4 *a, float4 *b, cudaStream_t st)
+                 const uint32_t *off, float4 *a, float4 *b, const PhaseState *ph, cudaStream_t st)
 {
     const uint64_t threads = (uint64_t)(bv.scenes ? bv.count : p.n) * G;
     const uint32_t blocks = (uint32_t)((threads + 255) / 256);
     if (bv.scenes) {
         if (force)
-            k_force<SYS, PLANAR, TRIM, G, true><<<blocks, 256, 0, st>>>(p, bv, spos, svel, aux, idx, off, a, b);
+            k_force<SYS, PLANAR, TRIM, G, true><<<blocks, 256, 0, st>>>(p, bv, spos, svel, aux, idx, off, a, b, ph);
         else
             k_density<SYS, PLANAR, TRIM, G, true><<<blocks, 256, 0, st>>>(p, bv, spos, off, meas, aux);
     } else {
         if (force)
-            k_force<SYS, PLANAR, TRIM, G, false><<<blocks, 256, 0, st>>>(p, bv, spos, svel, aux, idx, off, a, b);
+            k_force<SYS, PLANAR, TRIM, G, false><<<blocks, 256, 0, st>>>(p, bv, spos, svel, aux, idx, off, a, b, ph);
         else
             k_density<SYS, PLANAR, TRIM, G, false><<<blocks, 256, 0, st>>>(p, bv, spos, off, meas, aux);
     }
@@ -286,15 +352,16 @@ struct PairArgs {
     float2 *aux;
     const uint32_t *idx, *off;
     float4 *a, *b;
+    const PhaseState *ph;
 };
 
 template <int SYS, bool PLANAR, bool TRIM>
 void dispatch_g(int group, const DevParams &p, const BatchView &bv, const PairArgs &x, cudaStream_t st)
 {
     switch (group) {
-    case 2: launch_pair<SYS, PLANAR, TRIM, 2>(x.force, p, bv, x.spos, x.svel, x.meas, x.aux, x.idx, x.off, x.a, x.b, st); break;
-    case 4: launch_pair<SYS, PLANAR, TRIM, 4>(x.force, p, bv, x.spos, x.svel, x.meas, x.aux, x.idx, x.off, x.a, x.b, st); break;
-    default: launch_pair<SYS, PLANAR, TRIM, 1>(x.force, p, bv, x.spos, x.svel, x.meas, x.aux, x.idx, x.off, x.a, x.b, st); break;
+    case 2: launch_pair<SYS, PLANAR, TRIM, 2>(x.force, p, bv, x.spos, x.svel, x.meas, x.aux, x.idx, x.off, x.a, x.b, x.ph, st); break;
+    case 4: launch_pair<SYS, PLANAR, TRIM, 4>(x.force, p, bv, x.spos, x.svel, x.meas, x.aux, x.idx, x.off, x.a, x.b, x.ph, st); break;
+    default: launch_pair<SYS, PLANAR, TRIM, 1>(x.force, p, bv, x.spos, x.svel, x.meas, x.aux, x.idx, x.off, x.a, x.b, x.ph, st); break;
     }
 }
 
@@ -326,15 +393,15 @@ void dispatch_sys(int group, const DevParams &p, const BatchView &bv, const Pair
 void launch_density(const DevParams &p, const BatchView &bv, int group, const float4 *spos,
                     const uint32_t *off, float4 *meas, float2 *aux, cudaStream_t st)
 {
-    dispatch_sys(group, p, bv, PairArgs{false, spos, nullptr, meas, aux, nullptr, off, nullptr, nullptr}, st);
+    dispatch_sys(group, p, bv, PairArgs{false, spos, nullptr, meas, aux, nullptr, off, nullptr, nullptr, nullptr}, st);
 }
 
 void launch_force(const DevParams &p, const BatchView &bv, int group, const float4 *spos,
                   const float4 *svel, const float2 *aux, const uint32_t *idx, const uint32_t *off,
-                  float4 *out_a, float4 *out_b, cudaStream_t st)
+                  float4 *out_a, float4 *out_b, const PhaseState *ph, cudaStream_t st)
 {
     dispatch_sys(group, p, bv,
-                 PairArgs{true, spos, svel, nullptr, const_cast<float2 *>(aux), idx, off, out_a, out_b}, st);
+                 PairArgs{true, spos, svel, nullptr, const_cast<float2 *>(aux), idx, off, out_a, out_b, ph}, st);
 }
 
 }  // namespace cmag

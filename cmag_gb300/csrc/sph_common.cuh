@@ -48,6 +48,9 @@ struct DevParams {
     float lj_a2;                  // a^2 of the wall force
     float av_coeff;               // 2 alpha h c0 (fluid_kernel.cu:229-230)
     float visc_coeff;             // m (mu + mu) (poiseuilleFlowKernel.cu:242-243)
+    // Peristalsis no-slip extrapolation into moving walls (0: reference v_i - v_j)
+    int32_t wall_noslip;
+    float wall_beta_max;
     // batches: where this scene's cell table and particles start in the shared arrays
     uint32_t table_base;
     uint32_t part_base;

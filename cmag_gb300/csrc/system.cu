@@ -195,6 +195,8 @@ DevParams make_dev_params(const cmag_sph_params &p, uint32_t n, const SceneLayou
     d.lj_a2 = p.lj_a * p.lj_a;
     d.av_coeff = (float)(2.0 * p.av_alpha * h * p.soundspeed);
     d.visc_coeff = (float)((double)p.particle_mass * (2.0 * p.mu));
+    d.wall_noslip = (p.system == CMAG_PERISTALSIS && p.wall_noslip) ? 1 : 0;
+    d.wall_beta_max = p.wall_beta_max > 0.0f ? p.wall_beta_max : 1000.0f;
     return d;
 }
 
@@ -340,10 +342,10 @@ int record_step(cmag_system *s, int last, bool timed)
     if (last >= CMAG_STAGE_FORCE) {
         if (p.system == CMAG_PERISTALSIS)
             launch_force(d, BatchView{}, s->g_force, s->spos, s->svel, s->aux, sorted_idx(s), s->off,
-                         s->vforce, s->pforce, st);
+                         s->vforce, s->pforce, s->phase, st);
         else
             launch_force(d, BatchView{}, s->g_force, s->spos, s->svel, s->aux, sorted_idx(s), s->off, s->acc,
-                         nullptr, st);
+                         nullptr, s->phase, st);
         if (s->closure)
             launch_closure_apply(d, s->closure->view(), s->spos, s->svel, s->aux, s->meas,
                                  sorted_idx(s), s->off, s->acc, s->closure_x, st);
@@ -1125,10 +1127,12 @@ int cmag_system_autotune(cmag_system *s, int32_t reps)
     }
     launch_density(d, BatchView{}, gd, s->spos, s->off, s->meas, s->aux, st);
     for (int k = 0; k < 3; ++k) {
-        launch_force(d, BatchView{}, groups[k], s->spos, s->svel, s->aux, sorted_idx(s), s->off, fa, fb, st);
+        launch_force(d, BatchView{}, groups[k], s->spos, s->svel, s->aux, sorted_idx(s), s->off, fa, fb,
+                     s->phase, st);
         cudaEventRecord(a, st);
         for (int r = 0; r < reps; ++r)
-            launch_force(d, BatchView{}, groups[k], s->spos, s->svel, s->aux, sorted_idx(s), s->off, fa, fb, st);
+            launch_force(d, BatchView{}, groups[k], s->spos, s->svel, s->aux, sorted_idx(s), s->off, fa, fb,
+                     s->phase, st);
         cudaEventRecord(b, st);
         cudaEventSynchronize(b);
         float ms = 0;

@@ -9,6 +9,7 @@
 //                                                 -> velocity_field0x3.dat, velocity_field0x4.dat
 //   report pvprofile [dir]   Peristalsis.Report/poiseuille_velocity_profile.h:13-94
 //                                                 -> velocity_profile<t>.dat
+//   report pvprofile_noslip [dir]  the same with no-slip moving-wall extrapolation
 //
 // Same scenes, time frames and output formats as the reference.  The front,
 // height and per-step averages come from device reductions over the fluid
@@ -199,7 +200,9 @@ int velocityfield(const std::string &dir)
 
 // The Peristalsis solver as a plain channel (amplitude 0, body force 1e-4):
 // leap-frog u_x against height in the first column of cells, in sorted order.
-int pvprofile(const std::string &dir)
+// noslip: with the no-slip extrapolation into the walls (an option of this
+// build; the reference keeps it commented out).
+int pvprofile(const std::string &dir, bool noslip)
 {
     const int off = 3, sizex = 64;
     const float c = std::pow(10.0f, -4.0f);
@@ -209,6 +212,11 @@ int pvprofile(const std::string &dir)
     PeristalsisSystem *s = new PeristalsisSystem(std::pow(10.0f, -4.0f), fluid, 0, 0, c,
                                                  make_float3(std::pow(10.0f, -4.0f), 0, 0), off,
                                                  grid, radius, false);
+    if (noslip) {
+        cmag_sph_params p = s->params();
+        p.wall_noslip = 1;
+        s->setParams(p);
+    }
     s->Reset();
     const int n = s->getNumParticles();
     std::vector<float> pos(4 * (size_t)n), vlf(4 * (size_t)n);
@@ -240,7 +248,7 @@ int pvprofile(const std::string &dir)
 int main(int argc, char **argv)
 {
     if (argc < 2) {
-        std::fprintf(stderr, "usage: report xfront|yfront|poiseuille|density|forces|velocityfield|pvprofile [dir] [until]\n");
+        std::fprintf(stderr, "usage: report xfront|yfront|poiseuille|density|forces|velocityfield|pvprofile|pvprofile_noslip [dir] [until]\n");
         return 2;
     }
     const std::string what = argv[1], dir = argc > 2 ? argv[2] : ".";
@@ -252,7 +260,8 @@ int main(int argc, char **argv)
         if (what == "density") return density(dir, until);
         if (what == "forces") return forces(dir, until);
         if (what == "velocityfield") return velocityfield(dir);
-        if (what == "pvprofile") return pvprofile(dir);
+        if (what == "pvprofile") return pvprofile(dir, false);
+        if (what == "pvprofile_noslip") return pvprofile(dir, true);
     } catch (const cmag::Error &e) {
         std::fprintf(stderr, "cmag error %d: %s\n", e.code, e.what());
         return 1;

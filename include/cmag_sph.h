@@ -154,7 +154,12 @@ typedef struct cmag_sph_params {
                                     z_max_border] like the x/y clamps (3-D tanks)   */
     float z_min_border;
     float z_max_border;
-    int32_t reserved[5];
+    int32_t wall_noslip;         /* Peristalsis: 1 = no-slip extrapolation of the fluid
+                                    velocity into the moving walls (wall distance by
+                                    Newton's method, as the reference's commented-out
+                                    PeristalsisViscousForce.cu:4-138); 0 = reference   */
+    float wall_beta_max;         /* cap of that extrapolation factor (0: 1000)        */
+    int32_t reserved[3];
 } cmag_sph_params;
 
 /* Reference-constructor parameter derivations.

@@ -639,6 +639,54 @@ static f3 poiseuille_vab(const cmag_sph_params *p, f3 vi, f3 pi, f3 vj, f3 pj, f
     return sub3(vi, vj);
 }
 
+/* Peristalsis no-slip extrapolation into the moving walls (an option of this
+ * build; the reference keeps it commented out, PeristalsisViscousForce.cu:4-138):
+ * the wall interfaces y = +-half height +- A sin(K((x - ox) - c t)), their closest
+ * point to a fluid particle by Newton's method, and the wall velocity there.  The
+ * wall state (amplitude, time, moving) is set by orc_set_wall_state or orc_step. */
+static float g_wall_amp = 0.0f, g_wall_t = 0.0f;
+static int g_wall_moving = 0;
+
+void orc_set_wall_state(float amp, float t, int32_t moving)
+{
+    g_wall_amp = amp;
+    g_wall_t = t;
+    g_wall_moving = moving;
+}
+
+typedef struct { float xa, ya, slope, inv_norm, inv_da, vw; } wall_side_t;
+
+static wall_side_t wall_side(const cmag_sph_params *p, float sgn, float base, float x0, float y0)
+{
+    const float K = 3.141592654f * p->wave_count / (p->fluid_size[0] * p->particle_radius);
+    const float ox = p->world_origin[0], c = p->wave_speed, amp = g_wall_amp, t = g_wall_t;
+    const float r = p->particle_radius, h = p->smoothing_radius;
+    float x = x0;
+    for (int it = 0; it < 8; ++it) {
+        float ph = K * ((x - ox) - c * t);
+        float s = sinf(ph), cs = cosf(ph);
+        float yw = base + sgn * amp * s;
+        float d1 = sgn * amp * K * cs, d2 = -sgn * amp * K * K * s;
+        float f = (x0 - x) + (y0 - yw) * d1;
+        float df = -1.0f - d1 * d1 + (y0 - yw) * d2;
+        float dx = f / df;
+        x -= dx;
+        if (!(fabsf(dx) >= 1e-3f * r)) break;
+    }
+    if (!(fabsf(x - x0) < 4.0f * h)) x = x0;
+    float ph = K * ((x - ox) - c * t);
+    float s = sinf(ph), cs = cosf(ph);
+    wall_side_t w;
+    w.xa = x;
+    w.ya = base + sgn * amp * s;
+    w.slope = sgn * amp * K * cs;
+    w.inv_norm = 1.0f / sqrtf(1.0f + w.slope * w.slope);
+    float da = sqrtf((x0 - x) * (x0 - x) + (y0 - w.ya) * (y0 - w.ya));
+    w.inv_da = 1.0f / fmaxf(da, 1e-6f * r);
+    w.vw = g_wall_moving ? -sgn * amp * K * c * cs : 0.0f;
+    return w;
+}
+
 /* Force on sorted particle i.  Returns 0 when the reference writes nothing for i
  * (DamBreak non-fluid particles, fluid_kernel.cu:258). */
 /* |t| summed component-wise over the pair terms: the scale of the rounding error
@@ -659,6 +707,13 @@ static int force_one(const cmag_sph_params *p, const float *spos, const float *s
     int c = p->cell_count;
     float h = p->smoothing_radius, m = p->particle_mass;
     f3 fA = mk3(0, 0, 0), fB = mk3(0, 0, 0);
+    const int noslip = p->system == CMAG_PERISTALSIS && p->wall_noslip && wi == 0.0f;
+    wall_side_t wb = {0, 0, 0, 0, 0, 0}, wt = wb;
+    if (noslip) {
+        const float hf = p->fluid_size[1] * p->particle_radius;
+        wb = wall_side(p, 1.0f, -hf, pi.x, pi.y);
+        wt = wall_side(p, -1.0f, hf, pi.x, pi.y);
+    }
     for (int z = -c; z <= c; z++)
         for (int y = -c; y <= c; y++)
             for (int x = -c; x <= c; x++) {
@@ -738,11 +793,20 @@ static int force_one(const cmag_sph_params *p, const float *spos, const float *s
                                 float temp = kernel_dw(p, q);
                                 /* viscous, PeristalsisViscousForce.cu:206-213 */
                                 f3 vab = sub3(vi, vj);
+                                f3 vmag = add3(abs3(vi), abs3(vj));
+                                if (noslip && wj != 0.0f) {
+                                    const wall_side_t *w = wj > 0.0f ? &wb : &wt;
+                                    const f3 pjs = sub3(pi, rp);  /* j through its image shift */
+                                    float db = fabsf(w->slope * (pjs.x - w->xa) - (pjs.y - w->ya)) * w->inv_norm;
+                                    float bmax = p->wall_beta_max > 0.0f ? p->wall_beta_max : 1000.0f;
+                                    float beta = fminf(bmax, 1.0f + db * w->inv_da);
+                                    vab = mk3(beta * vi.x, beta * (vi.y - w->vw), beta * vi.z);
+                                    vmag = add3(abs3(vab), smul3(beta, abs3(mk3(0, w->vw, 0))));
+                                }
                                 float sv = m * temp * (p->mu + p->mu);
                                 f3 tv = divs3(smul3(sv, vab), rho * rho2 * dist);
                                 tA = add3(tA, tv);
-                                scA = add3(scA, muls3(add3(abs3(vi), abs3(vj)),
-                                                      fabsf(sv) * kernel_dw_cond(p, q) / (rho * rho2 * dist)));
+                                scA = add3(scA, muls3(vmag, fabsf(sv) * kernel_dw_cond(p, q) / (rho * rho2 * dist)));
                                 /* pressure, PeristalsisPressureForce.cu:39-43 */
                                 float sp = -1.0f * m * temp * (pr / powf(rho, 2) + pr2 / powf(rho2, 2));
                                 f3 tp = smul3(sp, normalize3(rp));
@@ -915,10 +979,12 @@ void orc_step(cmag_sph_params *p, uint32_t n, uint64_t ncells, float *pos, float
               int threads, int stop_after)
 {
     float dt = p->delta_time;
+    static float last_configured = 0.0f;
     if (p->system == CMAG_PERISTALSIS && p->is_boundary_configuration) { /* :330-343 */
         phase[1] += dt;
         if (phase[3] < p->amplitude) {
             orc_configure_boundary(p, pos, phase[3], n);
+            last_configured = phase[3];
             phase[3] += dt * powf(10.0f, -3.0f);
         } else {
             phase[2] -= dt;
@@ -933,6 +999,10 @@ void orc_step(cmag_sph_params *p, uint32_t n, uint64_t ncells, float *pos, float
     if (stop_after == CMAG_STAGE_REORDER) return;
     orc_density(p, spos, meas, cs, ce, n, threads);
     if (stop_after == CMAG_STAGE_DENSITY) return;
+    if (p->system == CMAG_PERISTALSIS && p->wall_noslip) {
+        if (p->is_boundary_configuration) orc_set_wall_state(last_configured, 0.0f, 0);
+        else orc_set_wall_state(p->amplitude, phase[0] - phase[1], 1);
+    }
     if (p->system == CMAG_PERISTALSIS)
         orc_force(p, spos, svel, meas, idx, cs, ce, vforce, pforce, n, threads);
     else

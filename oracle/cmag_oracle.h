@@ -70,6 +70,9 @@ void orc_force_scale(const cmag_sph_params *p, const float *spos, const float *s
                      const float *meas, const uint32_t *idx, const uint32_t *cell_start,
                      const uint32_t *cell_end, float *scale_a, float *scale_b, uint32_t n,
                      int threads);
+/* Peristalsis with wall_noslip: the wall state the force uses (interface
+ * amplitude, time of the wall law, whether the walls move) */
+void orc_set_wall_state(float amp, float t, int32_t moving);
 /* single-particle evaluations on given sorted arrays (spot checks at full size) */
 float orc_density_at(const cmag_sph_params *p, const float *spos, const uint32_t *cell_start,
                      const uint32_t *cell_end, uint32_t i);

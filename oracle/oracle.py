@@ -80,6 +80,7 @@ def lib():
                                 ctypes.c_uint32, ctypes.c_int]
         L.orc_force_scale.argtypes = [sp, c_f32p, c_f32p, c_f32p, c_u32p, c_u32p, c_u32p, c_f32p,
                                       c_f32p, ctypes.c_uint32, ctypes.c_int]
+        L.orc_set_wall_state.argtypes = [ctypes.c_float, ctypes.c_float, ctypes.c_int32]
         L.orc_density_at.argtypes = [sp, c_f32p, c_u32p, c_u32p, ctypes.c_uint32]
         L.orc_density_at.restype = ctypes.c_float
         L.orc_force_at.argtypes = [sp, c_f32p, c_f32p, c_f32p, c_u32p, c_u32p, ctypes.c_uint32,
@@ -245,10 +246,13 @@ class OracleState(_StateBase):
                               self.n, threads)
         return sa, sb
 
-    def forces_on(self, meas, spos=None, svel=None, threads=1):
+    def forces_on(self, meas, spos=None, svel=None, threads=1, wall=None):
         """This step's forces recomputed on given sorted inputs (e.g. another
         implementation's measures), with this state's sort and cell ranges.
-        Returns (out_a, out_b, scale_a, scale_b), original order."""
+        wall: (amplitude, time, moving) of the Peristalsis wall law for the
+        no-slip option.  Returns (out_a, out_b, scale_a, scale_b), original order."""
+        if wall is not None:
+            lib().orc_set_wall_state(float(wall[0]), float(wall[1]), int(wall[2]))
         meas = np.ascontiguousarray(meas, np.float32)
         spos = self.spos if spos is None else np.ascontiguousarray(spos, np.float32)
         svel = self.svel if svel is None else np.ascontiguousarray(svel, np.float32)

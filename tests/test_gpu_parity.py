@@ -136,6 +136,34 @@ def test_peristalsis_moving_walls_step(gpu):
     s.close()
 
 
+def test_peristalsis_noslip_walls_step(gpu):
+    """The no-slip extrapolation into the moving walls (wall_noslip = 1, an option
+    of this build): one step with the walls in motion against the oracle's
+    restatement (wall distance by Newton's method, wall velocity from the law)."""
+    s, ref = _peristalsis()
+    ref.p.is_boundary_configuration = 0
+    ref.p.wall_noslip = 1
+    sp = s.params
+    sp.wall_noslip = 1
+    s.set_params(sp)
+    for _ in range(12):
+        ref.step()
+    s.load_state(ref)
+    pre = O.OracleState(ref.p, ref.n).set_state(ref)
+    plain = O.OracleState(ref.p, ref.n).set_state(ref)
+    plain.p.wall_noslip = 0
+    plain.step()
+    ref.step()
+    s.update()
+    out = compare_step(s.state(), pre, ref, label="peristalsis no-slip: ")
+    # the option changes the viscous force next to the walls and nowhere else
+    d = np.abs(ref.vforce[:, :2] - plain.vforce[:, :2]).max(axis=1)
+    near = d > 0
+    assert near.any() and (~near).any()
+    print("no-slip step:", out, "particles changed:", int(near.sum()))
+    s.close()
+
+
 @pytest.mark.parametrize("graphs", [True, False])
 def test_graph_replay_equals_plain_launches(gpu, graphs):
     """A captured-and-replayed step produces the same bits as plain launches."""

@@ -136,3 +136,22 @@ def test_peristalsis_velocity_field_dump(harness, tmp_path):
     a = np.loadtxt(tmp_path / "velocity_field0x3.dat")
     b = np.loadtxt(tmp_path / "velocity_field0x4.dat")
     assert a.shape == b.shape and not np.array_equal(a, b)  # the walls moved the fluid
+
+
+def test_peristalsis_noslip_channel_runs(harness, tmp_path):
+    """The same channel with the no-slip extrapolation into the walls
+    (wall_noslip = 1).  The reference method's channel leaves the Poiseuille
+    series exponentially after about 0.05 s (previous test; the reference kernels
+    on the CPU do the same, for any dt, and the wall treatment does not change
+    it), so this checks the early, wall-dominated profile: closer to the series
+    than the reference treatment's at t = 0.0225 and 0.045 s."""
+    run(harness, "pvprofile_noslip", tmp_path)
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "peristalsis_channel_profile.npz"))
+    for k, (t, name) in enumerate(((0.0225, "0x0225"), (0.045, "0x045"))):
+        d = np.loadtxt(tmp_path / ("velocity_profile%s.dat" % name))[1:-1]
+        u, y = d[:, 0], d[:, 1]
+        e_noslip = float(np.abs(u - poiseuille_series(y, t)).max() / np.abs(poiseuille_series(y, t)).max())
+        yr, ur = g["y%d" % k].astype(np.float64), g["u%d" % k].astype(np.float64)
+        e_ref = float(np.abs(ur - poiseuille_series(yr, t)).max() / np.abs(poiseuille_series(yr, t)).max())
+        print("t=%g: error vs series, reference walls %.3f, no-slip walls %.3f" % (t, e_ref, e_noslip))
+        assert np.isfinite(u).all() and e_noslip < e_ref
