@@ -46,6 +46,64 @@ def sort_bytes(passes):
     return 4 + 16 * passes
 
 
+# Algorithmic flops of the neighbour loops: 10 per candidate (distance test) and
+# per interacting pair 15 (density) or 45 (force).
+FLOPS_CANDIDATE, FLOPS_DENSITY_PAIR, FLOPS_FORCE_PAIR = 10, 15, 45
+
+
+def pair_counts(p, pos, sample=2048, seed=0):
+    """Mean candidates visited (the kernels' trimmed row walk) and mean interacting
+    neighbours (|r| < 2h, other than itself) per fluid particle, from a seeded sample."""
+    from scipy.spatial import cKDTree
+    rng = np.random.default_rng(seed)
+    fluid_w = 4.0 if p.system == 0 else 0.0
+    xyz = pos[:, :3].astype(np.float64)
+    fl = np.flatnonzero(pos[:, 3] == fluid_w)
+    pick = fl[rng.choice(fl.size, min(sample, fl.size), replace=False)]
+    h = float(p.smoothing_radius)
+    tree = cKDTree(xyz)
+    inter = np.array([len(v) - 1 for v in tree.query_ball_point(xyz[pick], 2.0 * h)], np.float64)
+    g = np.array([int(v) for v in p.grid_size])
+    o = np.array([float(v) for v in p.world_origin])
+    if p.system == 0:
+        cs = np.array([float(v) for v in p.cell_size])
+        cell = np.floor((xyz - o) / cs).astype(np.int64)
+    else:
+        cs = np.full(3, 2.0 * float(p.particle_radius))
+        cell = np.floor((xyz - o) * 0.5 / float(p.particle_radius)).astype(np.int64)
+    cell %= g
+    counts = np.zeros((g[2], g[1], g[0]), np.int64)
+    np.add.at(counts, (cell[:, 2], cell[:, 1], cell[:, 0]), 1)
+    c = int(p.cell_count)
+    s2 = (2.0 * h / cs[0]) ** 2
+    trim = not (p.system == 0 and not p.lj_cutoff)
+    planar = int(p.dims) == 2
+    cand = np.zeros(pick.size)
+    for k, i in enumerate(pick):
+        f = (xyz[i] - o) / cs
+        gi = np.floor(f).astype(np.int64)
+        tot = 0
+        for dz in ([0] if planar else range(-c, c + 1)):
+            for dy in range(-c, c + 1):
+                xa, xb = gi[0] - c, gi[0] + c
+                if trim:
+                    yu, zu = gi[1] + dy, gi[2] + dz
+                    dym = (yu - f[1]) if dy > 0 else ((f[1] - (yu + 1)) if dy < 0 else 0.0)
+                    dzm = (zu - f[2]) if dz > 0 else ((f[2] - (zu + 1)) if dz < 0 else 0.0)
+                    dym, dzm = max(dym - 1e-3, 0.0), max(dzm - 1e-3, 0.0)
+                    r2 = s2 - dym * dym - dzm * dzm
+                    if r2 <= 0:
+                        continue
+                    R = np.sqrt(r2) + 1e-3
+                    xa, xb = max(xa, int(np.floor(f[0] - R))), min(xb, int(np.floor(f[0] + R)))
+                    if xa > xb:
+                        continue
+                xs = np.arange(xa, xb + 1) % g[0]
+                tot += int(counts[(gi[2] + dz) % g[2], (gi[1] + dy) % g[1], xs].sum())
+        cand[k] = tot
+    return float(cand.mean()), float(inter.mean())
+
+
 def load_peaks():
     path = os.path.join(HERE, "MEASURED_PEAKS.json")
     try:
@@ -514,6 +572,24 @@ def main():
         with open(tpath) as f:
             traffic = json.load(f).get(dom)
 
+    # ---- the neighbour loops against the FP32 issue roofline ----
+    fp32 = None
+    if not batched:
+        try:
+            cand, inter = pair_counts(p, s.getArray(cm.POSITION))
+            mhz = (clocks or {}).get("sm_mhz") or 2070.0
+            peak_tf = 152 * 128 * 2 * mhz * 1e6 / 1e12
+            fp32 = {"candidates_per_particle": round(cand, 1), "neighbours_per_particle": round(inter, 1),
+                    "peak_tflops": round(peak_tf, 1),
+                    "peak_kind": "nominal: 152 SMs x 128 FP32 lanes x 2 flop x sampled SM clock"}
+            for k, per_pair in (("density", FLOPS_DENSITY_PAIR), ("force", FLOPS_FORCE_PAIR)):
+                fl = FLOPS_CANDIDATE * cand + per_pair * inter
+                tf = fl * n / (per_stage[k] / 1e3) / 1e12
+                fp32[k] = {"flops_per_particle": round(fl, 1), "achieved_tflops": round(tf, 3),
+                           "frac": round(tf / peak_tf, 4)}
+        except Exception as e:  # scipy missing: report the HBM roofline alone
+            fp32 = {"unavailable": str(e)[:120]}
+
     # ---- end-to-end through the public API with host buffers ----
     arrays = [cm.POSITION, cm.VELOCITY, cm.VELOCITYLEAPFROG]
     host = {a: torch.empty((n, 4), dtype=torch.float32, pin_memory=True).numpy() for a in arrays}
@@ -553,7 +629,7 @@ def main():
         "stage_ms": {k: round(v, 5) for k, v in per_stage.items()},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "bytes_per_particle": bytes_pp[dom]},
+                     "traffic": traffic, "bytes_per_particle": bytes_pp[dom], "fp32": fp32},
         "clocks": clocks,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
