@@ -214,9 +214,9 @@ int launch_groups(cmag_batch *b, bool force)
         if (force) {
             const bool per = lg.system == CMAG_PERISTALSIS;
             launch_force(rep, v, lg.g_force, b->spos, b->svel, b->aux, sorted_idx(b), b->off,
-                         per ? b->vforce : b->acc, per ? b->pforce : nullptr, b->phase, gs);
+                         per ? b->vforce : b->acc, per ? b->pforce : nullptr, b->phase, NeighborList{}, gs);
         } else {
-            launch_density(rep, v, lg.g_density, b->spos, b->off, b->meas, b->aux, gs);
+            launch_density(rep, v, lg.g_density, b->spos, b->off, b->meas, b->aux, NeighborList{}, gs);
         }
         if (g > 0) {
             CB_CUDA(b, cudaEventRecord(lg.done, gs));
@@ -1072,9 +1072,9 @@ int cmag_batch_autotune(cmag_batch *b, int32_t reps)
             int pick = pass == 0 ? g.g_density : g.g_force;
             for (int k = 0; k < 3; ++k) {
                 auto run = [&]() {
-                    if (pass == 0) launch_density(rep, v, lanes[k], b->spos, b->off, b->meas, b->aux, st);
+                    if (pass == 0) launch_density(rep, v, lanes[k], b->spos, b->off, b->meas, b->aux, NeighborList{}, st);
                     else launch_force(rep, v, lanes[k], b->spos, b->svel, b->aux, sorted_idx(b), b->off, fa, fb,
-                                      b->phase, st);
+                                      b->phase, NeighborList{}, st);
                 };
                 run();
                 cudaEventRecord(e0, st);
@@ -1087,7 +1087,7 @@ int cmag_batch_autotune(cmag_batch *b, int32_t reps)
             }
             if (pass == 0) {
                 g.g_density = pick;
-                launch_density(rep, v, pick, b->spos, b->off, b->meas, b->aux, st);
+                launch_density(rep, v, pick, b->spos, b->off, b->meas, b->aux, NeighborList{}, st);
             } else {
                 g.g_force = pick;
             }

@@ -1,0 +1,205 @@
+// density.cu -- the density pass over cell-ordered particles (with the equation
+// of state, and optionally the per-step interaction lists).
+//
+// Reference kernels (one thread per particle, 7^3 cell lookups each):
+//   calculateDamBreakDensityD fluid_kernel.cu:130-169 (+ sumDensity :99-128)
+//   calculatePoiseuilleDensityD poiseuilleFlowKernel.cu:141-182
+//   computeDensityVariationD PeristalsisDensity.cu:39-79
+//
+// The particles of each neighbour row are visited as runs of consecutive sorted
+// particles (neighbor_walk.cuh).  The pass also stores, per particle, p/rho^2 and
+// rho (DamBreak) or 1/rho (the others), so the force loop needs no division per
+// pair, and with interaction lists the neighbours the force loop will use.
+//
+// Every fused multiply-add is written out (__fmaf_rn and the paired forms); the
+// library is compiled with -fmad=false, so no other multiply and add are fused.
+// Results therefore do not depend on how the compiler schedules a particular
+// template variant: a scene gives the same bits alone and inside a batch.
+#include <cuda_runtime.h>
+
+#include "kernels.h"
+#include "neighbor_walk.cuh"
+
+namespace cmag {
+
+namespace {
+
+using walk::for_each_candidate;
+using walk::for_each_run;
+using walk::frac_cell;
+using walk::group_sum;
+using walk::interacts;
+using walk::list_append;
+using walk::rel;
+using walk::shift_code;
+
+// Un-normalised Wendland sum over candidates [b, e) of one run, two candidates
+// per step in paired FP32 (FFMA2/FMUL2/FADD2: two FP32 operations per issued
+// instruction on sm_100+), scalar tail.  Adds (1 - q/2)^4 (2q + 1) for q < 2.
+template <int SYS, bool TRIM, bool LIST>
+__device__ __forceinline__ void wendland_run(const DevParams &p, const float4 *__restrict__ spos,
+                                             uint32_t b, uint32_t e, float4 pi, float sx, float sy,
+                                             float sz, float2 &acc, bool record, uint32_t i,
+                                             const NeighborList &nl, uint32_t &cnt)
+{
+    const uint32_t code = LIST ? shift_code(sx, sy, sz) : 0u;
+    const float2 px = make_float2(pi.x, pi.x), py = make_float2(pi.y, pi.y),
+                 pz = make_float2(pi.z, pi.z);
+    const float2 m1 = make_float2(-1.0f, -1.0f), half = make_float2(-0.5f, -0.5f),
+                 one = make_float2(1.0f, 1.0f), two = make_float2(2.0f, 2.0f),
+                 ih = make_float2(p.inv_h, p.inv_h);
+    uint32_t j = b;
+    for (; j + 1 < e; j += 2) {
+        const float4 a = __ldg(spos + j), c = __ldg(spos + j + 1);
+        float2 ax = make_float2(a.x, c.x), ay = make_float2(a.y, c.y), az = make_float2(a.z, c.z);
+        if (SYS != CMAG_DAMBREAK) ax = __fadd2_rn(ax, make_float2(sx, sx));
+        if (SYS == CMAG_PERISTALSIS) {
+            ay = __fadd2_rn(ay, make_float2(sy, sy));
+            az = __fadd2_rn(az, make_float2(sz, sz));
+        }
+        const float2 rx = __ffma2_rn(ax, m1, px), ry = __ffma2_rn(ay, m1, py), rz = __ffma2_rn(az, m1, pz);
+        const float2 d2 = __ffma2_rn(rz, rz, __ffma2_rn(ry, ry, __fmul2_rn(rx, rx)));
+        const float2 rs = make_float2(rsqrtf(fmaxf(d2.x, 1e-30f)), rsqrtf(fmaxf(d2.y, 1e-30f)));
+        float2 q = __fmul2_rn(__fmul2_rn(d2, rs), ih);
+        q = make_float2(fminf(q.x, 2.0f), fminf(q.y, 2.0f));
+        const float2 t = __ffma2_rn(q, half, one);
+        const float2 t2 = __fmul2_rn(t, t);
+        float2 w = __fmul2_rn(__fmul2_rn(t2, t2), __ffma2_rn(q, two, one));
+        w.x = (d2.x < p.support2) ? w.x : 0.0f;
+        w.y = (d2.y < p.support2) ? w.y : 0.0f;
+        acc = __fadd2_rn(acc, w);
+        if (LIST && record) {
+            if (interacts<SYS, TRIM>(p, d2.x, a.w, j, i)) list_append(nl, i, cnt, j | code);
+            if (interacts<SYS, TRIM>(p, d2.y, c.w, j + 1, i)) list_append(nl, i, cnt, (j + 1) | code);
+        }
+    }
+    if (j < e) {  // the same operations as one half of a pair step
+        const float4 pj = __ldg(spos + j);
+        const float3 r = rel<SYS>(pi, pj, sx, sy, sz);
+        const float d2 = __fmaf_rn(r.z, r.z, __fmaf_rn(r.y, r.y, __fmul_rn(r.x, r.x)));
+        const float q = fminf(__fmul_rn(__fmul_rn(d2, rsqrtf(fmaxf(d2, 1e-30f))), p.inv_h), 2.0f);
+        const float t = __fmaf_rn(q, -0.5f, 1.0f), t2 = __fmul_rn(t, t);
+        const float w = __fmul_rn(__fmul_rn(t2, t2), __fmaf_rn(q, 2.0f, 1.0f));
+        acc.x = __fadd_rn(acc.x, (d2 < p.support2) ? w : 0.0f);
+        if (LIST && record && interacts<SYS, TRIM>(p, d2, pj.w, j, i)) list_append(nl, i, cnt, j | code);
+    }
+}
+
+// ---------------------------------------------------------------- density --
+// 256 threads, 6 blocks per SM: at most 42 registers, no spills
+template <int SYS, bool PLANAR, bool TRIM, int G, bool BATCH, bool LIST>
+__global__ void __launch_bounds__(256, 6)
+    k_density(DevParams pv, BatchView bv, const float4 *__restrict__ spos,
+              const uint32_t *__restrict__ off_all, float4 *__restrict__ meas,
+              float2 *__restrict__ aux, NeighborList nl)
+{
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t i = (BATCH ? bv.first : 0u) + t / G;
+    const int lane = (int)(t % G);
+    const bool active = t / G < (BATCH ? bv.count : pv.n);
+    // a batch reads its scene's parameters; the scene's cells start at table_base
+    const DevParams &p = BATCH ? bv.scenes[active ? bv.scene_of[i] : bv.scene_of[bv.first]] : pv;
+    const uint32_t *off = off_all + p.table_base;
+    const float4 pi = active ? spos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    // Poiseuille walls keep rest density (poiseuilleFlowKernel.cu:154-158)
+    const bool pinned = SYS == CMAG_POISEUILLE && pi.w == 1.0f;
+    // lists for every particle whose force is computed (DamBreak: fluid only)
+    const bool record = LIST && active && (SYS != CMAG_DAMBREAK || pi.w == (float)CMAG_FLUID);
+    uint32_t cnt = 0;
+    float sum = 0.0f;
+    if (active && (!pinned || record)) {  // a pinned wall walks only to record its list
+        const int3 g = grid_pos(p, pi.x, pi.y, pi.z);
+        if (p.kernel == CMAG_KERNEL_WENDLAND) {
+            float2 acc = make_float2(0.0f, 0.0f);
+            for_each_run<SYS, PLANAR, TRIM, G>(
+                p, off, lane, g, frac_cell(p, pi),
+                [&](uint32_t b, uint32_t e, float sx, float sy, float sz) {
+                    wendland_run<SYS, TRIM, LIST>(p, spos, b, e, pi, sx, sy, sz, acc, record, i, nl, cnt);
+                });
+            sum = p.w_norm * (acc.x + acc.y);
+        } else {
+            for_each_candidate<SYS, PLANAR, TRIM, G>(
+                p, off, lane, g, frac_cell(p, pi), [&](uint32_t j, float sx, float sy, float sz) {
+                    const float4 pj = __ldg(spos + j);
+                    const float3 r = rel<SYS>(pi, pj, sx, sy, sz);
+                    const float d2 = __fmaf_rn(r.z, r.z, __fmaf_rn(r.y, r.y, __fmul_rn(r.x, r.x)));
+                    // evaluated for every candidate and selected: no divergent branch
+                    const float w = kernel_w(p, fminf(d2 * rsqrtf(fmaxf(d2, 1e-30f)) * p.inv_h, 2.0f));
+                    sum += (d2 < p.support2) ? w : 0.0f;
+                    if (LIST && record && interacts<SYS, TRIM>(p, d2, pj.w, j, i))
+                        list_append(nl, i, cnt, j | shift_code(sx, sy, sz));
+                });
+        }
+    }
+    if (LIST && active) nl.count[i] = cnt;
+    sum = group_sum<G>(sum);
+    if (active && lane == 0) {
+        float rho, pr;
+        if (pinned) {
+            rho = p.rho0;
+            pr = p.p_wall;
+        } else {
+            rho = sum * p.mass;
+            pr = eos_pressure(p, rho);
+        }
+        meas[i] = make_float4(rho, pr, 0.0f, SYS == CMAG_PERISTALSIS ? pi.w : 0.0f);
+        const float inv_rho = 1.0f / rho;
+        aux[i] = make_float2(pr * inv_rho * inv_rho, SYS == CMAG_DAMBREAK ? rho : inv_rho);
+    }
+}
+
+template <int SYS, bool PLANAR, bool TRIM, int G, bool LIST>
+void launch_d(const DevParams &p, const BatchView &bv, const float4 *spos, const uint32_t *off,
+              float4 *meas, float2 *aux, const NeighborList &nl, cudaStream_t st)
+{
+    const uint64_t threads = (uint64_t)(bv.scenes ? bv.count : p.n) * G;
+    const uint32_t blocks = (uint32_t)((threads + 255) / 256);
+    if (bv.scenes)
+        k_density<SYS, PLANAR, TRIM, G, true, LIST><<<blocks, 256, 0, st>>>(p, bv, spos, off, meas, aux, nl);
+    else
+        k_density<SYS, PLANAR, TRIM, G, false, LIST><<<blocks, 256, 0, st>>>(p, bv, spos, off, meas, aux, nl);
+}
+
+template <int SYS, bool PLANAR, bool TRIM>
+void dispatch_g(int group, const DevParams &p, const BatchView &bv, const float4 *spos,
+                const uint32_t *off, float4 *meas, float2 *aux, const NeighborList &nl, cudaStream_t st)
+{
+    if (nl.entry) {  // lists: one lane per particle
+        launch_d<SYS, PLANAR, TRIM, 1, true>(p, bv, spos, off, meas, aux, nl, st);
+        return;
+    }
+    switch (group) {
+    case 2: launch_d<SYS, PLANAR, TRIM, 2, false>(p, bv, spos, off, meas, aux, nl, st); break;
+    case 4: launch_d<SYS, PLANAR, TRIM, 4, false>(p, bv, spos, off, meas, aux, nl, st); break;
+    default: launch_d<SYS, PLANAR, TRIM, 1, false>(p, bv, spos, off, meas, aux, nl, st); break;
+    }
+}
+
+template <int SYS>
+void dispatch(int group, const DevParams &p, const BatchView &bv, const float4 *spos,
+              const uint32_t *off, float4 *meas, float2 *aux, const NeighborList &nl, cudaStream_t st)
+{
+    if (p.planar) {
+        if (p.trim) dispatch_g<SYS, true, true>(group, p, bv, spos, off, meas, aux, nl, st);
+        else dispatch_g<SYS, true, false>(group, p, bv, spos, off, meas, aux, nl, st);
+    } else {
+        if (p.trim) dispatch_g<SYS, false, true>(group, p, bv, spos, off, meas, aux, nl, st);
+        else dispatch_g<SYS, false, false>(group, p, bv, spos, off, meas, aux, nl, st);
+    }
+}
+
+}  // namespace
+
+// p: the scene's parameters, or for a batch launch group the parameters of any
+// scene of the group (family, planar and trim select the kernel variant)
+void launch_density(const DevParams &p, const BatchView &bv, int group, const float4 *spos,
+                    const uint32_t *off, float4 *meas, float2 *aux, const NeighborList &nl,
+                    cudaStream_t st)
+{
+    if ((bv.scenes ? bv.count : p.n) == 0) return;
+    if (p.system == CMAG_DAMBREAK) dispatch<CMAG_DAMBREAK>(group, p, bv, spos, off, meas, aux, nl, st);
+    else if (p.system == CMAG_POISEUILLE) dispatch<CMAG_POISEUILLE>(group, p, bv, spos, off, meas, aux, nl, st);
+    else dispatch<CMAG_PERISTALSIS>(group, p, bv, spos, off, meas, aux, nl, st);
+}
+
+}  // namespace cmag

@@ -1,26 +1,15 @@
-// neighbors.cu -- density and force neighbour loops over cell-ordered particles.
+// force.cu -- the force pass over cell-ordered particles.
 //
 // Reference kernels (one thread per particle, 7^3 cell lookups each):
-//   density  calculateDamBreakDensityD fluid_kernel.cu:130-169 (+ sumDensity :99-128)
-//            calculatePoiseuilleDensityD poiseuilleFlowKernel.cu:141-182
-//            computeDensityVariationD PeristalsisDensity.cu:39-79
-//   force    calcAndApplyAccelerationD fluid_kernel.cu:245-292 (+ :172-243)
-//            calculatePoiseuilleAccelerationD poiseuilleFlowKernel.cu:267-309 (+ :184-265)
-//            computeViscousForceD + computePressureForceD
-//            PeristalsisViscousForce.cu:198-242, PeristalsisPressureForce.cu:51-91
+//   calcAndApplyAccelerationD fluid_kernel.cu:245-292 (+ :172-243)
+//   calculatePoiseuilleAccelerationD poiseuilleFlowKernel.cu:267-309 (+ :184-265)
+//   computeViscousForceD + computePressureForceD
+//   PeristalsisViscousForce.cu:198-242, PeristalsisPressureForce.cu:51-91
 //
-// The particles of each neighbour row are visited as runs of consecutive sorted
-// particles (neighbor_walk.cuh: lanes per particle, periodic image shifts, runs
-// trimmed to the support circle when every interaction vanishes beyond q = 2,
-// which holds for all families except the reference DamBreak wall force).  Partial
-// sums of a particle's lanes meet in a shuffle reduction.  The density kernel also stores, per particle,
-// p/rho^2 and rho (DamBreak) or 1/rho (the others), so the force loop needs no
-// division per pair.
-//
-// Every fused multiply-add is written out (__fmaf_rn and the paired forms); the
-// library is compiled with -fmad=false, so no other multiply and add are fused.
-// Results therefore do not depend on how the compiler schedules a particular
-// template variant: a scene gives the same bits alone and inside a batch.
+// Each particle either walks its neighbour cells as runs of consecutive sorted
+// particles (neighbor_walk.cuh; lanes per particle split the rows) or reads the
+// interaction list the density pass recorded (the same pairs in the same order).
+// Fused multiply-adds are written out (the library is compiled with -fmad=false).
 #include <cuda_runtime.h>
 
 #include "kernels.h"
@@ -31,118 +20,9 @@ namespace cmag {
 namespace {
 
 using walk::for_each_candidate;
-using walk::for_each_run;
 using walk::frac_cell;
+using walk::group_sum;
 using walk::rel;
-
-// Un-normalised Wendland sum over candidates [b, e) of one run, two candidates
-// per step in paired FP32 (FFMA2/FMUL2/FADD2: two FP32 operations per issued
-// instruction on sm_100+), scalar tail.  Adds (1 - q/2)^4 (2q + 1) for q < 2.
-template <int SYS>
-__device__ __forceinline__ void wendland_run(const DevParams &p, const float4 *__restrict__ spos,
-                                             uint32_t b, uint32_t e, float4 pi, float sx, float sy,
-                                             float sz, float2 &acc)
-{
-    const float2 px = make_float2(pi.x, pi.x), py = make_float2(pi.y, pi.y),
-                 pz = make_float2(pi.z, pi.z);
-    const float2 m1 = make_float2(-1.0f, -1.0f), half = make_float2(-0.5f, -0.5f),
-                 one = make_float2(1.0f, 1.0f), two = make_float2(2.0f, 2.0f),
-                 ih = make_float2(p.inv_h, p.inv_h);
-    uint32_t j = b;
-    for (; j + 1 < e; j += 2) {
-        const float4 a = __ldg(spos + j), c = __ldg(spos + j + 1);
-        float2 ax = make_float2(a.x, c.x), ay = make_float2(a.y, c.y), az = make_float2(a.z, c.z);
-        if (SYS != CMAG_DAMBREAK) ax = __fadd2_rn(ax, make_float2(sx, sx));
-        if (SYS == CMAG_PERISTALSIS) {
-            ay = __fadd2_rn(ay, make_float2(sy, sy));
-            az = __fadd2_rn(az, make_float2(sz, sz));
-        }
-        const float2 rx = __ffma2_rn(ax, m1, px), ry = __ffma2_rn(ay, m1, py), rz = __ffma2_rn(az, m1, pz);
-        const float2 d2 = __ffma2_rn(rz, rz, __ffma2_rn(ry, ry, __fmul2_rn(rx, rx)));
-        const float2 rs = make_float2(rsqrtf(fmaxf(d2.x, 1e-30f)), rsqrtf(fmaxf(d2.y, 1e-30f)));
-        float2 q = __fmul2_rn(__fmul2_rn(d2, rs), ih);
-        q = make_float2(fminf(q.x, 2.0f), fminf(q.y, 2.0f));
-        const float2 t = __ffma2_rn(q, half, one);
-        const float2 t2 = __fmul2_rn(t, t);
-        float2 w = __fmul2_rn(__fmul2_rn(t2, t2), __ffma2_rn(q, two, one));
-        w.x = (d2.x < p.support2) ? w.x : 0.0f;
-        w.y = (d2.y < p.support2) ? w.y : 0.0f;
-        acc = __fadd2_rn(acc, w);
-    }
-    if (j < e) {  // the same operations as one half of a pair step
-        const float3 r = rel<SYS>(pi, __ldg(spos + j), sx, sy, sz);
-        const float d2 = __fmaf_rn(r.z, r.z, __fmaf_rn(r.y, r.y, __fmul_rn(r.x, r.x)));
-        const float q = fminf(__fmul_rn(__fmul_rn(d2, rsqrtf(fmaxf(d2, 1e-30f))), p.inv_h), 2.0f);
-        const float t = __fmaf_rn(q, -0.5f, 1.0f), t2 = __fmul_rn(t, t);
-        const float w = __fmul_rn(__fmul_rn(t2, t2), __fmaf_rn(q, 2.0f, 1.0f));
-        acc.x = __fadd_rn(acc.x, (d2 < p.support2) ? w : 0.0f);
-    }
-}
-
-template <int G>
-__device__ __forceinline__ float group_sum(float v)
-{
-#pragma unroll
-    for (int o = G / 2; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o, G);
-    return v;
-}
-
-
-// ---------------------------------------------------------------- density --
-// 256 threads, 6 blocks per SM: at most 42 registers, no spills
-template <int SYS, bool PLANAR, bool TRIM, int G, bool BATCH>
-__global__ void __launch_bounds__(256, 6)
-    k_density(DevParams pv, BatchView bv, const float4 *__restrict__ spos,
-              const uint32_t *__restrict__ off_all, float4 *__restrict__ meas,
-              float2 *__restrict__ aux)
-{
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t i = (BATCH ? bv.first : 0u) + t / G;
-    const int lane = (int)(t % G);
-    const bool active = t / G < (BATCH ? bv.count : pv.n);
-    // a batch reads its scene's parameters; the scene's cells start at table_base
-    const DevParams &p = BATCH ? bv.scenes[active ? bv.scene_of[i] : bv.scene_of[bv.first]] : pv;
-    const uint32_t *off = off_all + p.table_base;
-    const float4 pi = active ? spos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-    // Poiseuille walls keep rest density (poiseuilleFlowKernel.cu:154-158)
-    const bool pinned = SYS == CMAG_POISEUILLE && pi.w == 1.0f;
-    float sum = 0.0f;
-    if (active && !pinned) {
-        const int3 g = grid_pos(p, pi.x, pi.y, pi.z);
-        if (p.kernel == CMAG_KERNEL_WENDLAND) {
-            float2 acc = make_float2(0.0f, 0.0f);
-            for_each_run<SYS, PLANAR, TRIM, G>(
-                p, off, lane, g, frac_cell(p, pi),
-                [&](uint32_t b, uint32_t e, float sx, float sy, float sz) {
-                    wendland_run<SYS>(p, spos, b, e, pi, sx, sy, sz, acc);
-                });
-            sum = p.w_norm * (acc.x + acc.y);
-        } else {
-            for_each_candidate<SYS, PLANAR, TRIM, G>(
-                p, off, lane, g, frac_cell(p, pi), [&](uint32_t j, float sx, float sy, float sz) {
-                    const float3 r = rel<SYS>(pi, __ldg(spos + j), sx, sy, sz);
-                    const float d2 = __fmaf_rn(r.z, r.z, __fmaf_rn(r.y, r.y, __fmul_rn(r.x, r.x)));
-                    // evaluated for every candidate and selected: no divergent branch
-                    const float w = kernel_w(p, fminf(d2 * rsqrtf(fmaxf(d2, 1e-30f)) * p.inv_h, 2.0f));
-                    sum += (d2 < p.support2) ? w : 0.0f;
-                });
-        }
-    }
-    sum = group_sum<G>(sum);
-    if (active && lane == 0) {
-        float rho, pr;
-        if (pinned) {
-            rho = p.rho0;
-            pr = p.p_wall;
-        } else {
-            rho = sum * p.mass;
-            pr = eos_pressure(p, rho);
-        }
-        meas[i] = make_float4(rho, pr, 0.0f, SYS == CMAG_PERISTALSIS ? pi.w : 0.0f);
-        const float inv_rho = 1.0f / rho;
-        aux[i] = make_float2(pr * inv_rho * inv_rho, SYS == CMAG_DAMBREAK ? rho : inv_rho);
-    }
-}
 
 // ---------------------------------------------- no-slip into moving walls --
 // The closest point (xa, ya) of one Peristalsis wall interface
@@ -192,13 +72,13 @@ __device__ __forceinline__ WallSide wall_side(const DevParams &p, float amp, flo
 
 // ------------------------------------------------------------------ force --
 // 256 threads, 4 blocks per SM: at most 64 registers
-template <int SYS, bool PLANAR, bool TRIM, int G, bool BATCH>
+template <int SYS, bool PLANAR, bool TRIM, int G, bool BATCH, bool LIST>
 __global__ void __launch_bounds__(256, 4)
     k_force(DevParams pv, BatchView bv, const float4 *__restrict__ spos,
             const float4 *__restrict__ svel, const float2 *__restrict__ aux,
             const uint32_t *__restrict__ idx, const uint32_t *__restrict__ off_all,
             float4 *__restrict__ out_a, float4 *__restrict__ out_b,
-            const PhaseState *__restrict__ ph_all)
+            const PhaseState *__restrict__ ph_all, NeighborList nl)
 {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t i = (BATCH ? bv.first : 0u) + t / G;
@@ -226,10 +106,8 @@ __global__ void __launch_bounds__(256, 4)
             wb = wall_side(p, amp, tw, !ph.is_bc, 1.0f, -p.half_fluid_h, pi.x, pi.y);
             wt = wall_side(p, amp, tw, !ph.is_bc, -1.0f, p.half_fluid_h, pi.x, pi.y);
         }
-        for_each_candidate<SYS, PLANAR, TRIM, G>(
-            p, off, lane, g, frac_cell(p, pi), [&](uint32_t j, float sx, float sy, float sz) {
+        auto pair = [&](uint32_t j, const float4 &pj, float sx, float sy, float sz) {
                 if (j == i) return;
-                const float4 pj = __ldg(spos + j);
                 const float3 rv = rel<SYS>(pi, pj, sx, sy, sz);
                 const float rx = rv.x, ry = rv.y, rz = rv.z;
                 const float d2 = __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, rx * rx));
@@ -309,7 +187,30 @@ __global__ void __launch_bounds__(256, 4)
                     const float sp = -p.mass * temp * (pterm + aj.x) * inv_d;
                     bx = __fmaf_rn(sp, rx, bx); by = __fmaf_rn(sp, ry, by); bz = __fmaf_rn(sp, rz, bz);
                 }
-            });
+            };
+        const uint32_t cnt = LIST ? __ldg(nl.count + i) : 0u;
+        if (LIST && cnt <= nl.cap) {
+            // the density pass's list: the walk's interacting candidates, same order
+#pragma unroll 2
+            for (uint32_t k = 0; k < cnt; ++k) {
+                const uint32_t en = __ldg(nl.entry + (size_t)k * nl.stride + i);
+                float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+                if (SYS != CMAG_DAMBREAK) {
+                    const uint32_t cd = en >> kListIndexBits;
+                    sx = (float)((int)(cd & 3u) - 1) * p.wsx;
+                    if (SYS == CMAG_PERISTALSIS) {
+                        sy = (float)((int)((cd >> 2) & 3u) - 1) * p.wsy;
+                        sz = (float)((int)((cd >> 4) & 3u) - 1) * p.wsz;
+                    }
+                }
+                const uint32_t j = en & kListIndexMask;
+                pair(j, __ldg(spos + j), sx, sy, sz);
+            }
+        } else {
+            for_each_candidate<SYS, PLANAR, TRIM, G>(
+                p, off, lane, g, frac_cell(p, pi),
+                [&](uint32_t j, float sx, float sy, float sz) { pair(j, __ldg(spos + j), sx, sy, sz); });
+        }
     }
     if (G > 1) {
         ax = group_sum<G>(ax); ay = group_sum<G>(ay); az = group_sum<G>(az);
@@ -325,48 +226,42 @@ __global__ void __launch_bounds__(256, 4)
     }
 }
 
-template <int SYS, bool PLANAR, bool TRIM, int G>
-void launch_pair(bool force, const DevParams &p, const BatchView &bv, const float4 *spos,
-                 const float4 *svel, float4 *meas, float2 *aux, const uint32_t *idx,
-                 const uint32_t *off, float4 *a, float4 *b, const PhaseState *ph, cudaStream_t st)
-{
-    const uint64_t threads = (uint64_t)(bv.scenes ? bv.count : p.n) * G;
-    const uint32_t blocks = (uint32_t)((threads + 255) / 256);
-    if (bv.scenes) {
-        if (force)
-            k_force<SYS, PLANAR, TRIM, G, true><<<blocks, 256, 0, st>>>(p, bv, spos, svel, aux, idx, off, a, b, ph);
-        else
-            k_density<SYS, PLANAR, TRIM, G, true><<<blocks, 256, 0, st>>>(p, bv, spos, off, meas, aux);
-    } else {
-        if (force)
-            k_force<SYS, PLANAR, TRIM, G, false><<<blocks, 256, 0, st>>>(p, bv, spos, svel, aux, idx, off, a, b, ph);
-        else
-            k_density<SYS, PLANAR, TRIM, G, false><<<blocks, 256, 0, st>>>(p, bv, spos, off, meas, aux);
-    }
-}
-
-struct PairArgs {
-    bool force;
+struct ForceArgs {
     const float4 *spos, *svel;
-    float4 *meas;
-    float2 *aux;
+    const float2 *aux;
     const uint32_t *idx, *off;
     float4 *a, *b;
     const PhaseState *ph;
+    NeighborList nl;
 };
 
-template <int SYS, bool PLANAR, bool TRIM>
-void dispatch_g(int group, const DevParams &p, const BatchView &bv, const PairArgs &x, cudaStream_t st)
+template <int SYS, bool PLANAR, bool TRIM, int G, bool LIST>
+void launch_f(const DevParams &p, const BatchView &bv, const ForceArgs &x, cudaStream_t st)
 {
+    const uint64_t threads = (uint64_t)(bv.scenes ? bv.count : p.n) * G;
+    const uint32_t blocks = (uint32_t)((threads + 255) / 256);
+    if (bv.scenes)
+        k_force<SYS, PLANAR, TRIM, G, true, LIST><<<blocks, 256, 0, st>>>(p, bv, x.spos, x.svel, x.aux, x.idx, x.off, x.a, x.b, x.ph, x.nl);
+    else
+        k_force<SYS, PLANAR, TRIM, G, false, LIST><<<blocks, 256, 0, st>>>(p, bv, x.spos, x.svel, x.aux, x.idx, x.off, x.a, x.b, x.ph, x.nl);
+}
+
+template <int SYS, bool PLANAR, bool TRIM>
+void dispatch_g(int group, const DevParams &p, const BatchView &bv, const ForceArgs &x, cudaStream_t st)
+{
+    if (x.nl.entry) {  // lists: one lane per particle
+        launch_f<SYS, PLANAR, TRIM, 1, true>(p, bv, x, st);
+        return;
+    }
     switch (group) {
-    case 2: launch_pair<SYS, PLANAR, TRIM, 2>(x.force, p, bv, x.spos, x.svel, x.meas, x.aux, x.idx, x.off, x.a, x.b, x.ph, st); break;
-    case 4: launch_pair<SYS, PLANAR, TRIM, 4>(x.force, p, bv, x.spos, x.svel, x.meas, x.aux, x.idx, x.off, x.a, x.b, x.ph, st); break;
-    default: launch_pair<SYS, PLANAR, TRIM, 1>(x.force, p, bv, x.spos, x.svel, x.meas, x.aux, x.idx, x.off, x.a, x.b, x.ph, st); break;
+    case 2: launch_f<SYS, PLANAR, TRIM, 2, false>(p, bv, x, st); break;
+    case 4: launch_f<SYS, PLANAR, TRIM, 4, false>(p, bv, x, st); break;
+    default: launch_f<SYS, PLANAR, TRIM, 1, false>(p, bv, x, st); break;
     }
 }
 
 template <int SYS>
-void dispatch(int group, const DevParams &p, const BatchView &bv, const PairArgs &x, cudaStream_t st)
+void dispatch(int group, const DevParams &p, const BatchView &bv, const ForceArgs &x, cudaStream_t st)
 {
     if (p.planar) {
         if (p.trim) dispatch_g<SYS, true, true>(group, p, bv, x, st);
@@ -377,31 +272,18 @@ void dispatch(int group, const DevParams &p, const BatchView &bv, const PairArgs
     }
 }
 
-// p: the scene's parameters, or for a batch launch group the parameters of any
-// scene of the group (family, planar and trim select the kernel variant)
-void dispatch_sys(int group, const DevParams &p, const BatchView &bv, const PairArgs &x,
-                  cudaStream_t st)
-{
-    if ((bv.scenes ? bv.count : p.n) == 0) return;
-    if (p.system == CMAG_DAMBREAK) dispatch<CMAG_DAMBREAK>(group, p, bv, x, st);
-    else if (p.system == CMAG_POISEUILLE) dispatch<CMAG_POISEUILLE>(group, p, bv, x, st);
-    else dispatch<CMAG_PERISTALSIS>(group, p, bv, x, st);
-}
-
 }  // namespace
-
-void launch_density(const DevParams &p, const BatchView &bv, int group, const float4 *spos,
-                    const uint32_t *off, float4 *meas, float2 *aux, cudaStream_t st)
-{
-    dispatch_sys(group, p, bv, PairArgs{false, spos, nullptr, meas, aux, nullptr, off, nullptr, nullptr, nullptr}, st);
-}
 
 void launch_force(const DevParams &p, const BatchView &bv, int group, const float4 *spos,
                   const float4 *svel, const float2 *aux, const uint32_t *idx, const uint32_t *off,
-                  float4 *out_a, float4 *out_b, const PhaseState *ph, cudaStream_t st)
+                  float4 *out_a, float4 *out_b, const PhaseState *ph, const NeighborList &nl,
+                  cudaStream_t st)
 {
-    dispatch_sys(group, p, bv,
-                 PairArgs{true, spos, svel, nullptr, const_cast<float2 *>(aux), idx, off, out_a, out_b, ph}, st);
+    if ((bv.scenes ? bv.count : p.n) == 0) return;
+    const ForceArgs x{spos, svel, aux, idx, off, out_a, out_b, ph, nl};
+    if (p.system == CMAG_DAMBREAK) dispatch<CMAG_DAMBREAK>(group, p, bv, x, st);
+    else if (p.system == CMAG_POISEUILLE) dispatch<CMAG_POISEUILLE>(group, p, bv, x, st);
+    else dispatch<CMAG_PERISTALSIS>(group, p, bv, x, st);
 }
 
 }  // namespace cmag

@@ -57,16 +57,20 @@ void launch_reorder(const uint32_t *idx, const float4 *pos, const float4 *vlf, f
 void launch_cell_view(const uint32_t *off, uint32_t scan_base, uint32_t scan_cells,
                       uint64_t ncells, uint32_t *cell_start, uint32_t *cell_end, cudaStream_t st);
 
-// ---- neighbour loops (neighbors.cu) ----------------------------------------
+// ---- neighbour loops (density.cu, force.cu) ---------------------------------
 // density also writes aux[i] = (p/rho^2, rho) (DamBreak) or (p/rho^2, 1/rho).
 // bv empty: one scene with parameters p; otherwise one launch group of a batch
 // (p = the parameters of any of the group's scenes).
+// nl (entry != nullptr): density records the interaction lists, force reads them
+// (both with one lane per particle; group is then ignored)
 void launch_density(const DevParams &p, const BatchView &bv, int group, const float4 *spos,
-                    const uint32_t *off, float4 *meas, float2 *aux, cudaStream_t st);
+                    const uint32_t *off, float4 *meas, float2 *aux, const NeighborList &nl,
+                    cudaStream_t st);
 // ph: the Peristalsis phase (one per scene in a batch; read with wall_noslip only)
 void launch_force(const DevParams &p, const BatchView &bv, int group, const float4 *spos,
                   const float4 *svel, const float2 *aux, const uint32_t *idx, const uint32_t *off,
-                  float4 *out_a, float4 *out_b, const PhaseState *ph, cudaStream_t st);
+                  float4 *out_a, float4 *out_b, const PhaseState *ph, const NeighborList &nl,
+                  cudaStream_t st);
 
 // ---- integration and wall motion (integrate.cu) ------------------------------
 // bv empty: one scene; otherwise every particle of the batch with its scene's

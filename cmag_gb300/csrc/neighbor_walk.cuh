@@ -1,6 +1,6 @@
 // neighbor_walk.cuh -- the walk over a particle's neighbour cells as runs of
 // consecutive sorted particles, shared by the density/force loops
-// (neighbors.cu) and the learned closure's feature loop (closure.cu).
+// (density.cu, force.cu) and the learned closure's feature loop (closure.cu).
 //
 // The (2c+1)^2 rows of the cell box (only the particle's own z layer for planar
 // 2-D scenes) are walked as runs of consecutive cells: a run's particles are one
@@ -148,6 +148,42 @@ __device__ __forceinline__ float3 rel(float4 pi, float4 pj, float sx, float sy, 
 __device__ __forceinline__ float3 frac_cell(const DevParams &p, float4 q)
 {
     return make_float3((q.x - p.ox) * p.inv_csx, (q.y - p.oy) * p.inv_csy, (q.z - p.oz) * p.inv_csz);
+}
+
+
+// ---- pieces shared by the density and force loops --------------------------
+
+// Whether the force loop of particle i uses candidate j at squared distance d2
+// (type w): inside the support, or a DamBreak wall without the q < 2 cut-off.
+template <int SYS, bool TRIM>
+__device__ __forceinline__ bool interacts(const DevParams &p, float d2, float w, uint32_t j, uint32_t i)
+{
+    const bool far_wall = SYS == CMAG_DAMBREAK && !TRIM && w != (float)CMAG_FLUID;
+    return j != i && d2 > 0.0f && (d2 < p.support2 || far_wall);
+}
+
+// list entry code of a run's image shift: 2 bits per axis, 0/1/2 for -1/0/+1
+__device__ __forceinline__ uint32_t shift_code(float sx, float sy, float sz)
+{
+    const uint32_t cx = sx > 0.0f ? 2u : (sx < 0.0f ? 0u : 1u);
+    const uint32_t cy = sy > 0.0f ? 2u : (sy < 0.0f ? 0u : 1u);
+    const uint32_t cz = sz > 0.0f ? 2u : (sz < 0.0f ? 0u : 1u);
+    return (cx | (cy << 2) | (cz << 4)) << kListIndexBits;
+}
+
+__device__ __forceinline__ void list_append(const NeighborList &nl, uint32_t i, uint32_t &cnt,
+                                            uint32_t value)
+{
+    if (cnt < nl.cap) nl.entry[(size_t)cnt * nl.stride + i] = value;
+    ++cnt;
+}
+
+template <int G>
+__device__ __forceinline__ float group_sum(float v)
+{
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o, G);
+    return v;
 }
 
 }  // namespace walk

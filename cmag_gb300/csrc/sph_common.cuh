@@ -71,6 +71,22 @@ struct BatchView {
     uint32_t first, count;
 };
 
+// Per-step interaction lists: the density pass records, for every particle whose
+// force is computed, the sorted indices of the neighbours its force loop will use
+// (entry k of particle i at entry[k * stride + i], so a warp's k-th entries are
+// contiguous), in the walk's order, with the periodic image shift of each
+// (2 bits per axis above bit 26); the force pass reads them instead of walking the
+// cells again.  A particle with more than cap neighbours keeps count > cap and its
+// force loop walks the cells.  Empty (entry == nullptr): no lists.
+struct NeighborList {
+    uint32_t *entry;
+    uint32_t *count;
+    uint32_t cap;
+    uint32_t stride;
+};
+constexpr uint32_t kListIndexBits = 26;
+constexpr uint32_t kListIndexMask = (1u << kListIndexBits) - 1u;
+
 // Device-resident per-step scalars of the Peristalsis phase machine
 // (PeristalsisSystem.cpp:330-343), advanced on the device so that a captured
 // step can be replayed without host involvement.

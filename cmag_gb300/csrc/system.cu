@@ -59,6 +59,8 @@ struct cmag_system {
     int last_stage = CMAG_STAGE_INTEGRATE;
 
     int g_density = 1, g_force = 1;  // lanes per particle (cmag_system_autotune)
+    uint32_t *nl_entry = nullptr, *nl_count = nullptr;  // interaction lists (when enabled)
+    uint32_t nl_cap = 0;
     cmag_closure *closure = nullptr;   // learned correction added after the force stage
     __nv_bfloat16 *closure_x = nullptr;  // its normalised input rows (n x 16)
 
@@ -267,6 +269,61 @@ SceneLayout layout_of(const cmag_system *s)
 
 DevParams make_dev(const cmag_system *s) { return make_dev_params(s->p, s->n, layout_of(s)); }
 
+NeighborList nl_of(const cmag_system *s)
+{
+    NeighborList nl{};
+    if (s->nl_entry) {
+        nl.entry = s->nl_entry;
+        nl.count = s->nl_count;
+        nl.cap = s->nl_cap;
+        nl.stride = s->n;
+    }
+    return nl;
+}
+
+// Room per particle in the interaction lists: 1.5 times the lattice neighbour
+// count inside the support (or, with the un-cut DamBreak wall force, every
+// particle of the searched cell box) plus 32.  Particles beyond it walk the cells.
+uint32_t list_cap(const cmag_sph_params &p, bool trim)
+{
+    const double dx = 2.0 * p.particle_radius, s = 2.0 * p.smoothing_radius / dx;
+    const bool planar = p.dims == 2;
+    double expected = planar ? kPi * s * s : 4.0 / 3.0 * kPi * s * s * s;
+    if (!trim) {
+        const double c = 2 * p.cell_count + 1, per = p.cell_size[0] / dx;
+        expected = planar ? c * c * per * per : c * c * c * per * per * per;
+    }
+    return (uint32_t)std::ceil(1.5 * expected) + 32u;
+}
+
+int free_lists(cmag_system *s)
+{
+    if (s->nl_entry) cudaFree(s->nl_entry);
+    if (s->nl_count) cudaFree(s->nl_count);
+    s->nl_entry = s->nl_count = nullptr;
+    s->nl_cap = 0;
+    return CMAG_OK;
+}
+
+int alloc_lists(cmag_system *s, uint32_t cap = 0)
+{
+    if (s->nl_entry && (cap == 0 || cap == s->nl_cap)) return CMAG_OK;
+    free_lists(s);
+    if (s->n >= (1u << kListIndexBits))
+        return fail(s, CMAG_ERR_INVALID, "interaction lists need fewer than 2^26 particles");
+    if (cap == 0) cap = list_cap(s->p, make_dev(s).trim != 0);
+    cudaError_t e = cudaMalloc((void **)&s->nl_entry, sizeof(uint32_t) * (size_t)cap * s->n);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&s->nl_count, sizeof(uint32_t) * (size_t)s->n);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        free_lists(s);
+        return fail(s, e == cudaErrorMemoryAllocation ? CMAG_ERR_NOMEM : CMAG_ERR_CUDA,
+                    std::string("interaction lists: ") + cudaGetErrorString(e));
+    }
+    s->nl_cap = cap;
+    return CMAG_OK;
+}
+
 void invalidate_graph(cmag_system *s)
 {
     if (s->gexec) cudaGraphExecDestroy(s->gexec);
@@ -337,15 +394,15 @@ int record_step(cmag_system *s, int last, bool timed)
         launch_reorder(sorted_idx(s), s->pos, s->vlf, s->spos, s->svel, s->n, st);
     mark(3);
     if (last >= CMAG_STAGE_DENSITY)
-        launch_density(d, BatchView{}, s->g_density, s->spos, s->off, s->meas, s->aux, st);
+        launch_density(d, BatchView{}, s->g_density, s->spos, s->off, s->meas, s->aux, nl_of(s), st);
     mark(4);
     if (last >= CMAG_STAGE_FORCE) {
         if (p.system == CMAG_PERISTALSIS)
             launch_force(d, BatchView{}, s->g_force, s->spos, s->svel, s->aux, sorted_idx(s), s->off,
-                         s->vforce, s->pforce, s->phase, st);
+                         s->vforce, s->pforce, s->phase, nl_of(s), st);
         else
             launch_force(d, BatchView{}, s->g_force, s->spos, s->svel, s->aux, sorted_idx(s), s->off, s->acc,
-                         nullptr, s->phase, st);
+                         nullptr, s->phase, nl_of(s), st);
         if (s->closure)
             launch_closure_apply(d, s->closure->view(), s->spos, s->svel, s->aux, s->meas,
                                  sorted_idx(s), s->off, s->acc, s->closure_x, st);
@@ -459,6 +516,7 @@ void free_all(cmag_system *s)
                     s->closure_x};
     for (void *p : ptrs)
         if (p) cudaFree(p);
+    free_lists(s);
     if (s->own_stream) cudaStreamDestroy(s->own_stream);
 }
 
@@ -1110,35 +1168,50 @@ int cmag_system_autotune(cmag_system *s, int32_t reps)
     cudaEvent_t a, b;
     CM_CUDA(s, cudaEventCreate(&a));
     CM_CUDA(s, cudaEventCreate(&b));
+    auto timed = [&](auto &&launch) {
+        launch();  // warm
+        cudaEventRecord(a, st);
+        for (int r = 0; r < reps; ++r) launch();
+        cudaEventRecord(b, st);
+        cudaEventSynchronize(b);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, a, b);
+        return ms;
+    };
+    const bool had_lists = s->nl_entry != nullptr;
+    free_lists(s);
+    const NeighborList none{};
     const int groups[3] = {1, 2, 4};
     float best_d = 1e30f, best_f = 1e30f;
     int gd = s->g_density, gf = s->g_force;
     float4 *fa = s->p.system == CMAG_PERISTALSIS ? s->vforce : s->acc;
     float4 *fb = s->p.system == CMAG_PERISTALSIS ? s->pforce : nullptr;
     for (int k = 0; k < 3; ++k) {
-        launch_density(d, BatchView{}, groups[k], s->spos, s->off, s->meas, s->aux, st);  // warm
-        cudaEventRecord(a, st);
-        for (int r = 0; r < reps; ++r) launch_density(d, BatchView{}, groups[k], s->spos, s->off, s->meas, s->aux, st);
-        cudaEventRecord(b, st);
-        cudaEventSynchronize(b);
-        float ms = 0;
-        cudaEventElapsedTime(&ms, a, b);
+        const float ms = timed([&] { launch_density(d, BatchView{}, groups[k], s->spos, s->off, s->meas, s->aux, none, st); });
         if (ms < best_d) { best_d = ms; gd = groups[k]; }
     }
-    launch_density(d, BatchView{}, gd, s->spos, s->off, s->meas, s->aux, st);
+    launch_density(d, BatchView{}, gd, s->spos, s->off, s->meas, s->aux, none, st);
     for (int k = 0; k < 3; ++k) {
-        launch_force(d, BatchView{}, groups[k], s->spos, s->svel, s->aux, sorted_idx(s), s->off, fa, fb,
-                     s->phase, st);
-        cudaEventRecord(a, st);
-        for (int r = 0; r < reps; ++r)
+        const float ms = timed([&] {
             launch_force(d, BatchView{}, groups[k], s->spos, s->svel, s->aux, sorted_idx(s), s->off, fa, fb,
-                     s->phase, st);
-        cudaEventRecord(b, st);
-        cudaEventSynchronize(b);
-        float ms = 0;
-        cudaEventElapsedTime(&ms, a, b);
+                         s->phase, none, st);
+        });
         if (ms < best_f) { best_f = ms; gf = groups[k]; }
     }
+    // interaction lists: the density pass records them, the force pass reads them
+    bool lists = false;
+    if (alloc_lists(s) == CMAG_OK) {
+        const NeighborList nl = nl_of(s);
+        const float ld = timed([&] { launch_density(d, BatchView{}, 1, s->spos, s->off, s->meas, s->aux, nl, st); });
+        const float lf = timed([&] {
+            launch_force(d, BatchView{}, 1, s->spos, s->svel, s->aux, sorted_idx(s), s->off, fa, fb, s->phase, nl, st);
+        });
+        lists = ld + lf < best_d + best_f;
+        if (!lists) free_lists(s);
+    } else if (had_lists) {
+        (void)cudaGetLastError();
+    }
+    s->last_error.clear();
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     CM_CUDA(s, cudaGetLastError());
@@ -1148,6 +1221,24 @@ int cmag_system_autotune(cmag_system *s, int32_t reps)
     invalidate_graph(s);
     return CMAG_OK;
 }
+
+int cmag_system_set_neighbor_lists(cmag_system *s, int32_t enable)
+{
+    if (!s) return fail(nullptr, CMAG_ERR_INVALID, "null handle");
+    if (enable < 0) return fail(s, CMAG_ERR_INVALID, "enable must be 0, 1 or an entry count");
+    int rc = enable ? alloc_lists(s, enable > 1 ? (uint32_t)enable : 0u) : free_lists(s);
+    invalidate_graph(s);
+    return rc;
+}
+
+int cmag_system_get_neighbor_lists(const cmag_system *s, int32_t *enabled, uint32_t *cap)
+{
+    if (!s) return fail(nullptr, CMAG_ERR_INVALID, "null handle");
+    if (enabled) *enabled = s->nl_entry != nullptr;
+    if (cap) *cap = s->nl_cap;
+    return CMAG_OK;
+}
+
 
 int cmag_system_set_closure(cmag_system *s, cmag_closure *c)
 {

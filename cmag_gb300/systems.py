@@ -200,8 +200,21 @@ class _System:
         return a.value, b.value
 
     def autotune(self, reps=3):
+        """Pick lanes per particle and interaction lists by timing; returns
+        (density lanes, force lanes, lists on)."""
         self._chk(lib().cmag_system_autotune(self._h, int(reps)))
-        return self.groups()
+        return self.groups() + (self.neighbor_lists()[0],)
+
+    def set_neighbor_lists(self, enable, cap=None):
+        """Interaction lists on/off; cap: entries per particle (default automatic)."""
+        v = (int(cap) if cap else 1) if enable else 0
+        self._chk(lib().cmag_system_set_neighbor_lists(self._h, v))
+
+    def neighbor_lists(self):
+        """(enabled, entries per particle)."""
+        e, c = ctypes.c_int32(), ctypes.c_uint32()
+        self._chk(lib().cmag_system_get_neighbor_lists(self._h, ctypes.byref(e), ctypes.byref(c)))
+        return bool(e.value), c.value
 
     def set_stage_timing(self, enable):
         self._chk(lib().cmag_system_set_stage_timing(self._h, int(bool(enable))))

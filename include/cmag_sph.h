@@ -303,9 +303,18 @@ int cmag_system_device_error_bits(cmag_system *s, uint32_t *bits);
  * particle's cell box are split between its lanes). */
 int cmag_system_set_groups(cmag_system *s, int32_t density_lanes, int32_t force_lanes);
 int cmag_system_get_groups(const cmag_system *s, int32_t *density_lanes, int32_t *force_lanes);
+/* Interaction lists: the density pass records each particle's interacting
+ * neighbours (sorted indices, in the order the force loop would visit them) and
+ * the force pass reads them instead of walking the cells again; the forces are
+ * bit-identical to the one-lane walk.  Memory: num_particles x cap x 4 bytes (cap
+ * about 1.5 times the lattice neighbour count + 32; enable > 1 sets cap instead;
+ * a particle with more neighbours walks the cells).  Fewer than 2^26 particles. */
+int cmag_system_set_neighbor_lists(cmag_system *s, int32_t enable);
+int cmag_system_get_neighbor_lists(const cmag_system *s, int32_t *enabled, uint32_t *cap);
 /* Autotune: on the current state, time the density and force kernels for every
- * lane count (`reps` launches each) and keep the fastest.  Both kernels are
- * recomputed from scratch every step, so tuning leaves the trajectory unchanged. */
+ * lane count and with interaction lists (`reps` launches each) and keep the
+ * fastest.  Both kernels are recomputed from scratch every step; the choice
+ * changes only the summation order of the lanes' partial sums. */
 int cmag_system_autotune(cmag_system *s, int32_t reps);
 
 /* Per-stage timing: when enabled, every step records CUDA events around each

@@ -164,6 +164,29 @@ def test_peristalsis_noslip_walls_step(gpu):
     s.close()
 
 
+@pytest.mark.parametrize("cap", [None, 40, 4])
+@pytest.mark.parametrize("name", sorted(SCENES))
+def test_interaction_lists_equal_the_walk(gpu, name, cap):
+    """With interaction lists the force pass reads the pairs the density pass
+    recorded: 15 steps give the one-lane walk's state bit for bit, also when some
+    (cap 40) or all (cap 4) particles overflow their list and walk the cells."""
+    s1, _ = SCENES[name]()
+    s2, _ = SCENES[name]()
+    s1.set_groups(1, 1)
+    s2.set_groups(1, 1)
+    s2.set_neighbor_lists(True, cap)
+    assert s2.neighbor_lists()[0]
+    s1.update_n(15)
+    s2.update_n(15)
+    s2.synchronize()
+    for a in (cm.POSITION, cm.VELOCITY, cm.MEASURES):
+        assert_int_equal(s2.getArray(a).view(np.uint32), s1.getArray(a).view(np.uint32), "%s array %d" % (name, a))
+    s2.set_neighbor_lists(False)
+    assert not s2.neighbor_lists()[0]
+    s1.close()
+    s2.close()
+
+
 @pytest.mark.parametrize("graphs", [True, False])
 def test_graph_replay_equals_plain_launches(gpu, graphs):
     """A captured-and-replayed step produces the same bits as plain launches."""
