@@ -276,35 +276,59 @@ __device__ __forceinline__ void to_a(const float (&c)[8][4], uint32_t (&a)[4][4]
 // APPLY false: out[r * 3 ..] = network(xb row r) for r < n.
 // APPLY true: rows are sorted particles; acc[idx[r]] += out_scale * clamp(y) for
 // fluid rows.
+// Byte layout of the staged weights: padded BF16 rows of W1..W4, then FP32 biases.
+constexpr int kImageBytes = kSWEnd * 2 + kSBEnd * 4;
+constexpr int kImageWords = kImageBytes / 16;
+static_assert(kSWEnd * 2 % 16 == 0 && kImageBytes % 16 == 0, "image rows must stay 16-byte aligned");
+
+// Builds the image once per parameter change (one thread per 32-bit image word),
+// so each network block stages it with plain 16-byte copies.
+__global__ void k_pack(const __nv_bfloat16 *__restrict__ w, uint32_t *__restrict__ image)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < kSWEnd / 2) {  // two BF16 weights per word
+        __nv_bfloat16 h[2];
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+            const int q = 2 * k + e;
+            __nv_bfloat16 v = __float2bfloat16_rn(0.0f);
+            if (q < kSW2) {
+                const int o = q / kW1Stride, i = q % kW1Stride;
+                if (i < kFeat) v = w[kOffW1 + o * kFeat + i];
+            } else {
+                const int base = q < kSW3 ? kSW2 : (q < kSW4 ? kSW3 : kSW4);
+                const int off = q < kSW3 ? kOffW2 : (q < kSW4 ? kOffW3 : kOffW4);
+                const int o = (q - base) / kWStride, i = (q - base) % kWStride;
+                if (i < kHidden && (base != kSW4 || o < kOut)) v = w[off + o * kHidden + i];
+            }
+            h[e] = v;
+        }
+        const __nv_bfloat162 v2 = __halves2bfloat162(h[0], h[1]);
+        image[k] = *reinterpret_cast<const uint32_t *>(&v2);
+    } else if (k < kImageBytes / 4) {
+        const int b = k - kSWEnd / 2;
+        float v = 0.0f;
+        if (b < kSB2) v = __bfloat162float(w[kOffB1 + b]);
+        else if (b < kSB3) v = __bfloat162float(w[kOffB2 + b - kSB2]);
+        else if (b < kSB4) v = __bfloat162float(w[kOffB3 + b - kSB3]);
+        else if (b - kSB4 < kOut) v = __bfloat162float(w[kOffB4 + b - kSB4]);
+        image[k] = __float_as_uint(v);
+    }
+}
+
+// APPLY false: out[r * 3 ..] = network(xb row r) for r < n.
+// APPLY true: rows are sorted particles; acc[idx[r]] += out_scale * clamp(y) for
+// fluid rows.
 template <bool APPLY>
 __global__ void __launch_bounds__(128)
     k_mlp(ClosureView c, const __nv_bfloat16 *__restrict__ xb, uint32_t n,
           const float4 *__restrict__ spos, const uint32_t *__restrict__ idx, float4 *acc,
           float *__restrict__ out)
 {
-    __shared__ __align__(16) __nv_bfloat16 sw[kSWEnd];
-    __shared__ float sb[kSBEnd];
-    for (int k = threadIdx.x; k < kSWEnd; k += blockDim.x) {
-        float v = 0.0f;
-        if (k < kSW2) {
-            const int o = k / kW1Stride, i = k % kW1Stride;
-            if (i < kFeat) v = __bfloat162float(c.w[kOffW1 + o * kFeat + i]);
-        } else {
-            const int base = k < kSW3 ? kSW2 : (k < kSW4 ? kSW3 : kSW4);
-            const int off = k < kSW3 ? kOffW2 : (k < kSW4 ? kOffW3 : kOffW4);
-            const int o = (k - base) / kWStride, i = (k - base) % kWStride;
-            if (i < kHidden && (base != kSW4 || o < kOut)) v = __bfloat162float(c.w[off + o * kHidden + i]);
-        }
-        sw[k] = __float2bfloat16_rn(v);  // exact: v is a BF16 value
-    }
-    for (int k = threadIdx.x; k < kSBEnd; k += blockDim.x) {
-        float v = 0.0f;
-        if (k < kSB2) v = __bfloat162float(c.w[kOffB1 + k]);
-        else if (k < kSB3) v = __bfloat162float(c.w[kOffB2 + k - kSB2]);
-        else if (k < kSB4) v = __bfloat162float(c.w[kOffB3 + k - kSB3]);
-        else if (k - kSB4 < kOut) v = __bfloat162float(c.w[kOffB4 + k - kSB4]);
-        sb[k] = v;
-    }
+    __shared__ uint4 simage[kImageWords];
+    for (int k = threadIdx.x; k < kImageWords; k += blockDim.x) simage[k] = __ldg(c.image + k);
+    const __nv_bfloat16 *sw = reinterpret_cast<const __nv_bfloat16 *>(simage);
+    const float *sb = reinterpret_cast<const float *>(simage) + kSWEnd / 2;
     __syncthreads();
     const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
     const uint32_t warps = gridDim.x * (blockDim.x >> 5);
@@ -606,13 +630,14 @@ void dispatch_features(const DevParams &p, const ClosureView &c, const float4 *s
 #undef CMAG_FEAT
 }
 
-// Each block stages the weights once and its 4 warps loop over 16-row tiles, so
-// the grid stays at a few blocks per SM (152 SMs) however many rows there are.
+// Each block stages the weight image once (23 KB) and its 4 warps loop over
+// 16-row tiles, so the grid stays at a few blocks per SM (152 SMs) however many
+// rows there are.
 uint32_t mlp_blocks(uint32_t n)
 {
     const uint32_t tiles = (n + 15) / 16;
     uint32_t b = (tiles + 3) / 4;
-    return b < 1 ? 1 : (b > 152 * 4 ? 152 * 4 : b);
+    return b < 1 ? 1 : (b > 152 * 8 ? 152 * 8 : b);
 }
 
 }  // namespace
@@ -665,17 +690,21 @@ void launch_closure_backward(const ClosureView &c, const float *feat, const floa
     k_backward<<<(n + kTile - 1) / kTile, kTile, kSmemBackward, st>>>(c, feat, target, n, grad, loss);
 }
 
+uint32_t closure_image_words() { return (uint32_t)kImageWords; }
+
 void launch_closure_adam(float *master, float *m, float *v, float *grad, __nv_bfloat16 *w,
-                         float lr, float beta1, float beta2, float eps, float bias1, float bias2,
-                         cudaStream_t st)
+                         uint4 *image, float lr, float beta1, float beta2, float eps, float bias1,
+                         float bias2, cudaStream_t st)
 {
     k_adam<<<(kClosureParams + 255) / 256, 256, 0, st>>>(master, m, v, grad, w, lr, beta1, beta2,
                                                         eps, bias1, bias2);
+    k_pack<<<(kImageBytes / 4 + 255) / 256, 256, 0, st>>>(w, reinterpret_cast<uint32_t *>(image));
 }
 
-void launch_closure_round(const float *master, __nv_bfloat16 *w, cudaStream_t st)
+void launch_closure_round(const float *master, __nv_bfloat16 *w, uint4 *image, cudaStream_t st)
 {
     k_round<<<(kClosureParams + 255) / 256, 256, 0, st>>>(master, w);
+    k_pack<<<(kImageBytes / 4 + 255) / 256, 256, 0, st>>>(w, reinterpret_cast<uint32_t *>(image));
 }
 
 }  // namespace cmag

@@ -31,7 +31,13 @@ struct ClosureView {
     const float *inv_std;     // kFeat feature scales
     const float *out_scale;   // correction = *out_scale * clamp(network output, +-*out_limit)
     const float *out_limit;
+    const uint4 *image;       // closure_image_words() words: the weights as the network
+                              // kernel stages them in shared memory (padded BF16 rows,
+                              // then FP32 biases), rebuilt whenever w changes
 };
+
+// Size of ClosureView::image in 16-byte words.
+uint32_t closure_image_words();
 
 // Per sorted fluid particle of a DamBreak scene: the 16 raw features, written
 // to feat[idx[i] * 16 ..] (original order).  Rows of wall particles are left
@@ -58,12 +64,13 @@ void launch_closure_forward(const ClosureView &c, const float *feat, uint32_t n,
 // gradient with respect to the BF16 parameters added to grad (FP32).
 void launch_closure_backward(const ClosureView &c, const float *feat, const float *target,
                              uint32_t n, float *grad, float *loss, cudaStream_t st);
-// Adam on the FP32 master copy; refreshes the BF16 copy and clears grad.
+// Adam on the FP32 master copy; refreshes the BF16 copy and its shared-memory
+// image and clears grad.
 void launch_closure_adam(float *master, float *m, float *v, float *grad, __nv_bfloat16 *w,
-                         float lr, float beta1, float beta2, float eps, float bias1,
-                         float bias2, cudaStream_t st);
-// BF16 copy of the master parameters.
-void launch_closure_round(const float *master, __nv_bfloat16 *w, cudaStream_t st);
+                         uint4 *image, float lr, float beta1, float beta2, float eps,
+                         float bias1, float bias2, cudaStream_t st);
+// BF16 copy of the master parameters and its shared-memory image.
+void launch_closure_round(const float *master, __nv_bfloat16 *w, uint4 *image, cudaStream_t st);
 
 }  // namespace cmag
 
@@ -71,6 +78,7 @@ void launch_closure_round(const float *master, __nv_bfloat16 *w, cudaStream_t st
 struct cmag_closure {
     float *master = nullptr, *m = nullptr, *v = nullptr, *grad = nullptr;  // FP32, kClosureParams
     __nv_bfloat16 *w = nullptr;                                            // BF16 copy used by kernels
+    uint4 *image = nullptr;                                                // w as the network kernel stages it
     float *norm = nullptr;   // mean[16], inv_std[16], out_scale, loss, out_limit
     uint32_t adam_steps = 0;
     __nv_bfloat16 *xb = nullptr;   // forward() scratch: normalised input rows
@@ -80,7 +88,7 @@ struct cmag_closure {
     cmag::ClosureView view() const
     {
         return cmag::ClosureView{w, norm, norm + cmag::kFeat, norm + 2 * cmag::kFeat,
-                                 norm + 2 * cmag::kFeat + 2};
+                                 norm + 2 * cmag::kFeat + 2, image};
     }
     float *loss() const { return norm + 2 * cmag::kFeat + 1; }
 };

@@ -36,7 +36,7 @@ cudaStream_t stream_of(cmag_closure *c, void *stream)
 
 void free_all(cmag_closure *c)
 {
-    void *ptrs[] = {c->master, c->m, c->v, c->grad, c->w, c->norm, c->xb};
+    void *ptrs[] = {c->master, c->m, c->v, c->grad, c->w, c->image, c->norm, c->xb};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -64,6 +64,7 @@ int cmag_closure_create(const float *params, cmag_closure **out)
     if (e == cudaSuccess) e = cudaMalloc((void **)&c->grad, pb);
     if (e == cudaSuccess) e = cudaMalloc((void **)&c->w, sizeof(__nv_bfloat16) * kClosureParams);
     if (e == cudaSuccess) e = cudaMalloc((void **)&c->norm, sizeof(float) * kNormFloats);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&c->image, sizeof(uint4) * closure_image_words());
     if (e == cudaSuccess) e = cudaMemset(c->m, 0, pb);
     if (e == cudaSuccess) e = cudaMemset(c->v, 0, pb);
     if (e == cudaSuccess) e = cudaMemset(c->grad, 0, pb);
@@ -77,7 +78,7 @@ int cmag_closure_create(const float *params, cmag_closure **out)
         if (e == cudaSuccess)
             e = cudaMemcpy(c->norm, norm.data(), sizeof(float) * kNormFloats, cudaMemcpyHostToDevice);
         if (e == cudaSuccess) {
-            launch_closure_round(c->master, c->w, c->stream);
+            launch_closure_round(c->master, c->w, c->image, c->stream);
             e = cudaStreamSynchronize(c->stream);
         }
     }
@@ -107,7 +108,7 @@ int cmag_closure_set_params(cmag_closure *c, const float *params)
     if (!c || !params) return cfail(c, CMAG_ERR_INVALID, "null argument");
     CC_CUDA(c, cudaMemcpyAsync(c->master, params, sizeof(float) * kClosureParams,
                                cudaMemcpyHostToDevice, c->stream));
-    launch_closure_round(c->master, c->w, c->stream);
+    launch_closure_round(c->master, c->w, c->image, c->stream);
     CC_CUDA(c, cudaGetLastError());
     CC_CUDA(c, cudaStreamSynchronize(c->stream));
     return CMAG_OK;
@@ -225,7 +226,7 @@ int cmag_closure_train_step(cmag_closure *c, const float *d_features, const floa
     const float bias2 = (float)(1.0 - std::pow((double)b2, (double)c->adam_steps));
     if (loss_out) CC_CUDA(c, cudaMemsetAsync(c->loss(), 0, sizeof(float), st));
     launch_closure_backward(c->view(), d_features, d_targets, n, c->grad, c->loss(), st);
-    launch_closure_adam(c->master, c->m, c->v, c->grad, c->w, lr, b1, b2, eps, bias1, bias2, st);
+    launch_closure_adam(c->master, c->m, c->v, c->grad, c->w, c->image, lr, b1, b2, eps, bias1, bias2, st);
     CC_CUDA(c, cudaGetLastError());
     if (loss_out) {
         CC_CUDA(c, cudaMemcpyAsync(loss_out, c->loss(), sizeof(float), cudaMemcpyDeviceToHost, st));
