@@ -133,34 +133,41 @@ __global__ void __launch_bounds__(kScanThreads, 4)
     }
     uint32_t texcl = wbase + x - sum;
 
-    if (threadIdx.x == 0) {
+    // decoupled look-back by warp 0: lane k reads tile t - k, so each round covers
+    // 32 predecessors (the counts add up in the same way as one tile at a time)
+    if (warp == 0) {
         volatile uint32_t *st = status;
         uint32_t exclusive = 0;
         if (tile == 0) {
-            st[0] = kFlagPrefix | total;
+            if (lane == 0) st[0] = kFlagPrefix | total;
         } else {
-            st[tile] = kFlagAgg | total;
+            if (lane == 0) st[tile] = kFlagAgg | total;
             int t = (int)tile - 1;
+            int spins = 0;
             while (t >= 0) {
-                uint32_t s;
-                int spins = 0;
-                while (true) {
-                    s = st[t];
-                    if (s & (kFlagAgg | kFlagPrefix)) break;
+                const uint32_t v = (t - lane >= 0) ? (uint32_t)st[t - lane] : (uint32_t)kFlagPrefix;
+                const uint32_t pub = __ballot_sync(0xffffffffu, (v & (kFlagAgg | kFlagPrefix)) != 0);
+                const uint32_t pre = __ballot_sync(0xffffffffu, (v & kFlagPrefix) != 0);
+                // lanes before the first unpublished tile, up to the first prefix
+                const uint32_t unpub = ~pub;
+                const int first_unpub = unpub ? __ffs(unpub) - 1 : 32;
+                const int first_pre = pre ? __ffs(pre) - 1 : 32;
+                const bool done = first_pre < first_unpub;
+                const int used = done ? first_pre + 1 : first_unpub;
+                exclusive += __reduce_add_sync(0xffffffffu, lane < used ? (v & kCountMask) : 0u);
+                if (done) break;
+                t -= used;
+                if (used == 0) {
                     if (++spins > kSpinLimit) {
-                        set_error(err, CMAG_DEVERR_LOOKBACK_TIMEOUT);
-                        s = kFlagPrefix;
-                        break;
+                        if (lane == 0) set_error(err, CMAG_DEVERR_LOOKBACK_TIMEOUT);
+                        break;  // give up: the rest counts as zero
                     }
                     if (spins > 8) __nanosleep(64);
                 }
-                exclusive += s & kCountMask;
-                if (s & kFlagPrefix) break;
-                --t;
             }
-            st[tile] = kFlagPrefix | (exclusive + total);
+            if (lane == 0) st[tile] = kFlagPrefix | (exclusive + total);
         }
-        s_prefix = exclusive;
+        if (lane == 0) s_prefix = exclusive;
     }
     __syncthreads();
     uint32_t run = s_prefix + texcl;

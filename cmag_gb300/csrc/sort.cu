@@ -13,7 +13,7 @@
 //     tile and tiles follow tile order, so the sort is stable and equals a stable
 //     sort by key -- bit-identical to the reference's thrust result.
 // Every look-back wait is bounded: after kSpinLimit polls the CTA records
-// CMAG_DEVERR_LOOKBACK_TIMEOUT, treats the missing count as zero and finishes.
+// CMAG_DEVERR_LOOKBACK_TIMEOUT, treats the missing counts as zero and finishes.
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -32,6 +32,7 @@ constexpr uint32_t kCountMask = (1u << 30) - 1u;
 constexpr int kSpinLimit = 1 << 22;
 constexpr int kWarps = kSortThreads / 32;
 constexpr uint32_t kInvalidDigit = 256;
+constexpr int kLookback = 16;  // predecessor tiles read per look-back round
 
 __device__ __forceinline__ uint32_t lanemask_lt()
 {
@@ -136,7 +137,8 @@ __global__ void __launch_bounds__(kSortThreads)
         s_whist[w][d] = run;
         run += c;
     }
-    // decoupled look-back over the tiles before this one
+    // decoupled look-back over the tiles before this one, kLookback tiles per
+    // round: the counts add up in the same way, in fewer dependent round trips
     volatile uint32_t *st = status;
     uint32_t exclusive = 0;
     if (tile == 0) {
@@ -144,22 +146,39 @@ __global__ void __launch_bounds__(kSortThreads)
     } else {
         st[(size_t)tile * kRadix + d] = kFlagAgg | run;
         int t = (int)tile - 1;
+        int spins = 0;
         while (t >= 0) {
-            uint32_t v;
-            int spins = 0;
-            while (true) {
-                v = st[(size_t)t * kRadix + d];
-                if (v & (kFlagAgg | kFlagPrefix)) break;
+            uint32_t v[kLookback];
+#pragma unroll
+            for (int k = 0; k < kLookback; ++k)
+                v[k] = (t - k >= 0) ? (uint32_t)st[(size_t)(t - k) * kRadix + d] : (uint32_t)kFlagPrefix;
+            // consume published tiles up to the first inclusive prefix; stop at the
+            // first tile that has published nothing yet
+            uint32_t add = 0;
+            int used = 0;
+            bool stop = false, done = false;
+#pragma unroll
+            for (int k = 0; k < kLookback; ++k) {
+                if (!stop) {
+                    if (v[k] & (kFlagAgg | kFlagPrefix)) {
+                        add += v[k] & kCountMask;
+                        ++used;
+                        if (v[k] & kFlagPrefix) stop = done = true;
+                    } else {
+                        stop = true;
+                    }
+                }
+            }
+            exclusive += add;
+            if (done) break;
+            t -= used;
+            if (used == 0) {
                 if (++spins > kSpinLimit) {
                     set_error(err, CMAG_DEVERR_LOOKBACK_TIMEOUT);
-                    v = kFlagPrefix;  // give up: count as zero and stop
-                    break;
+                    break;  // give up: the rest counts as zero
                 }
                 if (spins > 8) __nanosleep(64);
             }
-            exclusive += v & kCountMask;
-            if (v & kFlagPrefix) break;
-            --t;
         }
         st[(size_t)tile * kRadix + d] = kFlagPrefix | (exclusive + run);
     }
