@@ -69,7 +69,6 @@ struct cmag_batch {
     std::vector<DevParams> host_dev;     // per slot
     uint32_t n_total = 0;
     uint32_t table_total = 0;
-    int passes = 1;
     bool any_peristalsis = false;
     float k_milli = 0.0f;
 
@@ -81,7 +80,7 @@ struct cmag_batch {
            *vforce = nullptr, *pforce = nullptr, *pred = nullptr, *spos = nullptr, *svel = nullptr;
     uint32_t *hash[2] = {nullptr, nullptr}, *idx[2] = {nullptr, nullptr};
     uint32_t *cnt = nullptr, *off = nullptr, *ws = nullptr, *err = nullptr, *red = nullptr;
-    size_t ws_words = 0, sort_words = 0;
+    size_t ws_words = 0;
     float2 *aux = nullptr;
     PhaseState *phase = nullptr;
     DevParams *dev = nullptr;
@@ -182,8 +181,9 @@ BatchView view_of(const cmag_batch *b)
     return v;
 }
 
-uint32_t *sorted_idx(cmag_batch *b) { return b->idx[b->passes & 1]; }
-uint32_t *sorted_hash(cmag_batch *b) { return b->hash[b->passes & 1]; }
+// the counting sort's outputs (hash[0]: keys in particle order, idx[1]: scratch)
+uint32_t *sorted_idx(cmag_batch *b) { return b->idx[0]; }
+uint32_t *sorted_hash(cmag_batch *b) { return b->hash[1]; }
 
 int ensure_events(cmag_batch *b, size_t count)
 {
@@ -243,17 +243,14 @@ int record_step(cmag_batch *b, int last, bool timed)
         launch_configure_boundary(rep, v, b->pos, b->phase, st);
     }
     mark(0);
+    // keys = table slots: hash + counts + arrival ranks, offsets, counting sort
     CB_CUDA(b, cudaMemsetAsync(b->ws, 0, b->ws_words * sizeof(uint32_t), st));
-    SortWorkspace sw = sort_workspace_view(b->ws, b->n_total);
-    launch_hash(rep, v, b->pos, b->hash[0], b->cnt, sw.hist, b->passes, b->err, st);
-    launch_cell_scan(b->cnt, b->off, b->table_total + 1, b->ws + b->sort_words, b->err, st);
+    launch_hash(rep, v, b->pos, b->hash[0], b->cnt, nullptr, 0, b->idx[0], b->err, st);
+    launch_cell_scan(b->cnt, b->off, b->table_total + 1, b->ws, b->err, st);
     mark(1);
     if (last >= CMAG_STAGE_SORT)
-        for (int k = 0; k < b->passes; ++k) {
-            const int src = k & 1, dst = src ^ 1;
-            launch_onesweep_pass(b->hash[src], b->idx[src], b->hash[dst], b->idx[dst], b->n_total,
-                                 k, k == 0, sw, b->err, st);
-        }
+        launch_cell_sort(b->hash[0], b->idx[0], b->off, 0u, b->n_total, b->hash[1], b->idx[1],
+                         b->idx[0], b->err, st);
     mark(2);
     if (last >= CMAG_STAGE_REORDER)
         launch_reorder(sorted_idx(b), b->pos, b->vlf, b->spos, b->svel, b->n_total, st);
@@ -487,11 +484,6 @@ int cmag_batch_create(const cmag_sph_params *params, const uint32_t *counts, uin
     }
     b->n_total = (uint32_t)part;
     b->table_total = (uint32_t)table;
-    b->passes = std::max(1, sort_passes(log2u(b->table_total)));
-    if (b->passes > kMaxPasses) {
-        delete b;
-        return bfail(nullptr, CMAG_ERR_INVALID, "sort keys wider than 32 bits");
-    }
     // launch groups: runs of scenes with equal (family, shape, trim, bucket)
     for (uint32_t k = 0; k < scenes; ++k) {
         const BatchScene &s = b->sc[k];
@@ -561,8 +553,7 @@ int cmag_batch_create(const cmag_sph_params *params, const uint32_t *counts, uin
         }
         step(dalloc(b, &b->cnt, sizeof(uint32_t) * ((size_t)b->table_total + 1)));
         step(dalloc(b, &b->off, sizeof(uint32_t) * ((size_t)b->table_total + 1)));
-        b->sort_words = sort_workspace_words(b->n_total, b->passes);
-        b->ws_words = b->sort_words + cell_scan_workspace_words(b->table_total + 1);
+        b->ws_words = cell_scan_workspace_words(b->table_total + 1);
         step(dalloc(b, &b->ws, sizeof(uint32_t) * b->ws_words));
         step(dalloc(b, &b->err, sizeof(uint32_t)));
         step(dalloc(b, &b->red, sizeof(uint32_t) * 6 * (size_t)scenes));

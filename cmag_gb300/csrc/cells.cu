@@ -37,7 +37,7 @@ template <bool BATCH>
 __global__ void __launch_bounds__(256)
     k_hash(DevParams pv, BatchView bv, const float4 *__restrict__ pos, uint32_t *__restrict__ hash,
            uint32_t *__restrict__ cnt, uint32_t *__restrict__ hist, int passes,
-           uint32_t *err)
+           uint32_t *__restrict__ rank, uint32_t *err)
 {
     __shared__ uint32_t s_hist[kMaxPasses * kRadix];
     if (hist)
@@ -65,8 +65,16 @@ __global__ void __launch_bounds__(256)
             hash[i] = h;
         }
         uint32_t peers = __match_any_sync(0xffffffffu, h);
-        bool leader = (threadIdx.x & 31) == (uint32_t)(__ffs(peers) - 1);
-        if (valid && leader) atomicAdd(&cnt[slot], (uint32_t)__popc(peers));
+        const int lead = __ffs(peers) - 1;
+        bool leader = (threadIdx.x & 31) == (uint32_t)lead;
+        uint32_t first = 0;
+        if (valid && leader) first = atomicAdd(&cnt[slot], (uint32_t)__popc(peers));
+        if (rank) {
+            uint32_t below;
+            asm("mov.u32 %0, %%lanemask_lt;" : "=r"(below));
+            first = __shfl_sync(0xffffffffu, first, lead);
+            if (valid) rank[i] = first + (uint32_t)__popc(peers & below);
+        }
         if (hist) {
             for (int ps = 0; ps < passes; ++ps) {
                 uint32_t dg = valid ? ((h >> (8 * ps)) & 255u) : 0xffffffffu;
@@ -192,6 +200,54 @@ __global__ void __launch_bounds__(kScanThreads, 4)
     }
 }
 
+// Counting sort, step 1: particle i goes to slot off[cell] + rank[i] of its
+// cell's range (arrival order within the cell).
+__global__ void __launch_bounds__(256)
+    k_cell_scatter(const uint32_t *__restrict__ hash, const uint32_t *__restrict__ rank,
+                   const uint32_t *__restrict__ off, uint32_t key_base, uint32_t n,
+                   uint32_t *__restrict__ shash, uint32_t *__restrict__ tmp, uint32_t *err)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t h = hash[i];
+    const uint32_t q = __ldg(off + (h - key_base)) + rank[i];
+    if (q < n) {  // always, unless the counts and offsets disagree
+        shash[q] = h;
+        tmp[q] = i;
+    } else {
+        set_error(err, CMAG_DEVERR_RANGE);
+    }
+}
+
+// Counting sort, step 2: within each cell, the entry at slot q moves to the
+// cell's start + the number of the cell's entries with a smaller original index,
+// so each cell lists its particles by original index: the order of a stable
+// sort by hash.  A cell of c particles costs c loads per entry; the neighbour
+// loops read every particle of a cell for each of its particles as well.
+__global__ void __launch_bounds__(256)
+    k_cell_order(const uint32_t *__restrict__ shash, const uint32_t *__restrict__ tmp,
+                 const uint32_t *__restrict__ off, uint32_t key_base, uint32_t n,
+                 uint32_t *__restrict__ idx, uint32_t *err)
+{
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    const uint32_t c = shash[q] - key_base;
+    const uint32_t a = __ldg(off + c), b = __ldg(off + c + 1);
+    const uint32_t own = tmp[q];
+    if (b - a == 1u && a == q) {
+        idx[q] = own;
+        return;
+    }
+    if (!(a <= q && q < b && b <= n)) {  // counts and offsets disagree
+        set_error(err, CMAG_DEVERR_RANGE);
+        idx[q] = own;
+        return;
+    }
+    uint32_t r = 0;
+    for (uint32_t k = a; k < b; ++k) r += __ldg(tmp + k) < own ? 1u : 0u;
+    idx[a + r] = own;
+}
+
 // the copy half of reorderDataAndFindCellStartD (fluid_kernel.cu:91-96)
 __global__ void __launch_bounds__(256)
     k_reorder(const uint32_t *__restrict__ idx, const float4 *__restrict__ pos,
@@ -226,14 +282,25 @@ __global__ void k_cell_view(const uint32_t *__restrict__ off, uint32_t scan_base
 }  // namespace
 
 void launch_hash(const DevParams &p, const BatchView &bv, const float4 *pos, uint32_t *hash,
-                 uint32_t *cnt, uint32_t *hist, int passes, uint32_t *err, cudaStream_t st)
+                 uint32_t *cnt, uint32_t *hist, int passes, uint32_t *rank, uint32_t *err,
+                 cudaStream_t st)
 {
     const uint32_t n = bv.scenes ? bv.n_total : p.n;
     if (n == 0) return;
     uint32_t blocks = (n + 256 * 8 - 1) / (256 * 8);
     if (blocks < 1) blocks = 1;
-    if (bv.scenes) k_hash<true><<<blocks, 256, 0, st>>>(p, bv, pos, hash, cnt, hist, passes, err);
-    else k_hash<false><<<blocks, 256, 0, st>>>(p, bv, pos, hash, cnt, hist, passes, err);
+    if (bv.scenes) k_hash<true><<<blocks, 256, 0, st>>>(p, bv, pos, hash, cnt, hist, passes, rank, err);
+    else k_hash<false><<<blocks, 256, 0, st>>>(p, bv, pos, hash, cnt, hist, passes, rank, err);
+}
+
+void launch_cell_sort(const uint32_t *hash, const uint32_t *rank, const uint32_t *off,
+                      uint32_t key_base, uint32_t n, uint32_t *shash, uint32_t *tmp,
+                      uint32_t *idx, uint32_t *err, cudaStream_t st)
+{
+    if (n == 0) return;
+    const uint32_t blocks = (n + 255) / 256;
+    k_cell_scatter<<<blocks, 256, 0, st>>>(hash, rank, off, key_base, n, shash, tmp, err);
+    k_cell_order<<<blocks, 256, 0, st>>>(shash, tmp, off, key_base, n, idx, err);
 }
 
 size_t cell_scan_workspace_words(uint32_t m) { return 1 + (m + kScanTile - 1) / kScanTile; }

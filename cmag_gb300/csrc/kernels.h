@@ -42,9 +42,18 @@ void launch_onesweep_pass(const uint32_t *kin, const uint32_t *vin, uint32_t *ko
 
 // ---- cells (cells.cu) --------------------------------------------------------
 // Hash every particle, count particles per cell and accumulate the sort's digit
-// histograms.  hist may be null.
+// histograms.  hist may be null.  rank (may be null): per particle, its arrival
+// order among the particles of its cell (0, 1, ...; not deterministic).
 void launch_hash(const DevParams &p, const BatchView &bv, const float4 *pos, uint32_t *hash,
-                 uint32_t *cnt, uint32_t *hist, int passes, uint32_t *err, cudaStream_t st);
+                 uint32_t *cnt, uint32_t *hist, int passes, uint32_t *rank, uint32_t *err,
+                 cudaStream_t st);
+// Stable counting sort of the hashed particles by cell, from the dense offsets
+// (after launch_cell_scan): shash/idx = the hashes and original indices in the
+// order of a stable sort by hash (the radix sort's result exactly).  Cell of a
+// hash: h - key_base.  tmp: n words of scratch; idx may alias rank.
+void launch_cell_sort(const uint32_t *hash, const uint32_t *rank, const uint32_t *off,
+                      uint32_t key_base, uint32_t n, uint32_t *shash, uint32_t *tmp,
+                      uint32_t *idx, uint32_t *err, cudaStream_t st);
 // Exclusive scan of cnt[0..m) into off[0..m) (single pass, chained look-back),
 // clearing cnt for the next step.  ws must hold cell_scan_workspace_words(m), zeroed.
 size_t cell_scan_workspace_words(uint32_t m);

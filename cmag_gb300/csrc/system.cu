@@ -25,7 +25,6 @@ struct cmag_system {
     cmag_sph_params p{};
     uint32_t n = 0;
     uint64_t ncells = 0;
-    int passes = 1;
     int device = 0;
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
@@ -37,8 +36,8 @@ struct cmag_system {
     uint32_t *hash[2] = {nullptr, nullptr}, *idx[2] = {nullptr, nullptr};
     uint32_t *cnt = nullptr, *off = nullptr;
     float2 *aux = nullptr;   // per sorted particle: p/rho^2 and rho or 1/rho
-    uint32_t *ws = nullptr;  // sort + scan workspace, cleared every step
-    size_t ws_words = 0, sort_words = 0;
+    uint32_t *ws = nullptr;  // cell scan workspace, cleared every step
+    size_t ws_words = 0;
     uint32_t *err = nullptr;
     PhaseState *phase = nullptr;
     uint32_t *view_cs = nullptr, *view_ce = nullptr;
@@ -345,8 +344,9 @@ void refresh_layout(cmag_system *s)
 
 cudaStream_t st_of(cmag_system *s) { return s->stream; }
 
-uint32_t *sorted_hash(cmag_system *s) { return s->hash[s->passes & 1]; }
-uint32_t *sorted_idx(cmag_system *s) { return s->idx[s->passes & 1]; }
+// the counting sort's outputs (hash[0]: hashes in particle order, idx[1]: scratch)
+uint32_t *sorted_hash(cmag_system *s) { return s->hash[1]; }
+uint32_t *sorted_idx(cmag_system *s) { return s->idx[0]; }
 
 int ensure_events(cmag_system *s, size_t count)
 {
@@ -377,18 +377,15 @@ int record_step(cmag_system *s, int last, bool timed)
         launch_configure_boundary(d, BatchView{}, s->pos, s->phase, st);
     }
     mark(0);
+    // hash + per-cell counts (and each particle's arrival rank in its cell), dense
+    // offsets, then the stable counting sort by cell
     CM_CUDA(s, cudaMemsetAsync(s->ws, 0, s->ws_words * sizeof(uint32_t), st));
-    SortWorkspace sw = sort_workspace_view(s->ws, s->n);
-    launch_hash(d, BatchView{}, s->pos, s->hash[0], s->cnt, sw.hist, s->passes, s->err, st);
-    launch_cell_scan(s->cnt, s->off, s->scan_cells + 1, s->ws + s->sort_words, s->err, st);
+    launch_hash(d, BatchView{}, s->pos, s->hash[0], s->cnt, nullptr, 0, s->idx[0], s->err, st);
+    launch_cell_scan(s->cnt, s->off, s->scan_cells + 1, s->ws, s->err, st);
     mark(1);
-    if (last >= CMAG_STAGE_SORT) {
-        for (int k = 0; k < s->passes; ++k) {
-            const int src = k & 1, dst = src ^ 1;
-            launch_onesweep_pass(s->hash[src], s->idx[src], s->hash[dst], s->idx[dst], s->n, k,
-                                 k == 0, sw, s->err, st);
-        }
-    }
+    if (last >= CMAG_STAGE_SORT)
+        launch_cell_sort(s->hash[0], s->idx[0], s->off, s->scan_base, s->n, s->hash[1], s->idx[1],
+                         s->idx[0], s->err, st);
     mark(2);
     if (last >= CMAG_STAGE_REORDER)
         launch_reorder(sorted_idx(s), s->pos, s->vlf, s->spos, s->svel, s->n, st);
@@ -638,9 +635,6 @@ int cmag_system_create(const cmag_sph_params *params, uint32_t n, cmag_system **
     s->p = *params;
     s->n = n;
     s->ncells = (uint64_t)params->grid_size[0] * params->grid_size[1] * params->grid_size[2];
-    const uint32_t bits = log2u(s->ncells);
-    s->passes = sort_passes(bits);
-    if (s->passes < 1) s->passes = 1;
     s->k_milli = std::pow(10.0f, -3.0f);
     s->scan_base = 0;
     s->scan_cells = (uint32_t)s->ncells;
@@ -685,8 +679,7 @@ int cmag_system_create(const cmag_sph_params *params, uint32_t n, cmag_system **
     // per-cell counters and offsets for the whole grid (+1 sentinel entry)
     step(dalloc(s, &s->cnt, sizeof(uint32_t) * (s->ncells + 1)));
     step(dalloc(s, &s->off, sizeof(uint32_t) * (s->ncells + 1)));
-    s->sort_words = sort_workspace_words(n, s->passes);
-    s->ws_words = s->sort_words + cell_scan_workspace_words((uint32_t)(s->ncells + 1));
+    s->ws_words = cell_scan_workspace_words((uint32_t)(s->ncells + 1));
     step(dalloc(s, &s->ws, sizeof(uint32_t) * s->ws_words));
     step(dalloc(s, &s->err, sizeof(uint32_t)));
     step(dalloc(s, &s->phase, sizeof(PhaseState)));
