@@ -1,16 +1,22 @@
-// cells.cu -- grid hash, per-cell counts and dense cell offsets, sorted gather.
+// cells.cu -- grid hash, per-cell counts and dense cell offsets, the per-step
+// counting sort, sorted gather.
 //
 // The reference finds cell ranges after the sort: it clears cellStart for the
 // whole grid (cudaMemset, fluidSystem.cu:161) and writes cellStart/cellEnd where
 // the sorted hash changes (reorderDataAndFindCellStartD, fluid_kernel.cu:50-97).
-// Here the hash kernel also counts particles per cell (warp-aggregated atomics),
-// and one chained-scan pass turns the counts into a dense offset table
+// Here the hash kernel also counts particles per cell (one atomic increment per
+// particle, whose return value is the particle's arrival rank in its cell), and
+// one chained-scan pass turns the counts into a dense offset table
 //     off[c] = number of particles with hash < c,   c = 0 .. scan_cells,
 // so the particles of any run of consecutive cells [a, b] are the sorted range
 // [off[a], off[b+1]).  A row of neighbour cells costs two loads instead of one
 // or two per cell, and no full-grid clear is needed: the scan re-zeroes exactly
 // the counters it consumed.  The reference's cellStart/cellEnd arrays are
 // derived from the table on request (launch_cell_view).
+//
+// The table also sorts the particles (sortParticles, fluidSystem.cu:94-99): each
+// particle goes to off[cell] + rank, and a second pass orders every cell's few
+// entries by original index, which is the order of a stable sort by hash.
 #include <cuda_runtime.h>
 
 #include "kernels.h"
@@ -27,67 +33,34 @@ constexpr uint32_t kFlagPrefix = 2u << 30;
 constexpr uint32_t kCountMask = (1u << 30) - 1u;
 constexpr int kSpinLimit = 1 << 22;
 
-// calcHashD (fluid_kernel.cu:34-48) + per-cell counts + radix digit histograms.
+// calcHashD (fluid_kernel.cu:34-48) + per-cell counts, one particle per thread.
 // The sort key is the reference hash for a single scene; in a batch it is the
 // particle's cell index in the shared offset table (scene table base + cell), so
-// one sort orders by scene, then by cell.  A particle whose cell lies outside
+// the sort orders by scene, then by cell.  A particle whose cell lies outside
 // its offset table (a planar scene's particle that left its z layer) is counted
-// in the table's last cell and reported as CMAG_DEVERR_RANGE.
+// in the table's last cell and reported as CMAG_DEVERR_RANGE.  rank[i] (when
+// given) is the count the particle's atomic increment found: its arrival order
+// among the particles of its cell.
 template <bool BATCH>
 __global__ void __launch_bounds__(256)
     k_hash(DevParams pv, BatchView bv, const float4 *__restrict__ pos, uint32_t *__restrict__ hash,
-           uint32_t *__restrict__ cnt, uint32_t *__restrict__ hist, int passes,
-           uint32_t *__restrict__ rank, uint32_t *err)
+           uint32_t *__restrict__ cnt, uint32_t *__restrict__ rank, uint32_t *err)
 {
-    __shared__ uint32_t s_hist[kMaxPasses * kRadix];
-    if (hist)
-        for (int b = threadIdx.x; b < passes * kRadix; b += blockDim.x) s_hist[b] = 0;
-    __syncthreads();
-    const uint32_t stride = gridDim.x * blockDim.x;
-    const uint32_t n = BATCH ? bv.n_total : pv.n;
-    // every lane runs the same trip count so the warp-collective calls stay converged
-    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
-        uint32_t i = base + threadIdx.x;
-        bool valid = i < n;
-        uint32_t h = 0xffffffffu, slot = 0;
-        if (valid) {
-            const DevParams &p = BATCH ? bv.scenes[bv.scene_of[i]] : pv;
-            float4 q = pos[i];
-            int3 g = grid_pos(p, q.x, q.y, q.z);
-            const uint32_t hr = grid_hash(p, g.x, g.y, g.z);
-            uint32_t rel = hr - p.scan_base;  // wraps for hr < scan_base
-            if (rel >= p.scan_cells) {
-                set_error(err, CMAG_DEVERR_RANGE);
-                rel = p.scan_cells - 1;
-            }
-            slot = p.table_base + rel;
-            h = BATCH ? slot : p.scan_base + rel;  // = hr inside the table
-            hash[i] = h;
-        }
-        uint32_t peers = __match_any_sync(0xffffffffu, h);
-        const int lead = __ffs(peers) - 1;
-        bool leader = (threadIdx.x & 31) == (uint32_t)lead;
-        uint32_t first = 0;
-        if (valid && leader) first = atomicAdd(&cnt[slot], (uint32_t)__popc(peers));
-        if (rank) {
-            uint32_t below;
-            asm("mov.u32 %0, %%lanemask_lt;" : "=r"(below));
-            first = __shfl_sync(0xffffffffu, first, lead);
-            if (valid) rank[i] = first + (uint32_t)__popc(peers & below);
-        }
-        if (hist) {
-            for (int ps = 0; ps < passes; ++ps) {
-                uint32_t dg = valid ? ((h >> (8 * ps)) & 255u) : 0xffffffffu;
-                uint32_t dp = __match_any_sync(0xffffffffu, dg);
-                if (valid && (threadIdx.x & 31) == (uint32_t)(__ffs(dp) - 1))
-                    atomicAdd(&s_hist[ps * kRadix + dg], (uint32_t)__popc(dp));
-            }
-        }
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (BATCH ? bv.n_total : pv.n)) return;
+    const DevParams &p = BATCH ? bv.scenes[bv.scene_of[i]] : pv;
+    const float4 q = pos[i];
+    const int3 g = grid_pos(p, q.x, q.y, q.z);
+    const uint32_t hr = grid_hash(p, g.x, g.y, g.z);
+    uint32_t rel = hr - p.scan_base;  // wraps for hr < scan_base
+    if (rel >= p.scan_cells) {
+        set_error(err, CMAG_DEVERR_RANGE);
+        rel = p.scan_cells - 1;
     }
-    __syncthreads();
-    if (hist)
-        for (int b = threadIdx.x; b < passes * kRadix; b += blockDim.x)
-            if (s_hist[b]) atomicAdd(&hist[b], s_hist[b]);
+    const uint32_t slot = p.table_base + rel;
+    hash[i] = BATCH ? slot : p.scan_base + rel;  // = hr inside the table
+    const uint32_t r = atomicAdd(cnt + slot, 1u);
+    if (rank) rank[i] = r;
 }
 
 __global__ void __launch_bounds__(kScanThreads, 4)
@@ -282,15 +255,13 @@ __global__ void k_cell_view(const uint32_t *__restrict__ off, uint32_t scan_base
 }  // namespace
 
 void launch_hash(const DevParams &p, const BatchView &bv, const float4 *pos, uint32_t *hash,
-                 uint32_t *cnt, uint32_t *hist, int passes, uint32_t *rank, uint32_t *err,
-                 cudaStream_t st)
+                 uint32_t *cnt, uint32_t *rank, uint32_t *err, cudaStream_t st)
 {
     const uint32_t n = bv.scenes ? bv.n_total : p.n;
     if (n == 0) return;
-    uint32_t blocks = (n + 256 * 8 - 1) / (256 * 8);
-    if (blocks < 1) blocks = 1;
-    if (bv.scenes) k_hash<true><<<blocks, 256, 0, st>>>(p, bv, pos, hash, cnt, hist, passes, rank, err);
-    else k_hash<false><<<blocks, 256, 0, st>>>(p, bv, pos, hash, cnt, hist, passes, rank, err);
+    const uint32_t blocks = (n + 255) / 256;
+    if (bv.scenes) k_hash<true><<<blocks, 256, 0, st>>>(p, bv, pos, hash, cnt, rank, err);
+    else k_hash<false><<<blocks, 256, 0, st>>>(p, bv, pos, hash, cnt, rank, err);
 }
 
 void launch_cell_sort(const uint32_t *hash, const uint32_t *rank, const uint32_t *off,

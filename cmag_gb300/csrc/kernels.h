@@ -41,12 +41,11 @@ void launch_onesweep_pass(const uint32_t *kin, const uint32_t *vin, uint32_t *ko
                           const SortWorkspace &ws, uint32_t *err, cudaStream_t st);
 
 // ---- cells (cells.cu) --------------------------------------------------------
-// Hash every particle, count particles per cell and accumulate the sort's digit
-// histograms.  hist may be null.  rank (may be null): per particle, its arrival
-// order among the particles of its cell (0, 1, ...; not deterministic).
+// Hash every particle and count particles per cell.  rank (may be null): per
+// particle, its arrival order among the particles of its cell (0, 1, ...; not
+// deterministic).
 void launch_hash(const DevParams &p, const BatchView &bv, const float4 *pos, uint32_t *hash,
-                 uint32_t *cnt, uint32_t *hist, int passes, uint32_t *rank, uint32_t *err,
-                 cudaStream_t st);
+                 uint32_t *cnt, uint32_t *rank, uint32_t *err, cudaStream_t st);
 // Stable counting sort of the hashed particles by cell, from the dense offsets
 // (after launch_cell_scan): shash/idx = the hashes and original indices in the
 // order of a stable sort by hash (the radix sort's result exactly).  Cell of a

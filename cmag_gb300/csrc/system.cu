@@ -380,7 +380,7 @@ int record_step(cmag_system *s, int last, bool timed)
     // hash + per-cell counts (and each particle's arrival rank in its cell), dense
     // offsets, then the stable counting sort by cell
     CM_CUDA(s, cudaMemsetAsync(s->ws, 0, s->ws_words * sizeof(uint32_t), st));
-    launch_hash(d, BatchView{}, s->pos, s->hash[0], s->cnt, nullptr, 0, s->idx[0], s->err, st);
+    launch_hash(d, BatchView{}, s->pos, s->hash[0], s->cnt, s->idx[0], s->err, st);
     launch_cell_scan(s->cnt, s->off, s->scan_cells + 1, s->ws, s->err, st);
     mark(1);
     if (last >= CMAG_STAGE_SORT)
