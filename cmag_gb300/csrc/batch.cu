@@ -244,9 +244,8 @@ int record_step(cmag_batch *b, int last, bool timed)
     }
     mark(0);
     // keys = table slots: hash + counts + arrival ranks, offsets, counting sort
-    CB_CUDA(b, cudaMemsetAsync(b->ws, 0, b->ws_words * sizeof(uint32_t), st));
     launch_hash(rep, v, b->pos, b->hash[0], b->cnt, b->idx[0], b->err, st);
-    launch_cell_scan(b->cnt, b->off, b->table_total + 1, b->ws, b->err, st);
+    launch_cell_scan(b->cnt, b->off, b->table_total + 1, b->ws, st);
     mark(1);
     if (last >= CMAG_STAGE_SORT)
         launch_cell_sort(b->hash[0], b->idx[0], b->off, 0u, b->n_total, b->hash[1], b->idx[1],

@@ -28,10 +28,6 @@ namespace {
 constexpr int kScanThreads = 256;
 constexpr int kScanItems = 16;
 constexpr uint32_t kScanTile = kScanThreads * kScanItems;
-constexpr uint32_t kFlagAgg = 1u << 30;
-constexpr uint32_t kFlagPrefix = 2u << 30;
-constexpr uint32_t kCountMask = (1u << 30) - 1u;
-constexpr int kSpinLimit = 1 << 22;
 
 // calcHashD (fluid_kernel.cu:34-48) + per-cell counts, one particle per thread.
 // The sort key is the reference hash for a single scene; in a batch it is the
@@ -63,95 +59,115 @@ __global__ void __launch_bounds__(256)
     if (rank) rank[i] = r;
 }
 
-__global__ void __launch_bounds__(kScanThreads, 4)
-    k_cell_scan(uint32_t *__restrict__ cnt, uint32_t *__restrict__ off, uint32_t m,
-                uint32_t *tile_ctr, uint32_t *status, uint32_t *err)
+// The 16 counts of cells [first, first + 16) (zeros past m).
+__device__ __forceinline__ void load_counts(const uint32_t *__restrict__ cnt, uint32_t first,
+                                            uint32_t m, uint32_t (&v)[kScanItems])
 {
-    __shared__ uint32_t s_warp[kScanThreads / 32];
-    __shared__ uint32_t s_tile, s_prefix;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (threadIdx.x == 0) s_tile = atomicAdd(tile_ctr, 1u);
-    __syncthreads();
-    const uint32_t tile = s_tile;
-    const uint32_t first = tile * kScanTile + threadIdx.x * kScanItems;
-    uint32_t v[kScanItems];
-    uint32_t sum = 0;
     if (first + kScanItems <= m) {
         const uint4 *src = reinterpret_cast<const uint4 *>(cnt + first);
 #pragma unroll
         for (int k = 0; k < kScanItems / 4; ++k) {
-            uint4 q = src[k];
+            const uint4 q = src[k];
             v[4 * k] = q.x; v[4 * k + 1] = q.y; v[4 * k + 2] = q.z; v[4 * k + 3] = q.w;
-            if (q.x | q.y | q.z | q.w)
-                reinterpret_cast<uint4 *>(cnt + first)[k] = make_uint4(0, 0, 0, 0);
         }
     } else {
 #pragma unroll
-        for (int k = 0; k < kScanItems; ++k) {
-            uint32_t c = first + k;
-            v[k] = (c < m) ? cnt[c] : 0u;
-            if (c < m && v[k]) cnt[c] = 0;
-        }
+        for (int k = 0; k < kScanItems; ++k) v[k] = (first + k < m) ? cnt[first + k] : 0u;
     }
+}
+
+// Sum over the block (result in every thread).
+__device__ __forceinline__ uint32_t block_sum(uint32_t x, uint32_t *s_warp)
+{
+    x = __reduce_add_sync(0xffffffffu, x);
+    if ((threadIdx.x & 31) == 0) s_warp[threadIdx.x >> 5] = x;
+    __syncthreads();
+    uint32_t t = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s_warp[w];
+    __syncthreads();
+    return t;
+}
+
+// Scan, step 1: the particle count of each tile of kScanTile cells.
+__global__ void __launch_bounds__(kScanThreads)
+    k_tile_sum(const uint32_t *__restrict__ cnt, uint32_t m, uint32_t *__restrict__ tot)
+{
+    __shared__ uint32_t s_warp[kScanThreads / 32];
+    uint32_t v[kScanItems];
+    load_counts(cnt, blockIdx.x * kScanTile + threadIdx.x * kScanItems, m, v);
+    uint32_t sum = 0;
 #pragma unroll
     for (int k = 0; k < kScanItems; ++k) sum += v[k];
+    sum = block_sum(sum, s_warp);
+    if (threadIdx.x == 0) tot[blockIdx.x] = sum;
+}
 
-    // block exclusive scan of the thread sums
+// Scan, step 2: exclusive scan of the tile counts in place, by one block: each
+// thread sums a contiguous chunk of tiles, the block scans the chunk sums, and
+// each thread rewrites its chunk from its offset.
+__global__ void __launch_bounds__(1024) k_tile_prefix(uint32_t *__restrict__ tot, uint32_t tiles)
+{
+    __shared__ uint32_t s_warp[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t per = (tiles + blockDim.x - 1) / blockDim.x;
+    const uint32_t a = min(tiles, threadIdx.x * per), b = min(tiles, a + per);
+    uint32_t sum = 0;
+    for (uint32_t k = a; k < b; ++k) sum += tot[k];
     uint32_t x = sum;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
         if (lane >= o) x += y;
     }
     if (lane == 31) s_warp[warp] = x;
     __syncthreads();
-    uint32_t wbase = 0, total = 0;
-#pragma unroll
-    for (int w = 0; w < kScanThreads / 32; ++w) {
-        uint32_t t = s_warp[w];
-        wbase += (w < warp) ? t : 0u;
-        total += t;
+    uint32_t run = x - sum;
+    for (int w = 0; w < warp; ++w) run += s_warp[w];
+    for (uint32_t k = a; k < b; ++k) {
+        const uint32_t v = tot[k];
+        tot[k] = run;
+        run += v;
     }
-    uint32_t texcl = wbase + x - sum;
+}
 
-    // decoupled look-back by warp 0: lane k reads tile t - k, so each round covers
-    // 32 predecessors (the counts add up in the same way as one tile at a time)
-    if (warp == 0) {
-        volatile uint32_t *st = status;
-        uint32_t exclusive = 0;
-        if (tile == 0) {
-            if (lane == 0) st[0] = kFlagPrefix | total;
-        } else {
-            if (lane == 0) st[tile] = kFlagAgg | total;
-            int t = (int)tile - 1;
-            int spins = 0;
-            while (t >= 0) {
-                const uint32_t v = (t - lane >= 0) ? (uint32_t)st[t - lane] : (uint32_t)kFlagPrefix;
-                const uint32_t pub = __ballot_sync(0xffffffffu, (v & (kFlagAgg | kFlagPrefix)) != 0);
-                const uint32_t pre = __ballot_sync(0xffffffffu, (v & kFlagPrefix) != 0);
-                // lanes before the first unpublished tile, up to the first prefix
-                const uint32_t unpub = ~pub;
-                const int first_unpub = unpub ? __ffs(unpub) - 1 : 32;
-                const int first_pre = pre ? __ffs(pre) - 1 : 32;
-                const bool done = first_pre < first_unpub;
-                const int used = done ? first_pre + 1 : first_unpub;
-                exclusive += __reduce_add_sync(0xffffffffu, lane < used ? (v & kCountMask) : 0u);
-                if (done) break;
-                t -= used;
-                if (used == 0) {
-                    if (++spins > kSpinLimit) {
-                        if (lane == 0) set_error(err, CMAG_DEVERR_LOOKBACK_TIMEOUT);
-                        break;  // give up: the rest counts as zero
-                    }
-                    if (spins > 8) __nanosleep(64);
-                }
-            }
-            if (lane == 0) st[tile] = kFlagPrefix | (exclusive + total);
-        }
-        if (lane == 0) s_prefix = exclusive;
+// Scan, step 3: each tile's cells from its prefix: off[c] = particles in cells
+// before c.  Clears the counts it read (the next hash pass adds to zeros).
+__global__ void __launch_bounds__(kScanThreads)
+    k_cell_offsets(uint32_t *__restrict__ cnt, uint32_t *__restrict__ off, uint32_t m,
+                   const uint32_t *__restrict__ tot)
+{
+    __shared__ uint32_t s_warp[kScanThreads / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t first = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    const uint32_t prefix = __ldg(tot + blockIdx.x);
+    uint32_t v[kScanItems];
+    load_counts(cnt, first, m, v);
+    uint32_t sum = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) sum += v[k];
+    if (first + kScanItems <= m) {
+        uint4 *c4 = reinterpret_cast<uint4 *>(cnt + first);
+#pragma unroll
+        for (int k = 0; k < kScanItems / 4; ++k)
+            if (v[4 * k] | v[4 * k + 1] | v[4 * k + 2] | v[4 * k + 3]) c4[k] = make_uint4(0, 0, 0, 0);
+    } else {
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k)
+            if (first + k < m && v[k]) cnt[first + k] = 0;
     }
+    // block exclusive scan of the thread sums
+    uint32_t x = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_warp[warp] = x;
     __syncthreads();
-    uint32_t run = s_prefix + texcl;
+    uint32_t wbase = 0;
+#pragma unroll
+    for (int w = 0; w < kScanThreads / 32; ++w) wbase += (w < warp) ? s_warp[w] : 0u;
+    uint32_t run = prefix + wbase + x - sum;
     if (first + kScanItems <= m) {
         uint4 *dst = reinterpret_cast<uint4 *>(off + first);
 #pragma unroll
@@ -166,8 +182,7 @@ __global__ void __launch_bounds__(kScanThreads, 4)
     } else {
 #pragma unroll
         for (int k = 0; k < kScanItems; ++k) {
-            uint32_t c = first + k;
-            if (c < m) off[c] = run;
+            if (first + k < m) off[first + k] = run;
             run += v[k];
         }
     }
@@ -274,13 +289,15 @@ void launch_cell_sort(const uint32_t *hash, const uint32_t *rank, const uint32_t
     k_cell_order<<<blocks, 256, 0, st>>>(shash, tmp, off, key_base, n, idx, err);
 }
 
-size_t cell_scan_workspace_words(uint32_t m) { return 1 + (m + kScanTile - 1) / kScanTile; }
+size_t cell_scan_workspace_words(uint32_t m) { return (m + kScanTile - 1) / kScanTile; }
 
-void launch_cell_scan(uint32_t *cnt, uint32_t *off, uint32_t m, uint32_t *ws, uint32_t *err,
-                      cudaStream_t st)
+void launch_cell_scan(uint32_t *cnt, uint32_t *off, uint32_t m, uint32_t *ws, cudaStream_t st)
 {
-    uint32_t tiles = (m + kScanTile - 1) / kScanTile;
-    k_cell_scan<<<tiles, kScanThreads, 0, st>>>(cnt, off, m, ws, ws + 1, err);
+    const uint32_t tiles = (m + kScanTile - 1) / kScanTile;
+    if (tiles == 0) return;
+    k_tile_sum<<<tiles, kScanThreads, 0, st>>>(cnt, m, ws);
+    k_tile_prefix<<<1, 1024, 0, st>>>(ws, tiles);
+    k_cell_offsets<<<tiles, kScanThreads, 0, st>>>(cnt, off, m, ws);
 }
 
 void launch_reorder(const uint32_t *idx, const float4 *pos, const float4 *vlf, float4 *spos,

@@ -53,11 +53,11 @@ void launch_hash(const DevParams &p, const BatchView &bv, const float4 *pos, uin
 void launch_cell_sort(const uint32_t *hash, const uint32_t *rank, const uint32_t *off,
                       uint32_t key_base, uint32_t n, uint32_t *shash, uint32_t *tmp,
                       uint32_t *idx, uint32_t *err, cudaStream_t st);
-// Exclusive scan of cnt[0..m) into off[0..m) (single pass, chained look-back),
-// clearing cnt for the next step.  ws must hold cell_scan_workspace_words(m), zeroed.
+// Exclusive scan of cnt[0..m) into off[0..m) (tile totals, their scan, then
+// every tile from its prefix), clearing cnt for the next step.  ws must hold
+// cell_scan_workspace_words(m) words (no clearing needed).
 size_t cell_scan_workspace_words(uint32_t m);
-void launch_cell_scan(uint32_t *cnt, uint32_t *off, uint32_t m, uint32_t *ws, uint32_t *err,
-                      cudaStream_t st);
+void launch_cell_scan(uint32_t *cnt, uint32_t *off, uint32_t m, uint32_t *ws, cudaStream_t st);
 // sortedPos/sortedVel gather (reorderDataAndFindCellStartD's copy half).
 void launch_reorder(const uint32_t *idx, const float4 *pos, const float4 *vlf, float4 *spos,
                     float4 *svel, uint32_t n, cudaStream_t st);

@@ -36,7 +36,7 @@ struct cmag_system {
     uint32_t *hash[2] = {nullptr, nullptr}, *idx[2] = {nullptr, nullptr};
     uint32_t *cnt = nullptr, *off = nullptr;
     float2 *aux = nullptr;   // per sorted particle: p/rho^2 and rho or 1/rho
-    uint32_t *ws = nullptr;  // cell scan workspace, cleared every step
+    uint32_t *ws = nullptr;  // cell scan: per-tile counts and their prefixes
     size_t ws_words = 0;
     uint32_t *err = nullptr;
     PhaseState *phase = nullptr;
@@ -379,9 +379,8 @@ int record_step(cmag_system *s, int last, bool timed)
     mark(0);
     // hash + per-cell counts (and each particle's arrival rank in its cell), dense
     // offsets, then the stable counting sort by cell
-    CM_CUDA(s, cudaMemsetAsync(s->ws, 0, s->ws_words * sizeof(uint32_t), st));
     launch_hash(d, BatchView{}, s->pos, s->hash[0], s->cnt, s->idx[0], s->err, st);
-    launch_cell_scan(s->cnt, s->off, s->scan_cells + 1, s->ws, s->err, st);
+    launch_cell_scan(s->cnt, s->off, s->scan_cells + 1, s->ws, st);
     mark(1);
     if (last >= CMAG_STAGE_SORT)
         launch_cell_sort(s->hash[0], s->idx[0], s->off, s->scan_base, s->n, s->hash[1], s->idx[1],
