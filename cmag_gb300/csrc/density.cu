@@ -35,7 +35,9 @@ using walk::shift_code;
 
 // Un-normalised Wendland sum over candidates [b, e) of one run, two candidates
 // per step in paired FP32 (FFMA2/FMUL2/FADD2: two FP32 operations per issued
-// instruction on sm_100+), scalar tail.  Adds (1 - q/2)^4 (2q + 1) for q < 2.
+// instruction on sm_100+), scalar tail.  Adds max(1 - q/2, 0)^4 (2q + 1): zero
+// outside the support without a compare and select (the loop is bound by the
+// integer/compare pipe, not by FP32).
 template <int SYS, bool TRIM, bool LIST>
 __device__ __forceinline__ void wendland_run(const DevParams &p, const float4 *__restrict__ spos,
                                              uint32_t b, uint32_t e, float4 pi, float sx, float sy,
@@ -47,7 +49,7 @@ __device__ __forceinline__ void wendland_run(const DevParams &p, const float4 *_
                  pz = make_float2(pi.z, pi.z);
     const float2 m1 = make_float2(-1.0f, -1.0f), half = make_float2(-0.5f, -0.5f),
                  one = make_float2(1.0f, 1.0f), two = make_float2(2.0f, 2.0f),
-                 ih = make_float2(p.inv_h, p.inv_h);
+                 ih = make_float2(p.inv_h, p.inv_h), tiny = make_float2(1e-30f, 1e-30f);
     uint32_t j = b;
     for (; j + 1 < e; j += 2) {
         const float4 a = __ldg(spos + j), c = __ldg(spos + j + 1);
@@ -59,14 +61,13 @@ __device__ __forceinline__ void wendland_run(const DevParams &p, const float4 *_
         }
         const float2 rx = __ffma2_rn(ax, m1, px), ry = __ffma2_rn(ay, m1, py), rz = __ffma2_rn(az, m1, pz);
         const float2 d2 = __ffma2_rn(rz, rz, __ffma2_rn(ry, ry, __fmul2_rn(rx, rx)));
-        const float2 rs = make_float2(rsqrtf(fmaxf(d2.x, 1e-30f)), rsqrtf(fmaxf(d2.y, 1e-30f)));
-        float2 q = __fmul2_rn(__fmul2_rn(d2, rs), ih);
-        q = make_float2(fminf(q.x, 2.0f), fminf(q.y, 2.0f));
-        const float2 t = __ffma2_rn(q, half, one);
+        const float2 dt = __fadd2_rn(d2, tiny);  // d2 = 0 (the particle itself) gives q = 0
+        const float2 rs = make_float2(rsqrtf(dt.x), rsqrtf(dt.y));
+        const float2 q = __fmul2_rn(__fmul2_rn(d2, rs), ih);
+        float2 t = __ffma2_rn(q, half, one);
+        t = make_float2(fmaxf(t.x, 0.0f), fmaxf(t.y, 0.0f));  // 0 outside the support (q >= 2)
         const float2 t2 = __fmul2_rn(t, t);
-        float2 w = __fmul2_rn(__fmul2_rn(t2, t2), __ffma2_rn(q, two, one));
-        w.x = (d2.x < p.support2) ? w.x : 0.0f;
-        w.y = (d2.y < p.support2) ? w.y : 0.0f;
+        const float2 w = __fmul2_rn(__fmul2_rn(t2, t2), __ffma2_rn(q, two, one));
         acc = __fadd2_rn(acc, w);
         if (LIST && record) {
             if (interacts<SYS, TRIM>(p, d2.x, a.w, j, i)) list_append(nl, i, cnt, j | code);
@@ -77,10 +78,10 @@ __device__ __forceinline__ void wendland_run(const DevParams &p, const float4 *_
         const float4 pj = __ldg(spos + j);
         const float3 r = rel<SYS>(pi, pj, sx, sy, sz);
         const float d2 = __fmaf_rn(r.z, r.z, __fmaf_rn(r.y, r.y, __fmul_rn(r.x, r.x)));
-        const float q = fminf(__fmul_rn(__fmul_rn(d2, rsqrtf(fmaxf(d2, 1e-30f))), p.inv_h), 2.0f);
-        const float t = __fmaf_rn(q, -0.5f, 1.0f), t2 = __fmul_rn(t, t);
+        const float q = __fmul_rn(__fmul_rn(d2, rsqrtf(__fadd_rn(d2, 1e-30f))), p.inv_h);
+        const float t = fmaxf(__fmaf_rn(q, -0.5f, 1.0f), 0.0f), t2 = __fmul_rn(t, t);
         const float w = __fmul_rn(__fmul_rn(t2, t2), __fmaf_rn(q, 2.0f, 1.0f));
-        acc.x = __fadd_rn(acc.x, (d2 < p.support2) ? w : 0.0f);
+        acc.x = __fadd_rn(acc.x, w);
         if (LIST && record && interacts<SYS, TRIM>(p, d2, pj.w, j, i)) list_append(nl, i, cnt, j | code);
     }
 }

@@ -95,6 +95,8 @@ __global__ void __launch_bounds__(256, 4)
         const float4 vi = svel[i];
         const float2 ai = aux[i];
         const float pterm = ai.x;
+        const float nmass = -p.mass;               // pressure factor
+        const float visc_i = p.visc_coeff * ai.y;  // viscous factor of particle i
         const int3 g = grid_pos(p, pi.x, pi.y, pi.z);
         // Peristalsis no-slip walls: the interfaces as seen by this fluid particle
         const bool noslip = SYS == CMAG_PERISTALSIS && p.wall_noslip && pi.w == 0.0f;
@@ -128,7 +130,7 @@ __global__ void __launch_bounds__(256, 4)
                     if (!(d2 < p.support2)) return;
                     // pressure + Monaghan viscosity (fluid_kernel.cu:221-237)
                     const float inv_d = rsqrtf(d2);
-                    const float temp = kernel_dw(p, d2 * inv_d * p.inv_h);
+                    const float g = kernel_dw_over_r(p, d2 * inv_d * p.inv_h, inv_d);  // dW/dr / r
                     const float2 aj = __ldg(aux + j);
                     float s = pterm + aj.x;
                     const float4 vj = __ldg(svel + j);
@@ -138,14 +140,14 @@ __global__ void __launch_bounds__(256, 4)
                         const float nu = __fdividef(p.av_coeff, ai.y + aj.y);
                         s -= __fdividef(nu * vij, d2 + p.av_eps2);
                     }
-                    s *= -p.mass * temp * inv_d;
+                    s *= nmass * g;
                     ax = __fmaf_rn(s, rx, ax); ay = __fmaf_rn(s, ry, ay); az = __fmaf_rn(s, rz, az);
                 } else if (SYS == CMAG_POISEUILLE) {
                     if (!(d2 < p.support2)) return;
                     // pressure + Morris viscosity with wall extrapolation
                     // (poiseuilleFlowKernel.cu:184-208, 236-245)
                     const float inv_d = rsqrtf(d2);
-                    const float temp = kernel_dw(p, d2 * inv_d * p.inv_h);
+                    const float g = kernel_dw_over_r(p, d2 * inv_d * p.inv_h, inv_d);
                     const float2 aj = __ldg(aux + j);
                     const float4 vj = __ldg(svel + j);
                     float vx, vy, vz;
@@ -158,8 +160,8 @@ __global__ void __launch_bounds__(256, 4)
                     } else {
                         vx = vi.x - vj.x; vy = vi.y - vj.y; vz = vi.z - vj.z;
                     }
-                    const float sp = -p.mass * (pterm + aj.x) * temp * inv_d;
-                    const float sv = p.visc_coeff * temp * ai.y * aj.y * inv_d;
+                    const float sp = nmass * g * (pterm + aj.x);
+                    const float sv = visc_i * aj.y * g;
                     ax = __fmaf_rn(sv, vx, __fmaf_rn(sp, rx, ax));
                     ay = __fmaf_rn(sv, vy, __fmaf_rn(sp, ry, ay));
                     az = __fmaf_rn(sv, vz, __fmaf_rn(sp, rz, az));
@@ -168,10 +170,10 @@ __global__ void __launch_bounds__(256, 4)
                     // viscous (PeristalsisViscousForce.cu:206-213) and pressure
                     // (PeristalsisPressureForce.cu:39-43) from one pass
                     const float inv_d = rsqrtf(d2);
-                    const float temp = kernel_dw(p, d2 * inv_d * p.inv_h);
+                    const float g = kernel_dw_over_r(p, d2 * inv_d * p.inv_h, inv_d);
                     const float2 aj = __ldg(aux + j);
                     const float4 vj = __ldg(svel + j);
-                    const float sv = p.visc_coeff * temp * ai.y * aj.y * inv_d;
+                    const float sv = visc_i * aj.y * g;
                     float dvx = vi.x - vj.x, dvy = vi.y - vj.y, dvz = vi.z - vj.z;
                     if (noslip && pj.w != 0.0f) {
                         const WallSide &w = pj.w > 0.0f ? wb : wt;
@@ -184,7 +186,7 @@ __global__ void __launch_bounds__(256, 4)
                     ax = __fmaf_rn(sv, dvx, ax);
                     ay = __fmaf_rn(sv, dvy, ay);
                     az = __fmaf_rn(sv, dvz, az);
-                    const float sp = -p.mass * temp * (pterm + aj.x) * inv_d;
+                    const float sp = nmass * g * (pterm + aj.x);
                     bx = __fmaf_rn(sp, rx, bx); by = __fmaf_rn(sp, ry, by); bz = __fmaf_rn(sp, rz, bz);
                 }
             };

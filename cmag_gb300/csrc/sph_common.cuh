@@ -36,6 +36,7 @@ struct DevParams {
     int32_t lj_cutoff;
     float av_alpha, av_eps2;      // artificial viscosity alpha, 0.001 h^2
     float w_norm, dw_norm;        // kernel normalisations (see kernel_w/kernel_dw)
+    float dwr_norm;               // Wendland dW/dr / r = dwr_norm (1 - q/2)^3 (kernel_dw_over_r)
     float wall_bottom, wall_top;  // Poiseuille extrapolation lines
     float amplitude, wave_k, wave_speed, half_fluid_h;  // Peristalsis wall law
     float half_world_x;
@@ -176,6 +177,18 @@ __device__ __forceinline__ float kernel_dw(const DevParams &p, float q)
     if (q < 1.0f) return p.dw_norm * (-3.0f * q + 2.25f * q * q);
     float t = 2.0f - q;
     return p.dw_norm * (-0.75f * t * t);
+}
+
+// dW/dr / r for 0 < q < 2 (q = r / h, inv_r = 1 / r).  Wendland: since q / r =
+// 1 / h, -2.5 dw_norm q (1-q/2)^3 / r = dwr_norm (1-q/2)^3 with dwr_norm =
+// -2.5 dw_norm / h (one multiply instead of three).
+__device__ __forceinline__ float kernel_dw_over_r(const DevParams &p, float q, float inv_r)
+{
+    if (p.kernel == CMAG_KERNEL_WENDLAND) {
+        const float t = __fmaf_rn(q, -0.5f, 1.0f);
+        return p.dwr_norm * (t * t * t);
+    }
+    return kernel_dw(p, q) * inv_r;
 }
 
 // Equation of state (fluid_kernel.cu:168, poiseuilleFlowKernel.cu:181,
