@@ -35,15 +35,13 @@ sys.path.insert(0, HERE)
 METRIC = "particle-updates/s"
 
 # Algorithmic bytes per particle and stage (float4 arrays read or written once,
-# neighbour re-reads counted once, P = radix passes).
+# neighbour re-reads counted once; cell-table terms left out).  hash: position in,
+# hash, rank and the cell count; sort (counting sort): hash + rank in, hash + index
+# out, then hash + index in, index out.
 STAGE_BYTES = {
-    "hash": 24, "reorder": 72, "density": 32,
+    "hash": 28, "sort": 28, "reorder": 72, "density": 32,
     "force": {0: 68, 1: 68, 2: 120}, "integrate": {0: 112, 1: 112, 2: 128},
 }
-
-
-def sort_bytes(passes):
-    return 4 + 16 * passes
 
 
 # Algorithmic flops of the neighbour loops: 10 per candidate (distance test) and
@@ -269,9 +267,8 @@ def make_batched(rank, world):
            "nu": "log-uniform [1e-6, 1e-4] (Poiseuille; body force scaled with nu)",
            "particles": run.n, "fluid": int(sum(run.F)), "table_cells": run.table_cells,
            "launch_groups": len(groups), "steps_per_graph": 10, "kernel": "wendland-2d"}
-    passes = max(1, (int(np.ceil(np.log2(max(run.table_cells, 2)))) + 7) // 8)
-    meta = {"passes": passes, "force_b": 68, "integrate_b": 112,
-            "launches": 1 + 1 + passes + 1 + 2 * len(groups) + 1}
+    meta = {"force_b": 68, "integrate_b": 112,
+            "launches": 1 + 3 + 2 + 1 + 2 * len(groups) + 1}
     return run, run.n, int(sum(run.F)), cfg, meta
 
 
@@ -524,10 +521,11 @@ def main():
         s, p, n, fluid, cfg = make_workload(args.workload)
         cfg["parallelism"] = "replicas%d" % world
         cells = p.num_grid_cells
-        passes = max(1, (int(np.ceil(np.log2(max(cells, 2)))) + 7) // 8)
-        meta = {"passes": passes, "force_b": STAGE_BYTES["force"][p.system],
+        meta = {"force_b": STAGE_BYTES["force"][p.system],
                 "integrate_b": STAGE_BYTES["integrate"][p.system],
-                "launches": {0: 4 + passes + 3, 1: 4 + passes + 3, 2: 6 + passes + 3}[p.system]}
+                # hash, 3 scan, 2 sort, reorder, density, force, integrate (+ phase and
+                # boundary configuration for Peristalsis)
+                "launches": {0: 10, 1: 10, 2: 12}[p.system]}
     cfg["l2"] = "inputs larger than L2 (working set %.0f MB)" % ((n * (7 * 16 + 4 * 4) + 8 * cells) / 1e6)
 
     # warm-up (graph capture happens on the first step), then pick the lanes per
@@ -561,7 +559,7 @@ def main():
     names = ["hash", "sort", "reorder", "density", "force", "integrate"]
     per_stage = {nm: stage_ms[k] / max(tsteps, 1) for k, nm in enumerate(names)}
     dom = max(per_stage, key=per_stage.get)
-    bytes_pp = {"hash": STAGE_BYTES["hash"], "sort": sort_bytes(meta["passes"]),
+    bytes_pp = {"hash": STAGE_BYTES["hash"], "sort": STAGE_BYTES["sort"],
                 "reorder": STAGE_BYTES["reorder"], "density": STAGE_BYTES["density"],
                 "force": meta["force_b"], "integrate": meta["integrate_b"]}
     peak, peak_kind = load_peaks()
@@ -598,9 +596,7 @@ def main():
         get = lambda a: s.download(a, host[a])  # noqa: E731
     else:
         put = lambda a: s.setArray(a, host[a])  # noqa: E731
-
-        def get(a):
-            host[a][:] = s.getArray(a)
+        get = lambda a: s.getArray(a, out=host[a])  # noqa: E731
     for a in arrays:
         get(a)
     e2e_steps = max(1, min(args.steps, 20 if batched else 50))

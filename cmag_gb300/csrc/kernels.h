@@ -102,6 +102,8 @@ void launch_fluid_extent(int32_t system, const float4 *pos, uint32_t n, uint32_t
 // per-scene extents of a batch: out[6 s ..] as out6 above (initialised the same way)
 void launch_fluid_extents_batch(const BatchView &bv, const float4 *pos, uint32_t *out,
                                 cudaStream_t st);
+// *flag = 1 when some a[i].z (i < n) differs from z, else 0.
+void launch_z_differs(const float4 *a, uint32_t n, float z, uint32_t *flag, cudaStream_t st);
 void launch_fluid_sum(int32_t system, const float4 *type_src, const float4 *a, uint32_t n,
                       double *sums4, unsigned long long *count, cudaStream_t st);
 

@@ -121,6 +121,16 @@ uint32_t blocks_for(uint32_t n)
     return b < 1 ? 1 : (b > 1216 ? 1216 : b);
 }
 
+// *flag |= 1 when some element's z differs from z (a NaN differs from everything).
+__global__ void __launch_bounds__(256)
+    k_z_differs(const float4 *__restrict__ a, uint32_t n, float z, uint32_t *__restrict__ flag)
+{
+    bool differs = false;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        differs |= a[i].z != z;
+    if (__any_sync(0xffffffffu, differs) && (threadIdx.x & 31) == 0) atomicOr(flag, 1u);
+}
+
 }  // namespace
 
 void launch_fluid_extent(int32_t system, const float4 *pos, uint32_t n, uint32_t *out6,
@@ -138,6 +148,12 @@ void launch_fluid_sum(int32_t system, const float4 *type_src, const float4 *a, u
                       double *sums4, unsigned long long *count, cudaStream_t st)
 {
     k_fluid_sum<<<blocks_for(n), 256, 0, st>>>(system, type_src, a, n, sums4, count);
+}
+
+void launch_z_differs(const float4 *a, uint32_t n, float z, uint32_t *flag, cudaStream_t st)
+{
+    cudaMemsetAsync(flag, 0, sizeof(uint32_t), st);
+    if (n) k_z_differs<<<blocks_for(n), 256, 0, st>>>(a, n, z, flag);
 }
 
 }  // namespace cmag

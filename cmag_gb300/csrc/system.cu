@@ -39,6 +39,7 @@ struct cmag_system {
     uint32_t *ws = nullptr;  // cell scan: per-tile counts and their prefixes
     size_t ws_words = 0;
     uint32_t *err = nullptr;
+    uint32_t *zflag = nullptr;  // set_array: whether uploaded z components differ
     PhaseState *phase = nullptr;
     uint32_t *view_cs = nullptr, *view_ce = nullptr;
     uint32_t *red = nullptr;  // reduction results: 6 extent keys, pad, 4 doubles, 1 count
@@ -510,7 +511,7 @@ void free_all(cmag_system *s)
     void *ptrs[] = {s->pos, s->vel, s->vlf, s->meas, s->acc, s->vforce, s->pforce, s->pred,
                     s->spos, s->svel, s->hash[0], s->hash[1], s->idx[0], s->idx[1], s->cnt,
                     s->off, s->aux, s->ws, s->err, s->phase, s->view_cs, s->view_ce, s->red,
-                    s->closure_x};
+                    s->zflag, s->closure_x};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     free_lists(s);
@@ -685,6 +686,7 @@ int cmag_system_create(const cmag_sph_params *params, uint32_t n, cmag_system **
     step(dalloc(s, &s->phase, sizeof(PhaseState)));
     // 6 extent keys + pad (32 B), 4 doubles (32 B), 1 count (8 B)
     step(dalloc(s, &s->red, 128));
+    step(dalloc(s, &s->zflag, sizeof(uint32_t)));
     if (rc != CMAG_OK) {
         std::string msg = s->last_error;
         free_all(s);
@@ -719,21 +721,31 @@ int cmag_system_set_array(cmag_system *s, int32_t array, const float *host, uint
     if (count == 0) return CMAG_OK;
     CM_CUDA(s, cudaMemcpyAsync(d + start, host, sizeof(float4) * (size_t)count,
                                cudaMemcpyHostToDevice, st_of(s)));
+    // a 2-D scene searches one z layer while its particles share one z and have no
+    // z velocity: check the uploaded z components on the device (3-D scenes never
+    // search one layer)
+    const bool pos_up = array == CMAG_POSITION;
+    const bool vel_up = array == CMAG_VELOCITY || array == CMAG_VELOCITYLEAPFROG;
+    uint32_t differs = 0;
+    const float z0 = pos_up ? host[2] : 0.0f;
+    if (s->p.dims == 2 && (pos_up || vel_up)) {
+        launch_z_differs(d + start, count, z0, s->zflag, st_of(s));
+        CM_CUDA(s, cudaGetLastError());
+        CM_CUDA(s, cudaMemcpyAsync(&differs, s->zflag, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                                   st_of(s)));
+    }
     CM_CUDA(s, cudaStreamSynchronize(st_of(s)));
-    if (array == CMAG_POSITION) {
-        bool uniform = true;
-        const float z0 = host[2];
-        for (uint32_t i = 0; i < count && uniform; ++i) uniform = host[4 * (size_t)i + 2] == z0;
+    if (s->p.dims != 2) {
+        s->z_uniform = false;
+    } else if (pos_up) {
         if (start == 0 && count == s->n) {
-            s->z_uniform = uniform;
+            s->z_uniform = !differs;
             s->z_value = z0;
-        } else if (!uniform || z0 != s->z_value) {
+        } else if (differs || z0 != s->z_value) {
             s->z_uniform = false;
         }
-    } else if (array == CMAG_VELOCITY || array == CMAG_VELOCITYLEAPFROG) {
-        bool nz = false;
-        for (uint32_t i = 0; i < count && !nz; ++i) nz = host[4 * (size_t)i + 2] != 0.0f;
-        if (nz) s->vz_nonzero = true;
+    } else if (vel_up) {
+        if (differs) s->vz_nonzero = true;
         else if (start == 0 && count == s->n && array == CMAG_VELOCITY) s->vz_nonzero = false;
     }
     refresh_layout(s);

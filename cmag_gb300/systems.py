@@ -93,9 +93,14 @@ class _System:
         count = a.shape[0] if count is None else int(count)
         self._chk(lib().cmag_system_set_array(self._h, int(array), _fp(a), int(start), count))
 
-    def getArray(self, array, start=0, count=None):
+    def getArray(self, array, start=0, count=None, out=None):
+        """Copy of a float4 array; into `out` (a C-contiguous float32 (count, 4)
+        array, e.g. pinned host memory) when given."""
         count = self.numParticles - start if count is None else int(count)
-        out = np.empty((count, 4), np.float32)
+        if out is None:
+            out = np.empty((count, 4), np.float32)
+        elif out.dtype != np.float32 or out.shape != (count, 4) or not out.flags.c_contiguous:
+            raise ValueError("out must be a C-contiguous float32 array of shape (%d, 4)" % count)
         self._chk(lib().cmag_system_get_array(self._h, int(array), _fp(out), int(start), count))
         return out
 
