@@ -1211,7 +1211,10 @@ int cmag_system_autotune(cmag_system *s, int32_t reps)
         const float lf = timed([&] {
             launch_force(d, BatchView{}, 1, s->spos, s->svel, s->aux, sorted_idx(s), s->off, fa, fb, s->phase, nl, st);
         });
-        lists = ld + lf < best_d + best_f;
+        // the walk's force cost grows as the flow develops (viscosity terms switch on,
+        // branches diverge over candidates outside the support) while the lists'
+        // does not: keep the lists unless they are clearly slower now
+        lists = ld + lf < 1.03f * (best_d + best_f);
         if (!lists) free_lists(s);
     } else if (had_lists) {
         (void)cudaGetLastError();
