@@ -38,7 +38,7 @@ using walk::shift_code;
 // instruction on sm_100+), scalar tail.  Adds max(1 - q/2, 0)^4 (2q + 1): zero
 // outside the support without a compare and select (the loop is bound by the
 // integer/compare pipe, not by FP32).
-template <int SYS, bool TRIM, bool LIST>
+template <int SYS, bool PLANAR, bool TRIM, bool LIST>
 __device__ __forceinline__ void wendland_run(const DevParams &p, const float4 *__restrict__ spos,
                                              uint32_t b, uint32_t e, float4 pi, float sx, float sy,
                                              float sz, float2 &acc, bool record, uint32_t i,
@@ -59,8 +59,11 @@ __device__ __forceinline__ void wendland_run(const DevParams &p, const float4 *_
             ay = __fadd2_rn(ay, make_float2(sy, sy));
             az = __fadd2_rn(az, make_float2(sz, sz));
         }
-        const float2 rx = __ffma2_rn(ax, m1, px), ry = __ffma2_rn(ay, m1, py), rz = __ffma2_rn(az, m1, pz);
-        const float2 d2 = __ffma2_rn(rz, rz, __ffma2_rn(ry, ry, __fmul2_rn(rx, rx)));
+        const float2 rx = __ffma2_rn(ax, m1, px), ry = __ffma2_rn(ay, m1, py);
+        // planar scenes: all z equal, rz = 0 exactly, left out (same bits)
+        const float2 dxy = __ffma2_rn(ry, ry, __fmul2_rn(rx, rx));
+        const float2 rz = __ffma2_rn(az, m1, pz);
+        const float2 d2 = PLANAR ? dxy : __ffma2_rn(rz, rz, dxy);
         const float2 dt = __fadd2_rn(d2, tiny);  // d2 = 0 (the particle itself) gives q = 0
         const float2 rs = make_float2(rsqrtf(dt.x), rsqrtf(dt.y));
         const float2 q = __fmul2_rn(__fmul2_rn(d2, rs), ih);
@@ -77,7 +80,8 @@ __device__ __forceinline__ void wendland_run(const DevParams &p, const float4 *_
     if (j < e) {  // the same operations as one half of a pair step
         const float4 pj = __ldg(spos + j);
         const float3 r = rel<SYS>(pi, pj, sx, sy, sz);
-        const float d2 = __fmaf_rn(r.z, r.z, __fmaf_rn(r.y, r.y, __fmul_rn(r.x, r.x)));
+        const float dxy = __fmaf_rn(r.y, r.y, __fmul_rn(r.x, r.x));
+        const float d2 = PLANAR ? dxy : __fmaf_rn(r.z, r.z, dxy);
         const float q = __fmul_rn(__fmul_rn(d2, rsqrtf(__fadd_rn(d2, 1e-30f))), p.inv_h);
         const float t = fmaxf(__fmaf_rn(q, -0.5f, 1.0f), 0.0f), t2 = __fmul_rn(t, t);
         const float w = __fmul_rn(__fmul_rn(t2, t2), __fmaf_rn(q, 2.0f, 1.0f));
@@ -115,7 +119,7 @@ __global__ void __launch_bounds__(256, 6)
             for_each_run<SYS, PLANAR, TRIM, G>(
                 p, off, lane, g, frac_cell(p, pi),
                 [&](uint32_t b, uint32_t e, float sx, float sy, float sz) {
-                    wendland_run<SYS, TRIM, LIST>(p, spos, b, e, pi, sx, sy, sz, acc, record, i, nl, cnt);
+                    wendland_run<SYS, PLANAR, TRIM, LIST>(p, spos, b, e, pi, sx, sy, sz, acc, record, i, nl, cnt);
                 });
             sum = p.w_norm * (acc.x + acc.y);
         } else {
@@ -123,7 +127,8 @@ __global__ void __launch_bounds__(256, 6)
                 p, off, lane, g, frac_cell(p, pi), [&](uint32_t j, float sx, float sy, float sz) {
                     const float4 pj = __ldg(spos + j);
                     const float3 r = rel<SYS>(pi, pj, sx, sy, sz);
-                    const float d2 = __fmaf_rn(r.z, r.z, __fmaf_rn(r.y, r.y, __fmul_rn(r.x, r.x)));
+                    const float dxy = __fmaf_rn(r.y, r.y, __fmul_rn(r.x, r.x));
+                    const float d2 = PLANAR ? dxy : __fmaf_rn(r.z, r.z, dxy);
                     // evaluated for every candidate and selected: no divergent branch
                     const float w = kernel_w(p, fminf(d2 * rsqrtf(fmaxf(d2, 1e-30f)) * p.inv_h, 2.0f));
                     sum += (d2 < p.support2) ? w : 0.0f;

@@ -111,8 +111,11 @@ __global__ void __launch_bounds__(256, 4)
         auto pair = [&](uint32_t j, const float4 &pj, float sx, float sy, float sz) {
                 if (j == i) return;
                 const float3 rv = rel<SYS>(pi, pj, sx, sy, sz);
-                const float rx = rv.x, ry = rv.y, rz = rv.z;
-                const float d2 = __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, rx * rx));
+                // planar scenes: every particle has the same z and no z velocity, so
+                // each z term is an exact zero and is left out (same bits)
+                const float rx = rv.x, ry = rv.y, rz = PLANAR ? 0.0f : rv.z;
+                const float d2 = PLANAR ? __fmaf_rn(ry, ry, rx * rx)
+                                        : __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, rx * rx));
                 // a coincident pair has no direction (the reference's terms turn into
                 // NaN there: 0 * inf); it contributes nothing
                 if (d2 == 0.0f) return;
@@ -124,7 +127,8 @@ __global__ void __launch_bounds__(256, 4)
                         const float a2 = p.lj_a2 * inv_d2;
                         const float a6 = a2 * a2 * a2;
                         const float s = p.lj_D * __fmaf_rn(a6, a6, -a6) * inv_d2;
-                        ax = __fmaf_rn(s, rx, ax); ay = __fmaf_rn(s, ry, ay); az = __fmaf_rn(s, rz, az);
+                        ax = __fmaf_rn(s, rx, ax); ay = __fmaf_rn(s, ry, ay);
+                        if (!PLANAR) az = __fmaf_rn(s, rz, az);
                         return;
                     }
                     if (!(d2 < p.support2)) return;
@@ -134,14 +138,15 @@ __global__ void __launch_bounds__(256, 4)
                     const float2 aj = __ldg(aux + j);
                     float s = pterm + aj.x;
                     const float4 vj = __ldg(svel + j);
-                    const float vij =
-                        __fmaf_rn(vi.z - vj.z, rz, __fmaf_rn(vi.y - vj.y, ry, (vi.x - vj.x) * rx));
+                    const float vxy = __fmaf_rn(vi.y - vj.y, ry, (vi.x - vj.x) * rx);
+                    const float vij = PLANAR ? vxy : __fmaf_rn(vi.z - vj.z, rz, vxy);
                     if (vij < 0.0f) {
                         const float nu = __fdividef(p.av_coeff, ai.y + aj.y);
                         s -= __fdividef(nu * vij, d2 + p.av_eps2);
                     }
                     s *= nmass * g;
-                    ax = __fmaf_rn(s, rx, ax); ay = __fmaf_rn(s, ry, ay); az = __fmaf_rn(s, rz, az);
+                    ax = __fmaf_rn(s, rx, ax); ay = __fmaf_rn(s, ry, ay);
+                    if (!PLANAR) az = __fmaf_rn(s, rz, az);
                 } else if (SYS == CMAG_POISEUILLE) {
                     if (!(d2 < p.support2)) return;
                     // pressure + Morris viscosity with wall extrapolation
@@ -164,7 +169,7 @@ __global__ void __launch_bounds__(256, 4)
                     const float sv = visc_i * aj.y * g;
                     ax = __fmaf_rn(sv, vx, __fmaf_rn(sp, rx, ax));
                     ay = __fmaf_rn(sv, vy, __fmaf_rn(sp, ry, ay));
-                    az = __fmaf_rn(sv, vz, __fmaf_rn(sp, rz, az));
+                    if (!PLANAR) az = __fmaf_rn(sv, vz, __fmaf_rn(sp, rz, az));
                 } else {
                     if (!(d2 < p.support2)) return;
                     // viscous (PeristalsisViscousForce.cu:206-213) and pressure
@@ -185,9 +190,10 @@ __global__ void __launch_bounds__(256, 4)
                     }
                     ax = __fmaf_rn(sv, dvx, ax);
                     ay = __fmaf_rn(sv, dvy, ay);
-                    az = __fmaf_rn(sv, dvz, az);
+                    if (!PLANAR) az = __fmaf_rn(sv, dvz, az);
                     const float sp = nmass * g * (pterm + aj.x);
-                    bx = __fmaf_rn(sp, rx, bx); by = __fmaf_rn(sp, ry, by); bz = __fmaf_rn(sp, rz, bz);
+                    bx = __fmaf_rn(sp, rx, bx); by = __fmaf_rn(sp, ry, by);
+                    if (!PLANAR) bz = __fmaf_rn(sp, rz, bz);
                 }
             };
         const uint32_t cnt = LIST ? __ldg(nl.count + i) : 0u;
