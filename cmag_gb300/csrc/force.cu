@@ -196,11 +196,65 @@ __global__ void __launch_bounds__(256, 4)
                     if (!PLANAR) bz = __fmaf_rn(sp, rz, bz);
                 }
             };
+        // DamBreak list entries j0, j1 that are both fluid: the pair terms of both in
+        // paired FP32, each operation the scalar pair's (same bits), added to the
+        // sums in list order
+        auto fluid_pair2 = [&](uint32_t j0, const float4 &q0, uint32_t j1, const float4 &q1) {
+            const float2 rx = __fadd2_rn(make_float2(pi.x, pi.x), make_float2(-q0.x, -q1.x));
+            const float2 ry = __fadd2_rn(make_float2(pi.y, pi.y), make_float2(-q0.y, -q1.y));
+            const float2 rz = __fadd2_rn(make_float2(pi.z, pi.z), make_float2(-q0.z, -q1.z));
+            const float2 dxy = __ffma2_rn(ry, ry, __fmul2_rn(rx, rx));
+            const float2 d2 = PLANAR ? dxy : __ffma2_rn(rz, rz, dxy);
+            if (!(d2.x > 0.0f && d2.y > 0.0f && d2.x < p.support2 && d2.y < p.support2)) {
+                pair(j0, q0, 0.0f, 0.0f, 0.0f);  // not both plain fluid pairs
+                pair(j1, q1, 0.0f, 0.0f, 0.0f);
+                return;
+            }
+            const float2 inv_d = make_float2(rsqrtf(d2.x), rsqrtf(d2.y));
+            const float2 q = __fmul2_rn(__fmul2_rn(d2, inv_d), make_float2(p.inv_h, p.inv_h));
+            const float2 t = __ffma2_rn(q, make_float2(-0.5f, -0.5f), make_float2(1.0f, 1.0f));
+            const float2 g = __fmul2_rn(make_float2(p.dwr_norm, p.dwr_norm), __fmul2_rn(__fmul2_rn(t, t), t));
+            const float2 a0 = __ldg(aux + j0), a1 = __ldg(aux + j1);
+            const float4 v0 = __ldg(svel + j0), v1 = __ldg(svel + j1);
+            float2 sp = __fadd2_rn(make_float2(pterm, pterm), make_float2(a0.x, a1.x));
+            const float2 dvx = __fadd2_rn(make_float2(vi.x, vi.x), make_float2(-v0.x, -v1.x));
+            const float2 dvy = __fadd2_rn(make_float2(vi.y, vi.y), make_float2(-v0.y, -v1.y));
+            const float2 vxy = __ffma2_rn(dvy, ry, __fmul2_rn(dvx, rx));
+            const float2 vij = PLANAR ? vxy
+                                      : __ffma2_rn(__fadd2_rn(make_float2(vi.z, vi.z), make_float2(-v0.z, -v1.z)), rz, vxy);
+            if (vij.x < 0.0f) {
+                const float nu = __fdividef(p.av_coeff, ai.y + a0.y);
+                sp.x -= __fdividef(nu * vij.x, d2.x + p.av_eps2);
+            }
+            if (vij.y < 0.0f) {
+                const float nu = __fdividef(p.av_coeff, ai.y + a1.y);
+                sp.y -= __fdividef(nu * vij.y, d2.y + p.av_eps2);
+            }
+            sp = __fmul2_rn(sp, __fmul2_rn(make_float2(nmass, nmass), g));
+            ax = __fmaf_rn(sp.x, rx.x, ax); ay = __fmaf_rn(sp.x, ry.x, ay);
+            if (!PLANAR) az = __fmaf_rn(sp.x, rz.x, az);
+            ax = __fmaf_rn(sp.y, rx.y, ax); ay = __fmaf_rn(sp.y, ry.y, ay);
+            if (!PLANAR) az = __fmaf_rn(sp.y, rz.y, az);
+        };
         const uint32_t cnt = LIST ? __ldg(nl.count + i) : 0u;
         if (LIST && cnt <= nl.cap) {
             // the density pass's list: the walk's interacting candidates, same order
+            uint32_t k = 0;
+            if (SYS == CMAG_DAMBREAK && p.kernel == CMAG_KERNEL_WENDLAND) {
+                for (; k + 1 < cnt; k += 2) {
+                    const uint32_t j0 = __ldg(nl.entry + (size_t)k * nl.stride + i) & kListIndexMask;
+                    const uint32_t j1 = __ldg(nl.entry + (size_t)(k + 1) * nl.stride + i) & kListIndexMask;
+                    const float4 q0 = __ldg(spos + j0), q1 = __ldg(spos + j1);
+                    if (q0.w == (float)CMAG_FLUID && q1.w == (float)CMAG_FLUID) {
+                        fluid_pair2(j0, q0, j1, q1);
+                    } else {
+                        pair(j0, q0, 0.0f, 0.0f, 0.0f);
+                        pair(j1, q1, 0.0f, 0.0f, 0.0f);
+                    }
+                }
+            }
 #pragma unroll 2
-            for (uint32_t k = 0; k < cnt; ++k) {
+            for (; k < cnt; ++k) {
                 const uint32_t en = __ldg(nl.entry + (size_t)k * nl.stride + i);
                 float sx = 0.0f, sy = 0.0f, sz = 0.0f;
                 if (SYS != CMAG_DAMBREAK) {
