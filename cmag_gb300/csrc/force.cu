@@ -241,9 +241,23 @@ __global__ void __launch_bounds__(256, 4)
             // the density pass's list: the walk's interacting candidates, same order
             uint32_t k = 0;
             if (SYS == CMAG_DAMBREAK && p.kernel == CMAG_KERNEL_WENDLAND) {
+                // the next pair's entries are loaded one step ahead (the force waits on
+                // the chain entry -> position -> velocity and aux data)
+                const uint32_t *ep = nl.entry + i;
+                uint32_t e0 = 0, e1 = 0;
+                if (cnt >= 2) {
+                    e0 = __ldg(ep);
+                    e1 = __ldg(ep + nl.stride);
+                }
                 for (; k + 1 < cnt; k += 2) {
-                    const uint32_t j0 = __ldg(nl.entry + (size_t)k * nl.stride + i) & kListIndexMask;
-                    const uint32_t j1 = __ldg(nl.entry + (size_t)(k + 1) * nl.stride + i) & kListIndexMask;
+                    uint32_t n0 = 0, n1 = 0;
+                    if (k + 3 < cnt) {
+                        n0 = __ldg(ep + (size_t)(k + 2) * nl.stride);
+                        n1 = __ldg(ep + (size_t)(k + 3) * nl.stride);
+                    }
+                    const uint32_t j0 = e0 & kListIndexMask, j1 = e1 & kListIndexMask;
+                    e0 = n0;
+                    e1 = n1;
                     const float4 q0 = __ldg(spos + j0), q1 = __ldg(spos + j1);
                     if (q0.w == (float)CMAG_FLUID && q1.w == (float)CMAG_FLUID) {
                         fluid_pair2(j0, q0, j1, q1);
