@@ -405,12 +405,13 @@ def cpu_run_batched(run, threads, budget_s=20.0):
 def run_learned(args):
     """Learned closure (3-D dam break at 2x the spacing of the fine 64x128x64
     column, 65,536 fluid particles): build training data from fine runs, train on
-    the GPU, then time fine, coarse and coarse + closure runs of a held-out seed to
-    t_end and compare their surge fronts."""
+    the GPU, choose the correction's strength on a validation seed against its
+    fine run, then time fine, coarse and coarse + closure runs of a held-out seed
+    to t_end and compare their surge fronts."""
     import torch
     import cmag_gb300 as cm  # noqa: F401
-    from cmag_gb300.closure import (Closure, Pair, collect, normalization_from, output_limit_from,
-                                    rollout, train)
+    from cmag_gb300.closure import (Closure, Pair, choose_strength, collect, normalization_from,
+                                    output_limit_from, rollout, train)
     from oracle import closure_oracle as CO
     t_end, width = args.t_end, 0.5
     pair = Pair()
@@ -432,12 +433,18 @@ def run_learned(args):
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
     del feat, tgt
+    # the fine run judges the closure on a validation seed: strength of the
+    # correction (0 = plain coarse) with the smallest front error there
+    valid = 998
+    t0 = time.perf_counter()
+    strength, verr = choose_strength(pair, c, valid, t_end, width)
+    t_valid = time.perf_counter() - t0
 
     held = 999
     runs = {}
     for name in ("fine", "coarse", "coarse_closure"):
         sysm = pair.fine if name == "fine" else pair.coarse
-        pair.coarse.set_closure(c if name == "coarse_closure" else None)
+        pair.coarse.set_closure(c if name == "coarse_closure" and strength > 0.0 else None)
         pair.start(held)
         sysm.update_n(3)  # warm-up and graph capture (restarted below)
         pair.start(held)
@@ -465,11 +472,14 @@ def run_learned(args):
                        "coarse_fluid": list(pair.fluid_c), "t_end": t_end,
                        "train_seeds": len(seeds), "snapshots_per_seed": snaps,
                        "train_rows": train_rows, "train_steps": args.train_steps,
-                       "held_out_seed": held, "network": "16-64-64-64-3 SiLU, bf16 params/activations"},
+                       "validation_seed": valid, "held_out_seed": held,
+                       "network": "16-64-64-64-3 SiLU, bf16 params/activations"},
             "learned": {"fine_device_s_to_t_end": runs["fine"]["device_s_to_t_end"],
                         "coarse": out["coarse"], "coarse_closure": out["coarse_closure"],
                         "meets_2pct_front": out["coarse_closure"]["front_err_max"] <= 0.02,
-                        "data_s": t_data, "train_s": t_train, "losses": losses,
+                        "strength": strength,
+                        "validation_front_err": {str(f): [round(a, 4), round(b, 4)] for f, (a, b) in verr.items()},
+                        "data_s": t_data, "train_s": t_train, "validation_s": t_valid, "losses": losses,
                         "fronts": {k: [round(float(v), 4) for v in r["fronts"][::10]] for k, r in runs.items()}}}
     pair.close()
     c.close()

@@ -299,3 +299,38 @@ def collect(pair, seeds, snapshots, every, min_shepard=0.5):
             pair.coarse.update_n(every // 2)
             row += pair.sample(feat_dev, target_dev, row, min_shepard)
     return feat_dev[:row].contiguous(), target_dev[:row].contiguous()
+
+
+def front_errors(fronts, fine_fronts, tank_over_column):
+    """Max and mean relative front error against the fine run while the fine
+    front is short of the far wall."""
+    judged = fine_fronts < 0.95 * tank_over_column
+    err = np.abs(fronts - fine_fronts) / fine_fronts
+    return float(err[judged].max()), float(err[judged].mean())
+
+
+def choose_strength(pair, closure, seed, t_end, column_width, factors=(0.0, 0.25, 0.5, 0.75, 1.0),
+                    sample_dt=0.01):
+    """The fine run judges the closure: on a validation seed (not a training or
+    held-out seed), roll the coarse run out with the correction scaled by each
+    factor (0 = the plain coarse method) and keep the factor whose surge front
+    stays closest to the fine run's (smallest maximum relative error).  Sets the
+    closure's output scale accordingly and returns (factor, {factor: (max, mean)})."""
+    mean, inv, scale = closure.normalization()
+    tank_over_column = pair.tank_f[0] / pair.fluid_f[0]
+    pair.start(seed)
+    _, _, fine = rollout(pair.fine, t_end, sample_dt, column_width)
+    errs = {}
+    for f in factors:
+        pair.start(seed)
+        if f > 0.0:
+            closure.set_normalization(mean, inv, scale * f)
+            pair.coarse.set_closure(closure)
+        else:
+            pair.coarse.set_closure(None)
+        _, _, fr = rollout(pair.coarse, t_end, sample_dt, column_width)
+        errs[f] = front_errors(fr, fine, tank_over_column)
+    pair.coarse.set_closure(None)
+    best = min(factors, key=lambda f: (errs[f][0], errs[f][1]))
+    closure.set_normalization(mean, inv, scale * max(best, 0.0))
+    return best, errs
