@@ -73,8 +73,8 @@ __device__ __forceinline__ void wendland_run(const DevParams &p, const float4 *_
         const float2 w = __fmul2_rn(__fmul2_rn(t2, t2), __ffma2_rn(q, two, one));
         acc = __fadd2_rn(acc, w);
         if (LIST && record) {
-            if (interacts<SYS, TRIM>(p, d2.x, a.w, j, i)) list_append(nl, i, cnt, j | code);
-            if (interacts<SYS, TRIM>(p, d2.y, c.w, j + 1, i)) list_append(nl, i, cnt, (j + 1) | code);
+            if (interacts<SYS, TRIM>(p, d2.x, a.w)) list_append(nl, i, cnt, j | code);
+            if (interacts<SYS, TRIM>(p, d2.y, c.w)) list_append(nl, i, cnt, (j + 1) | code);
         }
     }
     if (j < e) {  // the same operations as one half of a pair step
@@ -86,7 +86,7 @@ __device__ __forceinline__ void wendland_run(const DevParams &p, const float4 *_
         const float t = fmaxf(__fmaf_rn(q, -0.5f, 1.0f), 0.0f), t2 = __fmul_rn(t, t);
         const float w = __fmul_rn(__fmul_rn(t2, t2), __fmaf_rn(q, 2.0f, 1.0f));
         acc.x = __fadd_rn(acc.x, w);
-        if (LIST && record && interacts<SYS, TRIM>(p, d2, pj.w, j, i)) list_append(nl, i, cnt, j | code);
+        if (LIST && record && interacts<SYS, TRIM>(p, d2, pj.w)) list_append(nl, i, cnt, j | code);
     }
 }
 
@@ -132,7 +132,7 @@ __global__ void __launch_bounds__(256, 6)
                     // evaluated for every candidate and selected: no divergent branch
                     const float w = kernel_w(p, fminf(d2 * rsqrtf(fmaxf(d2, 1e-30f)) * p.inv_h, 2.0f));
                     sum += (d2 < p.support2) ? w : 0.0f;
-                    if (LIST && record && interacts<SYS, TRIM>(p, d2, pj.w, j, i))
+                    if (LIST && record && interacts<SYS, TRIM>(p, d2, pj.w))
                         list_append(nl, i, cnt, j | shift_code(sx, sy, sz));
                 });
         }

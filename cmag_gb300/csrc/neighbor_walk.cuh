@@ -153,13 +153,17 @@ __device__ __forceinline__ float3 frac_cell(const DevParams &p, float4 q)
 
 // ---- pieces shared by the density and force loops --------------------------
 
-// Whether the force loop of particle i uses candidate j at squared distance d2
-// (type w): inside the support, or a DamBreak wall without the q < 2 cut-off.
+// Whether the force loop of a particle uses a candidate at squared distance d2
+// (type w): inside the support, 0 < d2 < (2h)^2 (d2 = 0 is the particle itself or
+// a coincident one, which the force skips), or a DamBreak wall without the q < 2
+// cut-off.  d2 is a sum of squares (+0 or positive, or NaN), so the range test is
+// one unsigned compare of the bit patterns.
 template <int SYS, bool TRIM>
-__device__ __forceinline__ bool interacts(const DevParams &p, float d2, float w, uint32_t j, uint32_t i)
+__device__ __forceinline__ bool interacts(const DevParams &p, float d2, float w)
 {
-    const bool far_wall = SYS == CMAG_DAMBREAK && !TRIM && w != (float)CMAG_FLUID;
-    return j != i && d2 > 0.0f && (d2 < p.support2 || far_wall);
+    const bool inside = __float_as_uint(d2) - 1u < __float_as_uint(p.support2) - 1u;
+    if (SYS == CMAG_DAMBREAK && !TRIM) return inside || (w != (float)CMAG_FLUID && d2 > 0.0f);
+    return inside;
 }
 
 // list entry code of a run's image shift: 2 bits per axis, 0/1/2 for -1/0/+1
