@@ -433,6 +433,13 @@ def run_learned(args):
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
     del feat, tgt
+    # each solver at its best for the timed runs: lanes per particle and interaction
+    # lists chosen on a developed flow (t = 0.1 s of the held-out seed)
+    lanes = {}
+    for name, sysm, steps in (("fine", pair.fine, 2000), ("coarse", pair.coarse, 1000)):
+        pair.start(999)
+        sysm.update_n(steps)
+        lanes[name] = list(sysm.autotune(3))
     # the fine run judges the closure on a validation seed: strength of the
     # correction (0 = plain coarse) with the smallest front error there
     valid = 998
@@ -477,7 +484,7 @@ def run_learned(args):
             "learned": {"fine_device_s_to_t_end": runs["fine"]["device_s_to_t_end"],
                         "coarse": out["coarse"], "coarse_closure": out["coarse_closure"],
                         "meets_2pct_front": out["coarse_closure"]["front_err_max"] <= 0.02,
-                        "strength": strength,
+                        "strength": strength, "lanes_density_force_lists": lanes,
                         "validation_front_err": {str(f): [round(a, 4), round(b, 4)] for f, (a, b) in verr.items()},
                         "data_s": t_data, "train_s": t_train, "validation_s": t_valid, "losses": losses,
                         "fronts": {k: [round(float(v), 4) for v in r["fronts"][::10]] for k, r in runs.items()}}}
