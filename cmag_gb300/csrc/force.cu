@@ -236,11 +236,54 @@ __global__ void __launch_bounds__(256, 4)
             ax = __fmaf_rn(sp.y, rx.y, ax); ay = __fmaf_rn(sp.y, ry.y, ay);
             if (!PLANAR) az = __fmaf_rn(sp.y, rz.y, az);
         };
+        // Peristalsis list entries j0, j1 (image shifts s0, s1): both pair terms in
+        // paired FP32, each operation the scalar pair's (same bits), added in order
+        auto peri_pair2 = [&](uint32_t j0, const float4 &q0, float3 s0, uint32_t j1, const float4 &q1,
+                              float3 s1) {
+            const float2 tx = __fadd2_rn(make_float2(q0.x, q1.x), make_float2(s0.x, s1.x));
+            const float2 ty = __fadd2_rn(make_float2(q0.y, q1.y), make_float2(s0.y, s1.y));
+            const float2 tz = __fadd2_rn(make_float2(q0.z, q1.z), make_float2(s0.z, s1.z));
+            const float2 rx = __fadd2_rn(make_float2(pi.x, pi.x), make_float2(-tx.x, -tx.y));
+            const float2 ry = __fadd2_rn(make_float2(pi.y, pi.y), make_float2(-ty.x, -ty.y));
+            const float2 rz = __fadd2_rn(make_float2(pi.z, pi.z), make_float2(-tz.x, -tz.y));
+            const float2 dxy = __ffma2_rn(ry, ry, __fmul2_rn(rx, rx));
+            const float2 d2 = PLANAR ? dxy : __ffma2_rn(rz, rz, dxy);
+            if (!(d2.x > 0.0f && d2.y > 0.0f && d2.x < p.support2 && d2.y < p.support2)) {
+                pair(j0, q0, s0.x, s0.y, s0.z);
+                pair(j1, q1, s1.x, s1.y, s1.z);
+                return;
+            }
+            const float2 inv_d = make_float2(rsqrtf(d2.x), rsqrtf(d2.y));
+            const float2 q = __fmul2_rn(__fmul2_rn(d2, inv_d), make_float2(p.inv_h, p.inv_h));
+            const float2 t = __ffma2_rn(q, make_float2(-0.5f, -0.5f), make_float2(1.0f, 1.0f));
+            const float2 g = __fmul2_rn(make_float2(p.dwr_norm, p.dwr_norm), __fmul2_rn(__fmul2_rn(t, t), t));
+            const float2 a0 = __ldg(aux + j0), a1 = __ldg(aux + j1);
+            const float4 v0 = __ldg(svel + j0), v1 = __ldg(svel + j1);
+            const float2 sv = __fmul2_rn(__fmul2_rn(make_float2(visc_i, visc_i), make_float2(a0.y, a1.y)), g);
+            const float2 dvx = __fadd2_rn(make_float2(vi.x, vi.x), make_float2(-v0.x, -v1.x));
+            const float2 dvy = __fadd2_rn(make_float2(vi.y, vi.y), make_float2(-v0.y, -v1.y));
+            const float2 sp = __fmul2_rn(__fmul2_rn(make_float2(nmass, nmass), g),
+                                         __fadd2_rn(make_float2(pterm, pterm), make_float2(a0.x, a1.x)));
+            ax = __fmaf_rn(sv.x, dvx.x, ax); ay = __fmaf_rn(sv.x, dvy.x, ay);
+            bx = __fmaf_rn(sp.x, rx.x, bx); by = __fmaf_rn(sp.x, ry.x, by);
+            ax = __fmaf_rn(sv.y, dvx.y, ax); ay = __fmaf_rn(sv.y, dvy.y, ay);
+            bx = __fmaf_rn(sp.y, rx.y, bx); by = __fmaf_rn(sp.y, ry.y, by);
+            if (!PLANAR) {
+                az = __fmaf_rn(sv.x, vi.z - v0.z, az); bz = __fmaf_rn(sp.x, rz.x, bz);
+                az = __fmaf_rn(sv.y, vi.z - v1.z, az); bz = __fmaf_rn(sp.y, rz.y, bz);
+            }
+        };
+        // image shift of a list entry (2 bits per axis above the index)
+        auto entry_shift = [&](uint32_t en) {
+            const uint32_t cd = en >> kListIndexBits;
+            return make_float3((float)((int)(cd & 3u) - 1) * p.wsx, (float)((int)((cd >> 2) & 3u) - 1) * p.wsy,
+                               (float)((int)((cd >> 4) & 3u) - 1) * p.wsz);
+        };
         const uint32_t cnt = LIST ? __ldg(nl.count + i) : 0u;
         if (LIST && cnt <= nl.cap) {
             // the density pass's list: the walk's interacting candidates, same order
             uint32_t k = 0;
-            if (SYS == CMAG_DAMBREAK && p.kernel == CMAG_KERNEL_WENDLAND) {
+            if ((SYS == CMAG_DAMBREAK || SYS == CMAG_PERISTALSIS) && p.kernel == CMAG_KERNEL_WENDLAND) {
                 // the next pair's entries are loaded one step ahead (the force waits on
                 // the chain entry -> position -> velocity and aux data)
                 const uint32_t *ep = nl.entry + i;
@@ -256,14 +299,25 @@ __global__ void __launch_bounds__(256, 4)
                         n1 = __ldg(ep + (size_t)(k + 3) * nl.stride);
                     }
                     const uint32_t j0 = e0 & kListIndexMask, j1 = e1 & kListIndexMask;
+                    const uint32_t c0 = e0 >> kListIndexBits, c1 = e1 >> kListIndexBits;
                     e0 = n0;
                     e1 = n1;
                     const float4 q0 = __ldg(spos + j0), q1 = __ldg(spos + j1);
-                    if (q0.w == (float)CMAG_FLUID && q1.w == (float)CMAG_FLUID) {
-                        fluid_pair2(j0, q0, j1, q1);
+                    if (SYS == CMAG_DAMBREAK) {
+                        if (q0.w == (float)CMAG_FLUID && q1.w == (float)CMAG_FLUID) {
+                            fluid_pair2(j0, q0, j1, q1);
+                        } else {
+                            pair(j0, q0, 0.0f, 0.0f, 0.0f);
+                            pair(j1, q1, 0.0f, 0.0f, 0.0f);
+                        }
                     } else {
-                        pair(j0, q0, 0.0f, 0.0f, 0.0f);
-                        pair(j1, q1, 0.0f, 0.0f, 0.0f);
+                        const float3 s0 = entry_shift(c0 << kListIndexBits), s1 = entry_shift(c1 << kListIndexBits);
+                        if (!noslip || (q0.w == 0.0f && q1.w == 0.0f)) {
+                            peri_pair2(j0, q0, s0, j1, q1, s1);
+                        } else {  // wall neighbours of the no-slip extrapolation
+                            pair(j0, q0, s0.x, s0.y, s0.z);
+                            pair(j1, q1, s1.x, s1.y, s1.z);
+                        }
                     }
                 }
             }
