@@ -125,4 +125,5 @@ class BatchGroup(ctypes.Structure):
         ("particles", ctypes.c_uint32),
         ("density_lanes", ctypes.c_int32),
         ("force_lanes", ctypes.c_int32),
+        ("lists", ctypes.c_int32),
     ]

@@ -112,6 +112,7 @@ SIGNATURES = {
     "cmag_batch_group_info": ([c_bat, c_u32, P(BatchGroup)], ctypes.c_int),
     "cmag_batch_scene_group": ([c_bat, c_u32, c_u32p], ctypes.c_int),
     "cmag_batch_set_group_lanes": ([c_bat, c_u32, c_i32, c_i32], ctypes.c_int),
+    "cmag_batch_set_group_lists": ([c_bat, c_u32, c_i32], ctypes.c_int),
     "cmag_batch_autotune": ([c_bat, c_i32], ctypes.c_int),
     "cmag_batch_set_stage_timing": ([c_bat, c_i32], ctypes.c_int),
     "cmag_batch_stage_times": ([c_bat, c_f32p, c_u32p], ctypes.c_int),

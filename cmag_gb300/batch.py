@@ -179,6 +179,11 @@ class Batch:
     def set_group_lanes(self, group, density_lanes, force_lanes):
         self._chk(lib().cmag_batch_set_group_lanes(self._h, int(group), int(density_lanes), int(force_lanes)))
 
+    def set_group_lists(self, group, enable):
+        """Interaction lists for launch group `group` (one lane per particle, the
+        same results as the one-lane cell walk) or the cell walk."""
+        self._chk(lib().cmag_batch_set_group_lists(self._h, int(group), int(bool(enable))))
+
     def autotune(self, reps=3):
         self._chk(lib().cmag_batch_autotune(self._h, int(reps)))
 

@@ -54,6 +54,7 @@ struct LaunchGroup {
     bool planar = false, trim = false;
     uint32_t bucket = 0;
     int g_density = 1, g_force = 1;
+    bool lists = false;  // interaction lists (one lane per particle)
     cudaStream_t side = nullptr;
     cudaEvent_t done = nullptr;
 };
@@ -79,6 +80,10 @@ struct cmag_batch {
     float4 *pos = nullptr, *vel = nullptr, *vlf = nullptr, *meas = nullptr, *acc = nullptr,
            *vforce = nullptr, *pforce = nullptr, *pred = nullptr, *spos = nullptr, *svel = nullptr;
     uint32_t *hash[2] = {nullptr, nullptr}, *idx[2] = {nullptr, nullptr};
+    // interaction lists of the groups that use them: entry k of particle i at
+    // nl_entry[k * n_total + i] (allocated when the autotuner first tries them)
+    uint32_t *nl_entry = nullptr, *nl_count = nullptr;
+    uint32_t nl_cap = 0;
     uint32_t *cnt = nullptr, *off = nullptr, *ws = nullptr, *err = nullptr, *red = nullptr;
     size_t ws_words = 0;
     float2 *aux = nullptr;
@@ -195,6 +200,46 @@ int ensure_events(cmag_batch *b, size_t count)
     return CMAG_OK;
 }
 
+NeighborList lists_of(const cmag_batch *b)
+{
+    NeighborList nl{};
+    if (b->nl_entry) {
+        nl.entry = b->nl_entry;
+        nl.count = b->nl_count;
+        nl.cap = b->nl_cap;
+        nl.stride = b->n_total;
+    }
+    return nl;
+}
+
+void free_lists(cmag_batch *b)
+{
+    if (b->nl_entry) cudaFree(b->nl_entry);
+    if (b->nl_count) cudaFree(b->nl_count);
+    b->nl_entry = b->nl_count = nullptr;
+    b->nl_cap = 0;
+    for (LaunchGroup &g : b->groups) g.lists = false;
+}
+
+// Lists for every particle of the batch, with room for the largest per-scene
+// capacity; returns false when they cannot be had (too many particles or no memory).
+bool alloc_lists(cmag_batch *b)
+{
+    if (b->nl_entry) return true;
+    if (b->n_total >= (1u << kListIndexBits)) return false;
+    uint32_t cap = 0;
+    for (size_t k = 0; k < b->sc.size(); ++k) cap = std::max(cap, list_cap(b->sc[k].p, b->host_dev[k].trim != 0));
+    cudaError_t e = cudaMalloc((void **)&b->nl_entry, sizeof(uint32_t) * (size_t)cap * b->n_total);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&b->nl_count, sizeof(uint32_t) * (size_t)b->n_total);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        free_lists(b);
+        return false;
+    }
+    b->nl_cap = cap;
+    return true;
+}
+
 // Neighbour-loop launches of every group: groups after the first run on side
 // streams forked from the main stream and joined before the next stage.
 int launch_groups(cmag_batch *b, bool force)
@@ -211,12 +256,13 @@ int launch_groups(cmag_batch *b, bool force)
         v.first = lg.first;
         v.count = lg.count;
         const DevParams &rep = b->host_dev[lg.slot_first];
+        const NeighborList nl = lg.lists ? lists_of(b) : NeighborList{};
         if (force) {
             const bool per = lg.system == CMAG_PERISTALSIS;
             launch_force(rep, v, lg.g_force, b->spos, b->svel, b->aux, sorted_idx(b), b->off,
-                         per ? b->vforce : b->acc, per ? b->pforce : nullptr, b->phase, NeighborList{}, gs);
+                         per ? b->vforce : b->acc, per ? b->pforce : nullptr, b->phase, nl, gs);
         } else {
-            launch_density(rep, v, lg.g_density, b->spos, b->off, b->meas, b->aux, NeighborList{}, gs);
+            launch_density(rep, v, lg.g_density, b->spos, b->off, b->meas, b->aux, nl, gs);
         }
         if (g > 0) {
             CB_CUDA(b, cudaEventRecord(lg.done, gs));
@@ -362,6 +408,7 @@ void free_all(cmag_batch *b)
                     b->off, b->ws, b->err, b->red, b->aux, b->phase, b->dev, b->scene_of};
     for (void *p : ptrs)
         if (p) cudaFree(p);
+    free_lists(b);
     if (b->own_stream) cudaStreamDestroy(b->own_stream);
 }
 
@@ -1008,6 +1055,7 @@ int cmag_batch_group_info(cmag_batch *b, uint32_t group, cmag_batch_group *out)
     out->particles = g.count;
     out->density_lanes = g.g_density;
     out->force_lanes = g.g_force;
+    out->lists = g.lists ? 1 : 0;
     return CMAG_OK;
 }
 
@@ -1030,12 +1078,31 @@ int cmag_batch_set_group_lanes(cmag_batch *b, uint32_t group, int32_t density_la
         return bfail(b, CMAG_ERR_INVALID, "lanes per particle must be 1, 2 or 4");
     b->groups[group].g_density = density_lanes;
     b->groups[group].g_force = force_lanes;
+    b->groups[group].lists = false;  // lanes chosen by hand: the cell walk
+    invalidate_graphs(b);
+    return CMAG_OK;
+}
+
+int cmag_batch_set_group_lists(cmag_batch *b, uint32_t group, int32_t enable)
+{
+    if (!b) return bfail(nullptr, CMAG_ERR_INVALID, "null handle");
+    if (group >= b->groups.size()) return bfail(b, CMAG_ERR_INVALID, "group out of range");
+    LaunchGroup &g = b->groups[group];
+    if (enable) {
+        if (!alloc_lists(b))
+            return bfail(b, CMAG_ERR_NOMEM, "interaction lists: no device memory, or 2^26 particles or more");
+        g.lists = true;
+        g.g_density = g.g_force = 1;
+    } else {
+        g.lists = false;
+    }
     invalidate_graphs(b);
     return CMAG_OK;
 }
 
 // Per launch group, time density and force for 1, 2 and 4 lanes per particle on
-// the current state (`reps` launches each) and keep the fastest.
+// the current state (`reps` launches each) and keep the fastest, then try the
+// interaction lists.
 int cmag_batch_autotune(cmag_batch *b, int32_t reps)
 {
     if (!b) return bfail(nullptr, CMAG_ERR_INVALID, "null handle");
@@ -1057,6 +1124,7 @@ int cmag_batch_autotune(cmag_batch *b, int32_t reps)
         const DevParams &rep = b->host_dev[g.slot_first];
         const bool per = g.system == CMAG_PERISTALSIS;
         float4 *fa = per ? b->vforce : b->acc, *fb = per ? b->pforce : nullptr;
+        float walk_ms[2] = {0.0f, 0.0f};
         for (int pass = 0; pass < 2; ++pass) {
             float best = 1e30f;
             int pick = pass == 0 ? g.g_density : g.g_force;
@@ -1081,8 +1149,37 @@ int cmag_batch_autotune(cmag_batch *b, int32_t reps)
             } else {
                 g.g_force = pick;
             }
+            walk_ms[pass] = best;
+        }
+        // interaction lists (one lane per particle, the same bits as the one-lane
+        // walk): kept unless more than 3 % slower on this state, since the walk's
+        // force cost grows as the flow develops
+        g.lists = false;
+        if (alloc_lists(b)) {
+            const NeighborList nl = lists_of(b);
+            auto timed = [&](auto &&run) {
+                run();
+                cudaEventRecord(e0, st);
+                for (int r = 0; r < reps; ++r) run();
+                cudaEventRecord(e1, st);
+                cudaEventSynchronize(e1);
+                float ms = 0;
+                cudaEventElapsedTime(&ms, e0, e1);
+                return ms;
+            };
+            const float ld = timed([&] { launch_density(rep, v, 1, b->spos, b->off, b->meas, b->aux, nl, st); });
+            const float lf = timed([&] {
+                launch_force(rep, v, 1, b->spos, b->svel, b->aux, sorted_idx(b), b->off, fa, fb, b->phase, nl, st);
+            });
+            if (ld + lf < 1.03f * (walk_ms[0] + walk_ms[1])) {
+                g.lists = true;
+                g.g_density = g.g_force = 1;
+            }
         }
     }
+    bool any_lists = false;
+    for (const LaunchGroup &g : b->groups) any_lists |= g.lists;
+    if (!any_lists) free_lists(b);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     CB_CUDA(b, cudaGetLastError());

@@ -233,6 +233,21 @@ SceneLayout layout_for(const cmag_sph_params &p, bool planar, float z_value)
     return l;
 }
 
+// Room per particle in the interaction lists: 1.5 times the lattice neighbour
+// count inside the support (or, with the un-cut DamBreak wall force, every
+// particle of the searched cell box) plus 32.  Particles beyond it walk the cells.
+uint32_t list_cap(const cmag_sph_params &p, bool trim)
+{
+    const double dx = 2.0 * p.particle_radius, s = 2.0 * p.smoothing_radius / dx;
+    const bool planar = p.dims == 2;
+    double expected = planar ? kPi * s * s : 4.0 / 3.0 * kPi * s * s * s;
+    if (!trim) {
+        const double c = 2 * p.cell_count + 1, per = p.cell_size[0] / dx;
+        expected = planar ? c * c * per * per : c * c * c * per * per * per;
+    }
+    return (uint32_t)std::ceil(1.5 * expected) + 32u;
+}
+
 }  // namespace cmag
 
 namespace {
@@ -280,21 +295,6 @@ NeighborList nl_of(const cmag_system *s)
         nl.stride = s->n;
     }
     return nl;
-}
-
-// Room per particle in the interaction lists: 1.5 times the lattice neighbour
-// count inside the support (or, with the un-cut DamBreak wall force, every
-// particle of the searched cell box) plus 32.  Particles beyond it walk the cells.
-uint32_t list_cap(const cmag_sph_params &p, bool trim)
-{
-    const double dx = 2.0 * p.particle_radius, s = 2.0 * p.smoothing_radius / dx;
-    const bool planar = p.dims == 2;
-    double expected = planar ? kPi * s * s : 4.0 / 3.0 * kPi * s * s * s;
-    if (!trim) {
-        const double c = 2 * p.cell_count + 1, per = p.cell_size[0] / dx;
-        expected = planar ? c * c * per * per : c * c * c * per * per * per;
-    }
-    return (uint32_t)std::ceil(1.5 * expected) + 32u;
 }
 
 int free_lists(cmag_system *s)

@@ -271,6 +271,7 @@ public:
     void fluidExtents(float *lo, float *hi) const { chk(cmag_batch_fluid_extents(h_, lo, hi)); }
     void setGraphs(bool enable, uint32_t stepsPerGraph = 1) { chk(cmag_batch_set_graphs(h_, enable ? 1 : 0, stepsPerGraph)); }
     void autotune(int reps = 3) { chk(cmag_batch_autotune(h_, reps)); }
+    void set_group_lists(uint32_t group, bool enable) { chk(cmag_batch_set_group_lists(h_, group, enable ? 1 : 0)); }
     void synchronize() { chk(cmag_batch_synchronize(h_)); }
 
 private:

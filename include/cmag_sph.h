@@ -396,6 +396,7 @@ typedef struct cmag_batch_group {
     uint32_t particles;
     int32_t density_lanes;
     int32_t force_lanes;
+    int32_t lists;           /* 1: interaction lists (one lane per particle) */
 } cmag_batch_group;
 
 int cmag_batch_create(const cmag_sph_params *params, const uint32_t *counts, uint32_t scenes,
@@ -442,6 +443,11 @@ int cmag_batch_group_info(cmag_batch *b, uint32_t group, cmag_batch_group *out);
 int cmag_batch_scene_group(cmag_batch *b, uint32_t scene, uint32_t *group);
 int cmag_batch_set_group_lanes(cmag_batch *b, uint32_t group, int32_t density_lanes,
                                int32_t force_lanes);
+/* Interaction lists for one launch group (enable 1) or the cell walk (0): the
+ * density pass records each particle's neighbours and the force pass reads
+ * them; one lane per particle, the same results as the one-lane walk.  No
+ * reference counterpart (the reference walks the cells in both passes). */
+int cmag_batch_set_group_lists(cmag_batch *b, uint32_t group, int32_t enable);
 /* per launch group, the fastest lanes per particle for density and force */
 int cmag_batch_autotune(cmag_batch *b, int32_t reps);
 int cmag_batch_set_stage_timing(cmag_batch *b, int32_t enable);

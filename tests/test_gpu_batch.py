@@ -201,6 +201,37 @@ def test_batch_autotuned_lanes(gpu):
     batch.close()
 
 
+def test_batch_interaction_lists_bit_exact(gpu):
+    """Every launch group on interaction lists: each scene equals its twin on the
+    one-lane cell walk after 20 graph-replayed steps (dam breaks released part-way)."""
+    batch, singles, scenes = build_pair()
+    for gi in range(len(batch.groups())):
+        batch.set_group_lists(gi, True)
+    for g in batch.groups():
+        assert g["lists"] == 1 and g["density_lanes"] == 1 and g["force_lanes"] == 1
+    for s in singles:
+        s.set_groups(1, 1)
+    batch.set_graphs(True, 4)
+    batch.update_n(8)
+    for s in singles:
+        s.update_n(8)
+    for k, (p, _, pos) in enumerate(scenes):
+        if p.system == _abi.DAMBREAK and pos is None:
+            batch.dambreak_remove_right_boundary(k)
+            singles[k].removeRightBoundary()
+    batch.update_n(12)
+    for s in singles:
+        s.update_n(12)
+    batch.synchronize()
+    for k, s in enumerate(singles):
+        assert_scene_equal(batch, k, s, what="lists")
+    assert batch.device_error_bits() == 0
+    # back to the walk
+    batch.set_group_lists(0, False)
+    assert batch.groups()[0]["lists"] == 0
+    batch.close()
+
+
 def test_batch_set_params_and_planar_checks(gpu):
     scenes = mixed_scenes()
     batch = Batch([s[0] for s in scenes], [s[1] for s in scenes])
