@@ -273,6 +273,46 @@ __global__ void __launch_bounds__(256, 4)
                 az = __fmaf_rn(sv.y, vi.z - v1.z, az); bz = __fmaf_rn(sp.y, rz.y, bz);
             }
         };
+        // Poiseuille list entries j0, j1 (x image shifts sx0, sx1) outside the wall
+        // extrapolation: both pair terms in paired FP32, each operation the scalar
+        // pair's (same bits), added in order
+        auto poi_pair2 = [&](uint32_t j0, const float4 &q0, float sx0, uint32_t j1, const float4 &q1,
+                             float sx1) {
+            const float2 tx = __fadd2_rn(make_float2(q0.x, q1.x), make_float2(sx0, sx1));
+            const float2 rx = __fadd2_rn(make_float2(pi.x, pi.x), make_float2(-tx.x, -tx.y));
+            const float2 ry = __fadd2_rn(make_float2(pi.y, pi.y), make_float2(-q0.y, -q1.y));
+            const float2 rz = __fadd2_rn(make_float2(pi.z, pi.z), make_float2(-q0.z, -q1.z));
+            const float2 dxy = __ffma2_rn(ry, ry, __fmul2_rn(rx, rx));
+            const float2 d2 = PLANAR ? dxy : __ffma2_rn(rz, rz, dxy);
+            if (!(d2.x > 0.0f && d2.y > 0.0f && d2.x < p.support2 && d2.y < p.support2)) {
+                pair(j0, q0, sx0, 0.0f, 0.0f);
+                pair(j1, q1, sx1, 0.0f, 0.0f);
+                return;
+            }
+            const float2 inv_d = make_float2(rsqrtf(d2.x), rsqrtf(d2.y));
+            const float2 q = __fmul2_rn(__fmul2_rn(d2, inv_d), make_float2(p.inv_h, p.inv_h));
+            const float2 t = __ffma2_rn(q, make_float2(-0.5f, -0.5f), make_float2(1.0f, 1.0f));
+            const float2 g = __fmul2_rn(make_float2(p.dwr_norm, p.dwr_norm), __fmul2_rn(__fmul2_rn(t, t), t));
+            const float2 a0 = __ldg(aux + j0), a1 = __ldg(aux + j1);
+            const float4 v0 = __ldg(svel + j0), v1 = __ldg(svel + j1);
+            const float2 vx = __fadd2_rn(make_float2(vi.x, vi.x), make_float2(-v0.x, -v1.x));
+            const float2 vy = __fadd2_rn(make_float2(vi.y, vi.y), make_float2(-v0.y, -v1.y));
+            const float2 sp = __fmul2_rn(__fmul2_rn(make_float2(nmass, nmass), g),
+                                         __fadd2_rn(make_float2(pterm, pterm), make_float2(a0.x, a1.x)));
+            const float2 sv = __fmul2_rn(__fmul2_rn(make_float2(visc_i, visc_i), make_float2(a0.y, a1.y)), g);
+            ax = __fmaf_rn(sv.x, vx.x, __fmaf_rn(sp.x, rx.x, ax));
+            ay = __fmaf_rn(sv.x, vy.x, __fmaf_rn(sp.x, ry.x, ay));
+            ax = __fmaf_rn(sv.y, vx.y, __fmaf_rn(sp.y, rx.y, ax));
+            ay = __fmaf_rn(sv.y, vy.y, __fmaf_rn(sp.y, ry.y, ay));
+            if (!PLANAR) {
+                az = __fmaf_rn(sv.x, vi.z - v0.z, __fmaf_rn(sp.x, rz.x, az));
+                az = __fmaf_rn(sv.y, vi.z - v1.z, __fmaf_rn(sp.y, rz.y, az));
+            }
+        };
+        // a Poiseuille wall particle beyond the extrapolation lines
+        auto extrapolated = [&](const float4 &q) {
+            return q.w == 1.0f && (q.y > p.wall_top || q.y < p.wall_bottom);
+        };
         // image shift of a list entry (2 bits per axis above the index)
         auto entry_shift = [&](uint32_t en) {
             const uint32_t cd = en >> kListIndexBits;
@@ -283,7 +323,7 @@ __global__ void __launch_bounds__(256, 4)
         if (LIST && cnt <= nl.cap) {
             // the density pass's list: the walk's interacting candidates, same order
             uint32_t k = 0;
-            if ((SYS == CMAG_DAMBREAK || SYS == CMAG_PERISTALSIS) && p.kernel == CMAG_KERNEL_WENDLAND) {
+            if (p.kernel == CMAG_KERNEL_WENDLAND) {
                 // the next pair's entries are loaded one step ahead (the force waits on
                 // the chain entry -> position -> velocity and aux data)
                 const uint32_t *ep = nl.entry + i;
@@ -309,6 +349,14 @@ __global__ void __launch_bounds__(256, 4)
                         } else {
                             pair(j0, q0, 0.0f, 0.0f, 0.0f);
                             pair(j1, q1, 0.0f, 0.0f, 0.0f);
+                        }
+                    } else if (SYS == CMAG_POISEUILLE) {
+                        const float sx0 = entry_shift(c0 << kListIndexBits).x, sx1 = entry_shift(c1 << kListIndexBits).x;
+                        if (!extrapolated(q0) && !extrapolated(q1)) {
+                            poi_pair2(j0, q0, sx0, j1, q1, sx1);
+                        } else {
+                            pair(j0, q0, sx0, 0.0f, 0.0f);
+                            pair(j1, q1, sx1, 0.0f, 0.0f);
                         }
                     } else {
                         const float3 s0 = entry_shift(c0 << kListIndexBits), s1 = entry_shift(c1 << kListIndexBits);
