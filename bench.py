@@ -597,9 +597,15 @@ def main():
             fp32 = {"candidates_per_particle": round(cand, 1), "neighbours_per_particle": round(inter, 1),
                     "peak_tflops": round(peak_tf, 1),
                     "peak_kind": "nominal: 152 SMs x 128 FP32 lanes x 2 flop x sampled SM clock"}
+            lists = bool(cfg["lanes_density_force"][2])
+            fp32["force_path"] = "interaction lists" if lists else "cell walk"
             for k, per_pair in (("density", FLOPS_DENSITY_PAIR), ("force", FLOPS_FORCE_PAIR)):
-                fl = FLOPS_CANDIDATE * cand + per_pair * inter
-                tf = fl * n / (per_stage[k] / 1e3) / 1e12
+                # the list-driven force visits interacting pairs only; the DamBreak
+                # force runs for fluid particles only
+                visits = 0.0 if (k == "force" and lists) else cand
+                fl = FLOPS_CANDIDATE * visits + per_pair * inter
+                parts = fluid if (k == "force" and p.system == 0) else n
+                tf = fl * parts / (per_stage[k] / 1e3) / 1e12
                 fp32[k] = {"flops_per_particle": round(fl, 1), "achieved_tflops": round(tf, 3),
                            "frac": round(tf / peak_tf, 4)}
         except Exception as e:  # scipy missing: report the HBM roofline alone
