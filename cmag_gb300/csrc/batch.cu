@@ -295,10 +295,9 @@ int record_step(cmag_batch *b, int last, bool timed)
     mark(1);
     if (last >= CMAG_STAGE_SORT)
         launch_cell_sort(b->hash[0], b->idx[0], b->off, 0u, b->n_total, b->hash[1], b->idx[1],
-                         b->idx[0], b->err, st);
+                         b->idx[0], b->pos, b->vlf, b->spos, b->svel, b->err, st);
     mark(2);
-    if (last >= CMAG_STAGE_REORDER)
-        launch_reorder(sorted_idx(b), b->pos, b->vlf, b->spos, b->svel, b->n_total, st);
+    // (the gather of sorted positions and velocities ran with the sort)
     mark(3);
     if (last >= CMAG_STAGE_DENSITY) {
         int rc = launch_groups(b, false);

@@ -1,5 +1,5 @@
 // cells.cu -- grid hash, per-cell counts and dense cell offsets, the per-step
-// counting sort, sorted gather.
+// counting sort with the sorted gather.
 //
 // The reference finds cell ranges after the sort: it clears cellStart for the
 // whole grid (cudaMemset, fluidSystem.cu:161) and writes cellStart/cellEnd where
@@ -211,43 +211,36 @@ __global__ void __launch_bounds__(256)
 // cell's start + the number of the cell's entries with a smaller original index,
 // so each cell lists its particles by original index: the order of a stable
 // sort by hash.  A cell of c particles costs c loads per entry; the neighbour
-// loops read every particle of a cell for each of its particles as well.
+// loops read every particle of a cell for each of its particles as well.  The
+// same thread gathers the particle's position and leap-frog velocity into the
+// sorted copies (the copy half of reorderDataAndFindCellStartD,
+// fluid_kernel.cu:91-96).
 __global__ void __launch_bounds__(256)
     k_cell_order(const uint32_t *__restrict__ shash, const uint32_t *__restrict__ tmp,
                  const uint32_t *__restrict__ off, uint32_t key_base, uint32_t n,
-                 uint32_t *__restrict__ idx, uint32_t *err)
+                 uint32_t *__restrict__ idx, const float4 *__restrict__ pos,
+                 const float4 *__restrict__ vlf, float4 *__restrict__ spos,
+                 float4 *__restrict__ svel, uint32_t *err)
 {
     const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= n) return;
     const uint32_t c = shash[q] - key_base;
     const uint32_t a = __ldg(off + c), b = __ldg(off + c + 1);
     const uint32_t own = tmp[q];
-    if (b - a == 1u && a == q) {
-        idx[q] = own;
-        return;
+    uint32_t dst = q;
+    if (!(b - a == 1u && a == q)) {
+        if (!(a <= q && q < b && b <= n)) {  // counts and offsets disagree
+            set_error(err, CMAG_DEVERR_RANGE);
+        } else {
+            uint32_t r = 0;
+            for (uint32_t k = a; k < b; ++k) r += __ldg(tmp + k) < own ? 1u : 0u;
+            dst = a + r;
+        }
     }
-    if (!(a <= q && q < b && b <= n)) {  // counts and offsets disagree
-        set_error(err, CMAG_DEVERR_RANGE);
-        idx[q] = own;
-        return;
-    }
-    uint32_t r = 0;
-    for (uint32_t k = a; k < b; ++k) r += __ldg(tmp + k) < own ? 1u : 0u;
-    idx[a + r] = own;
-}
-
-// the copy half of reorderDataAndFindCellStartD (fluid_kernel.cu:91-96)
-__global__ void __launch_bounds__(256)
-    k_reorder(const uint32_t *__restrict__ idx, const float4 *__restrict__ pos,
-              const float4 *__restrict__ vlf, float4 *__restrict__ spos,
-              float4 *__restrict__ svel, uint32_t n)
-{
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    uint32_t j = idx[i];
-    if (j >= n) j = i;  // only after a failed sort (reported by the sort itself)
-    spos[i] = __ldg(pos + j);
-    svel[i] = __ldg(vlf + j);
+    idx[dst] = own;
+    const uint32_t j = own < n ? own : dst;  // own >= n only after a failed sort
+    spos[dst] = __ldg(pos + j);
+    svel[dst] = __ldg(vlf + j);
 }
 
 __global__ void k_cell_view(const uint32_t *__restrict__ off, uint32_t scan_base,
@@ -281,12 +274,13 @@ void launch_hash(const DevParams &p, const BatchView &bv, const float4 *pos, uin
 
 void launch_cell_sort(const uint32_t *hash, const uint32_t *rank, const uint32_t *off,
                       uint32_t key_base, uint32_t n, uint32_t *shash, uint32_t *tmp,
-                      uint32_t *idx, uint32_t *err, cudaStream_t st)
+                      uint32_t *idx, const float4 *pos, const float4 *vlf, float4 *spos,
+                      float4 *svel, uint32_t *err, cudaStream_t st)
 {
     if (n == 0) return;
     const uint32_t blocks = (n + 255) / 256;
     k_cell_scatter<<<blocks, 256, 0, st>>>(hash, rank, off, key_base, n, shash, tmp, err);
-    k_cell_order<<<blocks, 256, 0, st>>>(shash, tmp, off, key_base, n, idx, err);
+    k_cell_order<<<blocks, 256, 0, st>>>(shash, tmp, off, key_base, n, idx, pos, vlf, spos, svel, err);
 }
 
 size_t cell_scan_workspace_words(uint32_t m) { return (m + kScanTile - 1) / kScanTile; }
@@ -298,13 +292,6 @@ void launch_cell_scan(uint32_t *cnt, uint32_t *off, uint32_t m, uint32_t *ws, cu
     k_tile_sum<<<tiles, kScanThreads, 0, st>>>(cnt, m, ws);
     k_tile_prefix<<<1, 1024, 0, st>>>(ws, tiles);
     k_cell_offsets<<<tiles, kScanThreads, 0, st>>>(cnt, off, m, ws);
-}
-
-void launch_reorder(const uint32_t *idx, const float4 *pos, const float4 *vlf, float4 *spos,
-                    float4 *svel, uint32_t n, cudaStream_t st)
-{
-    if (n == 0) return;
-    k_reorder<<<(n + 255) / 256, 256, 0, st>>>(idx, pos, vlf, spos, svel, n);
 }
 
 void launch_cell_view(const uint32_t *off, uint32_t scan_base, uint32_t scan_cells,

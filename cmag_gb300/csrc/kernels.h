@@ -48,19 +48,18 @@ void launch_hash(const DevParams &p, const BatchView &bv, const float4 *pos, uin
                  uint32_t *cnt, uint32_t *rank, uint32_t *err, cudaStream_t st);
 // Stable counting sort of the hashed particles by cell, from the dense offsets
 // (after launch_cell_scan): shash/idx = the hashes and original indices in the
-// order of a stable sort by hash (the radix sort's result exactly).  Cell of a
-// hash: h - key_base.  tmp: n words of scratch; idx may alias rank.
+// order of a stable sort by hash (the radix sort's result exactly), and
+// spos/svel = pos/vlf gathered in that order.  Cell of a hash: h - key_base.
+// tmp: n words of scratch; idx may alias rank.
 void launch_cell_sort(const uint32_t *hash, const uint32_t *rank, const uint32_t *off,
                       uint32_t key_base, uint32_t n, uint32_t *shash, uint32_t *tmp,
-                      uint32_t *idx, uint32_t *err, cudaStream_t st);
+                      uint32_t *idx, const float4 *pos, const float4 *vlf, float4 *spos,
+                      float4 *svel, uint32_t *err, cudaStream_t st);
 // Exclusive scan of cnt[0..m) into off[0..m) (tile totals, their scan, then
 // every tile from its prefix), clearing cnt for the next step.  ws must hold
 // cell_scan_workspace_words(m) words (no clearing needed).
 size_t cell_scan_workspace_words(uint32_t m);
 void launch_cell_scan(uint32_t *cnt, uint32_t *off, uint32_t m, uint32_t *ws, cudaStream_t st);
-// sortedPos/sortedVel gather (reorderDataAndFindCellStartD's copy half).
-void launch_reorder(const uint32_t *idx, const float4 *pos, const float4 *vlf, float4 *spos,
-                    float4 *svel, uint32_t n, cudaStream_t st);
 // Reference cellStart/cellEnd view of the dense offsets.
 void launch_cell_view(const uint32_t *off, uint32_t scan_base, uint32_t scan_cells,
                       uint64_t ncells, uint32_t *cell_start, uint32_t *cell_end, cudaStream_t st);

@@ -386,10 +386,9 @@ int record_step(cmag_system *s, int last, bool timed)
     mark(1);
     if (last >= CMAG_STAGE_SORT)
         launch_cell_sort(s->hash[0], s->idx[0], s->off, s->scan_base, s->n, s->hash[1], s->idx[1],
-                         s->idx[0], s->err, st);
+                         s->idx[0], s->pos, s->vlf, s->spos, s->svel, s->err, st);
     mark(2);
-    if (last >= CMAG_STAGE_REORDER)
-        launch_reorder(sorted_idx(s), s->pos, s->vlf, s->spos, s->svel, s->n, st);
+    // (the gather of sorted positions and velocities ran with the sort)
     mark(3);
     if (last >= CMAG_STAGE_DENSITY)
         launch_density(d, BatchView{}, s->g_density, s->spos, s->off, s->meas, s->aux, nl_of(s), st);
