@@ -246,12 +246,11 @@ class BatchedRun:
         return self.b.stage_times()
 
     def upload(self, array, host):
-        for k, (a, n) in enumerate(self.ranges):
-            self.b.set_array(k, array, host[a:a + n])
+        """Every scene's rows in one call (scenes one after another)."""
+        self.b.set_array_all(array, host)
 
     def download(self, array, host):
-        for k, (a, n) in enumerate(self.ranges):
-            self.b.get_array(k, array, out=host[a:a + n])
+        self.b.get_array_all(array, out=host)
 
     def close(self):
         self.b.close()

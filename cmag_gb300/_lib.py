@@ -90,6 +90,8 @@ SIGNATURES = {
     "cmag_batch_reset_scene": ([c_bat, c_u32], ctypes.c_int),
     "cmag_batch_set_array": ([c_bat, c_u32, c_i32, c_f32p, c_u32, c_u32], ctypes.c_int),
     "cmag_batch_get_array": ([c_bat, c_u32, c_i32, c_f32p, c_u32, c_u32], ctypes.c_int),
+    "cmag_batch_set_array_all": ([c_bat, c_i32, c_f32p], ctypes.c_int),
+    "cmag_batch_get_array_all": ([c_bat, c_i32, c_f32p], ctypes.c_int),
     "cmag_batch_get_uint_array": ([c_bat, c_u32, c_i32, c_u32p, c_u32, c_u32], ctypes.c_int),
     "cmag_batch_device_array": ([c_bat, c_i32], ctypes.c_void_p),
     "cmag_batch_get_params": ([c_bat, c_u32, P(SphParams)], ctypes.c_int),

@@ -85,6 +85,25 @@ class Batch:
         self._chk(lib().cmag_batch_get_array(self._h, int(scene), int(array), _fp(out), int(start), count))
         return out
 
+    def set_array_all(self, array, data):
+        """Every scene's rows at once, scenes one after another in scene order
+        ((num_particles, 4) float32)."""
+        a = np.ascontiguousarray(data, dtype=np.float32).reshape(-1, 4)
+        if a.shape[0] != self.num_particles:
+            raise ValueError("expected %d rows" % self.num_particles)
+        self._chk(lib().cmag_batch_set_array_all(self._h, int(array), _fp(a)))
+
+    def get_array_all(self, array, out=None):
+        """Every scene's rows, scenes one after another in scene order; into `out`
+        (a C-contiguous (num_particles, 4) float32 array) when given."""
+        n = self.num_particles
+        if out is None:
+            out = np.empty((n, 4), np.float32)
+        elif out.dtype != np.float32 or out.shape != (n, 4) or not out.flags["C_CONTIGUOUS"]:
+            raise ValueError("out must be a C-contiguous (%d, 4) float32 array" % n)
+        self._chk(lib().cmag_batch_get_array_all(self._h, int(array), _fp(out)))
+        return out
+
     def get_uint_array(self, scene, array, start=0, count=None):
         if count is None:
             if array in (_abi.CELLSTART, _abi.CELLEND):

@@ -90,6 +90,8 @@ struct cmag_batch {
     PhaseState *phase = nullptr;
     DevParams *dev = nullptr;
     uint16_t *scene_of = nullptr;
+    float2 *zexpect = nullptr;  // whole-batch uploads: z each planar slot must keep
+    uint32_t *zflags = nullptr;
     bool dev_dirty = true;
 
     bool use_graphs = true;
@@ -404,7 +406,8 @@ void free_all(cmag_batch *b)
     for (auto s : b->side) cudaStreamDestroy(s);
     void *ptrs[] = {b->pos, b->vel, b->vlf, b->meas, b->acc, b->vforce, b->pforce, b->pred,
                     b->spos, b->svel, b->hash[0], b->hash[1], b->idx[0], b->idx[1], b->cnt,
-                    b->off, b->ws, b->err, b->red, b->aux, b->phase, b->dev, b->scene_of};
+                    b->off, b->ws, b->err, b->red, b->aux, b->phase, b->dev, b->scene_of,
+                    b->zexpect, b->zflags};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     free_lists(b);
@@ -605,6 +608,8 @@ int cmag_batch_create(const cmag_sph_params *params, const uint32_t *counts, uin
         step(dalloc(b, &b->phase, sizeof(PhaseState) * (size_t)scenes));
         step(dalloc(b, &b->dev, sizeof(DevParams) * (size_t)scenes));
         step(dalloc(b, &b->scene_of, sizeof(uint16_t) * n));
+        step(dalloc(b, &b->zexpect, sizeof(float2) * (size_t)scenes));
+        step(dalloc(b, &b->zflags, sizeof(uint32_t) * (size_t)scenes));
     }
     if (rc == CMAG_OK) {
         std::vector<uint16_t> so(n);
@@ -703,6 +708,80 @@ int cmag_batch_get_array(cmag_batch *b, uint32_t scene, int32_t array, float *ho
     if (count == 0) return CMAG_OK;
     CB_CUDA(b, cudaMemcpyAsync(host, d + s->part_base + start, sizeof(float4) * (size_t)count,
                                cudaMemcpyDeviceToHost, b->stream));
+    CB_CUDA(b, cudaStreamSynchronize(b->stream));
+    return CMAG_OK;
+}
+
+// Every scene's array in one call: one asynchronous copy per scene, one
+// synchronisation, and the planar scenes' z checks on the device.
+int cmag_batch_set_array_all(cmag_batch *b, int32_t array, const float *host)
+{
+    if (!b || !host) return bfail(b, CMAG_ERR_INVALID, "null argument");
+    float4 *d = float_array(b, array);
+    if (!d) return bfail(b, CMAG_ERR_INVALID, "not a settable float4 array: " + std::to_string(array));
+    cudaStream_t st = b->stream;
+    const bool pos_up = array == CMAG_POSITION;
+    const bool vel_up = array == CMAG_VELOCITY || array == CMAG_VELOCITYLEAPFROG;
+    std::vector<float2> expect(b->sc.size(), make_float2(0.0f, 0.0f));
+    bool check = false;
+    size_t row = 0;
+    for (size_t k = 0; k < b->slot_of_user.size(); ++k) {
+        const BatchScene &s = b->sc[b->slot_of_user[k]];
+        CB_CUDA(b, cudaMemcpyAsync(d + s.part_base, host + 4 * row, sizeof(float4) * (size_t)s.n,
+                                   cudaMemcpyHostToDevice, st));
+        if (s.planar_slot && (pos_up || vel_up)) {
+            expect[b->slot_of_user[k]] = make_float2(pos_up ? host[4 * row + 2] : 0.0f, 1.0f);
+            check = true;
+        }
+        row += s.n;
+    }
+    std::vector<uint32_t> flags(b->sc.size(), 0u);
+    if (check) {
+        CB_CUDA(b, cudaMemcpyAsync(b->zexpect, expect.data(), sizeof(float2) * expect.size(),
+                                   cudaMemcpyHostToDevice, st));
+        launch_z_differs_slots(d, b->scene_of, b->n_total, b->zexpect, b->zflags, (uint32_t)flags.size(), st);
+        CB_CUDA(b, cudaGetLastError());
+        CB_CUDA(b, cudaMemcpyAsync(flags.data(), b->zflags, sizeof(uint32_t) * flags.size(),
+                                   cudaMemcpyDeviceToHost, st));
+    }
+    CB_CUDA(b, cudaStreamSynchronize(st));
+    for (size_t k = 0; k < b->slot_of_user.size(); ++k)
+        if (flags[b->slot_of_user[k]])
+            return bfail(b, CMAG_ERR_INVALID,
+                         std::string("scene ") + std::to_string(k) +
+                             (pos_up ? ": a planar 2-D batch scene keeps every particle at one z"
+                                     : ": a planar 2-D batch scene has no z velocity") +
+                             " (the array holds the new data; set it again)");
+    if (pos_up) {
+        bool moved = false;
+        for (size_t slot = 0; slot < b->sc.size(); ++slot) {
+            BatchScene &s = b->sc[slot];
+            if (!s.planar_slot) continue;
+            s.z_value = expect[slot].x;
+            s.z_uniform = true;
+            const SceneLayout l = layout_for(s.p, true, s.z_value);
+            if (l.scan_base != s.lay.scan_base) {
+                s.lay = l;
+                moved = true;
+            }
+        }
+        if (moved) refresh_dev(b);
+    }
+    return CMAG_OK;
+}
+
+int cmag_batch_get_array_all(cmag_batch *b, int32_t array, float *host)
+{
+    if (!b || !host) return bfail(b, CMAG_ERR_INVALID, "null argument");
+    float4 *d = float_array(b, array);
+    if (!d) return bfail(b, CMAG_ERR_INVALID, "not a float4 array: " + std::to_string(array));
+    size_t row = 0;
+    for (size_t k = 0; k < b->slot_of_user.size(); ++k) {
+        const BatchScene &s = b->sc[b->slot_of_user[k]];
+        CB_CUDA(b, cudaMemcpyAsync(host + 4 * row, d + s.part_base, sizeof(float4) * (size_t)s.n,
+                                   cudaMemcpyDeviceToHost, b->stream));
+        row += s.n;
+    }
     CB_CUDA(b, cudaStreamSynchronize(b->stream));
     return CMAG_OK;
 }

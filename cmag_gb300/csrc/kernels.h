@@ -103,6 +103,10 @@ void launch_fluid_extents_batch(const BatchView &bv, const float4 *pos, uint32_t
                                 cudaStream_t st);
 // *flag = 1 when some a[i].z (i < n) differs from z, else 0.
 void launch_z_differs(const float4 *a, uint32_t n, float z, uint32_t *flag, cudaStream_t st);
+// flags[slot] = 1 when a particle of a checked slot (expect[slot].y != 0) has a z
+// other than expect[slot].x, else 0 (slots entries).
+void launch_z_differs_slots(const float4 *a, const uint16_t *slot_of, uint32_t n, const float2 *expect,
+                            uint32_t *flags, uint32_t slots, cudaStream_t st);
 void launch_fluid_sum(int32_t system, const float4 *type_src, const float4 *a, uint32_t n,
                       double *sums4, unsigned long long *count, cudaStream_t st);
 

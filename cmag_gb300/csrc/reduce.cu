@@ -131,6 +131,19 @@ __global__ void __launch_bounds__(256)
     if (__any_sync(0xffffffffu, differs) && (threadIdx.x & 31) == 0) atomicOr(flag, 1u);
 }
 
+// flags[slot] |= 1 when a particle of a checked slot (expect[slot].y != 0) has a z
+// other than expect[slot].x (a NaN differs from everything).
+__global__ void __launch_bounds__(256)
+    k_z_differs_slots(const float4 *__restrict__ a, const uint16_t *__restrict__ slot_of, uint32_t n,
+                      const float2 *__restrict__ expect, uint32_t *__restrict__ flags)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t s = slot_of[i];
+        const float2 e = __ldg(expect + s);
+        if (e.y != 0.0f && a[i].z != e.x) atomicOr(flags + s, 1u);
+    }
+}
+
 }  // namespace
 
 void launch_fluid_extent(int32_t system, const float4 *pos, uint32_t n, uint32_t *out6,
@@ -154,6 +167,13 @@ void launch_z_differs(const float4 *a, uint32_t n, float z, uint32_t *flag, cuda
 {
     cudaMemsetAsync(flag, 0, sizeof(uint32_t), st);
     if (n) k_z_differs<<<blocks_for(n), 256, 0, st>>>(a, n, z, flag);
+}
+
+void launch_z_differs_slots(const float4 *a, const uint16_t *slot_of, uint32_t n, const float2 *expect,
+                            uint32_t *flags, uint32_t slots, cudaStream_t st)
+{
+    cudaMemsetAsync(flags, 0, sizeof(uint32_t) * (size_t)slots, st);
+    if (n) k_z_differs_slots<<<blocks_for(n), 256, 0, st>>>(a, slot_of, n, expect, flags);
 }
 
 }  // namespace cmag

@@ -262,6 +262,9 @@ public:
     {
         chk(cmag_batch_get_array(h_, scene, array, data, (uint32_t)start, (uint32_t)count));
     }
+    // every scene's rows at once, scenes one after another in scene order
+    void setArrayAll(int array, const float *data) { chk(cmag_batch_set_array_all(h_, array, data)); }
+    void getArrayAll(int array, float *data) const { chk(cmag_batch_get_array_all(h_, array, data)); }
     void *deviceArray(int array) const { return cmag_batch_device_array(h_, array); }
     float elapsedTime(uint32_t scene) const { float t = 0; chk(cmag_batch_elapsed_time(h_, scene, &t)); return t; }
     void removeRightBoundary(uint32_t scene) { chk(cmag_batch_dambreak_remove_right_boundary(h_, scene)); }

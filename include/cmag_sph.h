@@ -412,6 +412,14 @@ int cmag_batch_set_array(cmag_batch *b, uint32_t scene, int32_t array, const flo
                          uint32_t start, uint32_t count);
 int cmag_batch_get_array(cmag_batch *b, uint32_t scene, int32_t array, float *host,
                          uint32_t start, uint32_t count);
+/* Every scene's float4 array in one call: host holds the scenes one after another
+ * in scene order (cmag_batch_num_particles(b) x 4 floats); one copy per scene and
+ * one synchronisation.  A planar 2-D scene must keep one z (positions) and no z
+ * velocity: checked on the device after the transfer, so on that error the array
+ * holds the new data and should be set again.  No reference counterpart (the
+ * reference has one scene per process). */
+int cmag_batch_set_array_all(cmag_batch *b, int32_t array, const float *host);
+int cmag_batch_get_array_all(cmag_batch *b, int32_t array, float *host);
 /* scene-local: HASH = the scene's reference hash, INDEX = scene-local original
  * index, CELLOFFSET = offsets over the scene's table (scan_cells + 1 entries),
  * CELLSTART / CELLEND = the reference arrays over the scene's grid */

@@ -232,6 +232,39 @@ def test_batch_interaction_lists_bit_exact(gpu):
     batch.close()
 
 
+def test_batch_whole_arrays(gpu):
+    """set_array_all / get_array_all move every scene's rows (scene order) and agree
+    with the per-scene calls; a planar scene's z is checked on the device."""
+    batch, singles, scenes = build_pair()
+    batch.update_n(3)
+    n = batch.num_particles
+    for a in (cm.POSITION, cm.VELOCITY, cm.VELOCITYLEAPFROG, cm.ACCELERATION):
+        whole = batch.get_array_all(a)
+        per = np.concatenate([batch.get_array(k, a) for k in range(len(scenes))])
+        assert whole.shape == (n, 4) and np.array_equal(whole.view(np.uint32), per.view(np.uint32))
+    # round trip through the whole-batch upload
+    pos = batch.get_array_all(cm.POSITION)
+    vel = batch.get_array_all(cm.VELOCITY)
+    batch.set_array_all(cm.POSITION, pos)
+    batch.set_array_all(cm.VELOCITY, vel)
+    assert np.array_equal(batch.get_array_all(cm.POSITION), pos)
+    # a planar scene's particle off its z layer, or with a z velocity: rejected
+    first = sum(s[1] for s in scenes[:1])  # scene 1 (planar dam break) starts here
+    bad = pos.copy()
+    bad[first + 5, 2] += 0.01
+    with pytest.raises(cm.CmagError):
+        batch.set_array_all(cm.POSITION, bad)
+    batch.set_array_all(cm.POSITION, pos)
+    badv = vel.copy()
+    badv[first + 5, 2] = 1.0
+    with pytest.raises(cm.CmagError):
+        batch.set_array_all(cm.VELOCITY, badv)
+    batch.set_array_all(cm.VELOCITY, vel)
+    batch.update_n(2)
+    assert np.isfinite(batch.get_array_all(cm.POSITION)).all()
+    batch.close()
+
+
 def test_batch_set_params_and_planar_checks(gpu):
     scenes = mixed_scenes()
     batch = Batch([s[0] for s in scenes], [s[1] for s in scenes])
