@@ -42,6 +42,7 @@ __global__ void __launch_bounds__(256)
     k_hash(DevParams pv, BatchView bv, const float4 *__restrict__ pos, uint32_t *__restrict__ hash,
            uint32_t *__restrict__ cnt, uint32_t *__restrict__ rank, uint32_t *err)
 {
+    pdl_entry();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= (BATCH ? bv.n_total : pv.n)) return;
     const DevParams &p = BATCH ? bv.scenes[bv.scene_of[i]] : pv;
@@ -92,6 +93,7 @@ __device__ __forceinline__ uint32_t block_sum(uint32_t x, uint32_t *s_warp)
 __global__ void __launch_bounds__(kScanThreads)
     k_tile_sum(const uint32_t *__restrict__ cnt, uint32_t m, uint32_t *__restrict__ tot)
 {
+    pdl_entry();
     __shared__ uint32_t s_warp[kScanThreads / 32];
     uint32_t v[kScanItems];
     load_counts(cnt, blockIdx.x * kScanTile + threadIdx.x * kScanItems, m, v);
@@ -107,6 +109,7 @@ __global__ void __launch_bounds__(kScanThreads)
 // each thread rewrites its chunk from its offset.
 __global__ void __launch_bounds__(1024) k_tile_prefix(uint32_t *__restrict__ tot, uint32_t tiles)
 {
+    pdl_entry();
     __shared__ uint32_t s_warp[32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t per = (tiles + blockDim.x - 1) / blockDim.x;
@@ -136,6 +139,7 @@ __global__ void __launch_bounds__(kScanThreads)
     k_cell_offsets(uint32_t *__restrict__ cnt, uint32_t *__restrict__ off, uint32_t m,
                    const uint32_t *__restrict__ tot)
 {
+    pdl_entry();
     __shared__ uint32_t s_warp[kScanThreads / 32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t first = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
@@ -195,6 +199,7 @@ __global__ void __launch_bounds__(256)
                    const uint32_t *__restrict__ off, uint32_t key_base, uint32_t n,
                    uint32_t *__restrict__ shash, uint32_t *__restrict__ tmp, uint32_t *err)
 {
+    pdl_entry();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t h = hash[i];
@@ -222,6 +227,7 @@ __global__ void __launch_bounds__(256)
                  const float4 *__restrict__ vlf, float4 *__restrict__ spos,
                  float4 *__restrict__ svel, uint32_t *err)
 {
+    pdl_entry();
     const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= n) return;
     const uint32_t c = shash[q] - key_base;
@@ -268,8 +274,8 @@ void launch_hash(const DevParams &p, const BatchView &bv, const float4 *pos, uin
     const uint32_t n = bv.scenes ? bv.n_total : p.n;
     if (n == 0) return;
     const uint32_t blocks = (n + 255) / 256;
-    if (bv.scenes) k_hash<true><<<blocks, 256, 0, st>>>(p, bv, pos, hash, cnt, rank, err);
-    else k_hash<false><<<blocks, 256, 0, st>>>(p, bv, pos, hash, cnt, rank, err);
+    if (bv.scenes) launch_pdl(k_hash<true>, blocks, 256, 0, st, p, bv, pos, hash, cnt, rank, err);
+    else launch_pdl(k_hash<false>, blocks, 256, 0, st, p, bv, pos, hash, cnt, rank, err);
 }
 
 void launch_cell_sort(const uint32_t *hash, const uint32_t *rank, const uint32_t *off,
@@ -279,8 +285,8 @@ void launch_cell_sort(const uint32_t *hash, const uint32_t *rank, const uint32_t
 {
     if (n == 0) return;
     const uint32_t blocks = (n + 255) / 256;
-    k_cell_scatter<<<blocks, 256, 0, st>>>(hash, rank, off, key_base, n, shash, tmp, err);
-    k_cell_order<<<blocks, 256, 0, st>>>(shash, tmp, off, key_base, n, idx, pos, vlf, spos, svel, err);
+    launch_pdl(k_cell_scatter, blocks, 256, 0, st, hash, rank, off, key_base, n, shash, tmp, err);
+    launch_pdl(k_cell_order, blocks, 256, 0, st, shash, tmp, off, key_base, n, idx, pos, vlf, spos, svel, err);
 }
 
 size_t cell_scan_workspace_words(uint32_t m) { return (m + kScanTile - 1) / kScanTile; }
@@ -289,9 +295,9 @@ void launch_cell_scan(uint32_t *cnt, uint32_t *off, uint32_t m, uint32_t *ws, cu
 {
     const uint32_t tiles = (m + kScanTile - 1) / kScanTile;
     if (tiles == 0) return;
-    k_tile_sum<<<tiles, kScanThreads, 0, st>>>(cnt, m, ws);
-    k_tile_prefix<<<1, 1024, 0, st>>>(ws, tiles);
-    k_cell_offsets<<<tiles, kScanThreads, 0, st>>>(cnt, off, m, ws);
+    launch_pdl(k_tile_sum, tiles, kScanThreads, 0, st, cnt, m, ws);
+    launch_pdl(k_tile_prefix, 1, 1024, 0, st, ws, tiles);
+    launch_pdl(k_cell_offsets, tiles, kScanThreads, 0, st, cnt, off, m, ws);
 }
 
 void launch_cell_view(const uint32_t *off, uint32_t scan_base, uint32_t scan_cells,

@@ -166,6 +166,7 @@ __global__ void __launch_bounds__(256)
                        const uint32_t *__restrict__ off, const float4 *__restrict__ acc,
                        float *feat, __nv_bfloat16 *xb)
 {
+    pdl_entry();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
     const float4 pi = spos[i];
@@ -325,6 +326,7 @@ __global__ void __launch_bounds__(128)
           const float4 *__restrict__ spos, const uint32_t *__restrict__ idx, float4 *acc,
           float *__restrict__ out)
 {
+    pdl_entry();
     __shared__ uint4 simage[kImageWords];
     for (int k = threadIdx.x; k < kImageWords; k += blockDim.x) simage[k] = __ldg(c.image + k);
     const __nv_bfloat16 *sw = reinterpret_cast<const __nv_bfloat16 *>(simage);
@@ -619,7 +621,7 @@ void dispatch_features(const DevParams &p, const ClosureView &c, const float4 *s
     if (p.n == 0) return;
     const uint32_t blocks = (p.n + 255) / 256;
 #define CMAG_FEAT(PL, TR) \
-    k_closure_features<PL, TR, NORM><<<blocks, 256, 0, st>>>(p, c, spos, svel, aux, meas, idx, off, acc, feat, xb)
+    launch_pdl(k_closure_features<PL, TR, NORM>, blocks, 256, 0, st, p, c, spos, svel, aux, meas, idx, off, acc, feat, xb)
     if (p.planar) {
         if (p.trim) CMAG_FEAT(true, true);
         else CMAG_FEAT(true, false);
@@ -656,7 +658,7 @@ void launch_closure_apply(const DevParams &p, const ClosureView &c, const float4
 {
     if (p.n == 0) return;
     dispatch_features<true>(p, c, spos, svel, aux, meas, idx, off, acc, nullptr, xb, st);
-    k_mlp<true><<<mlp_blocks(p.n), 128, 0, st>>>(c, xb, p.n, spos, idx, acc, nullptr);
+    launch_pdl(k_mlp<true>, mlp_blocks(p.n), 128, 0, st, c, xb, p.n, spos, idx, acc, (float *)nullptr);
 }
 
 void launch_closure_forward(const ClosureView &c, const float *feat, uint32_t n,

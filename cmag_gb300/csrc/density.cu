@@ -98,6 +98,7 @@ __global__ void __launch_bounds__(256, 6)
               const uint32_t *__restrict__ off_all, float4 *__restrict__ meas,
               float2 *__restrict__ aux, NeighborList nl)
 {
+    pdl_entry();
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t i = (BATCH ? bv.first : 0u) + t / G;
     const int lane = (int)(t % G);
@@ -161,9 +162,9 @@ void launch_d(const DevParams &p, const BatchView &bv, const float4 *spos, const
     const uint64_t threads = (uint64_t)(bv.scenes ? bv.count : p.n) * G;
     const uint32_t blocks = (uint32_t)((threads + 255) / 256);
     if (bv.scenes)
-        k_density<SYS, PLANAR, TRIM, G, true, LIST><<<blocks, 256, 0, st>>>(p, bv, spos, off, meas, aux, nl);
+        launch_pdl(k_density<SYS, PLANAR, TRIM, G, true, LIST>, blocks, 256, 0, st, p, bv, spos, off, meas, aux, nl);
     else
-        k_density<SYS, PLANAR, TRIM, G, false, LIST><<<blocks, 256, 0, st>>>(p, bv, spos, off, meas, aux, nl);
+        launch_pdl(k_density<SYS, PLANAR, TRIM, G, false, LIST>, blocks, 256, 0, st, p, bv, spos, off, meas, aux, nl);
 }
 
 template <int SYS, bool PLANAR, bool TRIM>

@@ -80,6 +80,7 @@ __global__ void __launch_bounds__(256, 4)
             float4 *__restrict__ out_a, float4 *__restrict__ out_b,
             const PhaseState *__restrict__ ph_all, NeighborList nl)
 {
+    pdl_entry();
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t i = (BATCH ? bv.first : 0u) + t / G;
     const int lane = (int)(t % G);
@@ -419,9 +420,9 @@ void launch_f(const DevParams &p, const BatchView &bv, const ForceArgs &x, cudaS
     const uint64_t threads = (uint64_t)(bv.scenes ? bv.count : p.n) * G;
     const uint32_t blocks = (uint32_t)((threads + 255) / 256);
     if (bv.scenes)
-        k_force<SYS, PLANAR, TRIM, G, true, LIST><<<blocks, 256, 0, st>>>(p, bv, x.spos, x.svel, x.aux, x.idx, x.off, x.a, x.b, x.ph, x.nl);
+        launch_pdl(k_force<SYS, PLANAR, TRIM, G, true, LIST>, blocks, 256, 0, st, p, bv, x.spos, x.svel, x.aux, x.idx, x.off, x.a, x.b, x.ph, x.nl);
     else
-        k_force<SYS, PLANAR, TRIM, G, false, LIST><<<blocks, 256, 0, st>>>(p, bv, x.spos, x.svel, x.aux, x.idx, x.off, x.a, x.b, x.ph, x.nl);
+        launch_pdl(k_force<SYS, PLANAR, TRIM, G, false, LIST>, blocks, 256, 0, st, p, bv, x.spos, x.svel, x.aux, x.idx, x.off, x.a, x.b, x.ph, x.nl);
 }
 
 template <int SYS, bool PLANAR, bool TRIM>

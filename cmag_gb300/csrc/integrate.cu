@@ -42,11 +42,16 @@ __device__ __forceinline__ void advance_phase(const DevParams &p, PhaseState *ph
     *ph = s;
 }
 
-__global__ void k_phase(DevParams p, PhaseState *ph, float k_milli) { advance_phase(p, ph, k_milli); }
+__global__ void k_phase(DevParams p, PhaseState *ph, float k_milli)
+{
+    pdl_entry();
+    advance_phase(p, ph, k_milli);
+}
 
 __global__ void k_phase_batch(const DevParams *__restrict__ scenes, uint32_t nscenes,
                               PhaseState *ph, float k_milli)
 {
+    pdl_entry();
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s < nscenes && scenes[s].system == CMAG_PERISTALSIS) advance_phase(scenes[s], ph + s, k_milli);
 }
@@ -56,6 +61,7 @@ __global__ void __launch_bounds__(256)
     k_configure_boundary(DevParams pv, BatchView bv, float4 *__restrict__ pos,
                          const PhaseState *__restrict__ ph_all)
 {
+    pdl_entry();
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= (BATCH ? bv.n_total : pv.n)) return;
     const uint32_t sc = BATCH ? bv.scene_of[i] : 0u;
@@ -81,6 +87,7 @@ __global__ void __launch_bounds__(256)
                 const float4 *__restrict__ vforce, const float4 *__restrict__ pforce,
                 const PhaseState *__restrict__ ph_all)
 {
+    pdl_entry();
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= (BATCH ? bv.n_total : pv.n)) return;
     const uint32_t sc = BATCH ? bv.scene_of[i] : 0u;
@@ -148,14 +155,14 @@ __global__ void k_gate(DevParams p, float4 *__restrict__ pos, int remove, float 
 
 void launch_phase(const DevParams &p, PhaseState *ph, float k_milli, cudaStream_t st)
 {
-    k_phase<<<1, 1, 0, st>>>(p, ph, k_milli);
+    launch_pdl(k_phase, 1, 1, 0, st, p, ph, k_milli);
 }
 
 void launch_phase_batch(const DevParams *scenes, uint32_t nscenes, PhaseState *ph, float k_milli,
                         cudaStream_t st)
 {
     if (nscenes == 0) return;
-    k_phase_batch<<<(nscenes + 127) / 128, 128, 0, st>>>(scenes, nscenes, ph, k_milli);
+    launch_pdl(k_phase_batch, (nscenes + 127) / 128, 128, 0, st, scenes, nscenes, ph, k_milli);
 }
 
 void launch_configure_boundary(const DevParams &p, const BatchView &bv, float4 *pos,
@@ -163,8 +170,8 @@ void launch_configure_boundary(const DevParams &p, const BatchView &bv, float4 *
 {
     const uint32_t n = bv.scenes ? bv.n_total : p.n;
     if (n == 0) return;
-    if (bv.scenes) k_configure_boundary<true><<<(n + 255) / 256, 256, 0, st>>>(p, bv, pos, ph);
-    else k_configure_boundary<false><<<(n + 255) / 256, 256, 0, st>>>(p, bv, pos, ph);
+    if (bv.scenes) launch_pdl(k_configure_boundary<true>, (n + 255) / 256, 256, 0, st, p, bv, pos, ph);
+    else launch_pdl(k_configure_boundary<false>, (n + 255) / 256, 256, 0, st, p, bv, pos, ph);
 }
 
 void launch_integrate(const DevParams &p, const BatchView &bv, float4 *pos, float4 *vel,
@@ -174,9 +181,9 @@ void launch_integrate(const DevParams &p, const BatchView &bv, float4 *pos, floa
     const uint32_t n = bv.scenes ? bv.n_total : p.n;
     if (n == 0) return;
     if (bv.scenes)
-        k_integrate<true><<<(n + 255) / 256, 256, 0, st>>>(p, bv, pos, vel, vlf, acc, vforce, pforce, ph);
+        launch_pdl(k_integrate<true>, (n + 255) / 256, 256, 0, st, p, bv, pos, vel, vlf, acc, vforce, pforce, ph);
     else
-        k_integrate<false><<<(n + 255) / 256, 256, 0, st>>>(p, bv, pos, vel, vlf, acc, vforce, pforce, ph);
+        launch_pdl(k_integrate<false>, (n + 255) / 256, 256, 0, st, p, bv, pos, vel, vlf, acc, vforce, pforce, ph);
 }
 
 // shiftRightBoundaryD (remove = 0: x += dx) and removeRightBoundaryD

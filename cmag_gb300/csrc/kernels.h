@@ -10,6 +10,27 @@
 
 namespace cmag {
 
+// Launch `kernel` (which begins with pdl_entry()) with programmatic dependent
+// launch allowed: it may start launching while the previous kernel on the stream
+// finishes (in a captured graph too).
+template <typename... KArgs, typename... Args>
+inline void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                       Args &&...args)
+{
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
+
 // ---- onesweep radix sort (sort.cu) ----------------------------------------
 constexpr int kSortThreads = 256;
 constexpr int kSortItems = 16;

@@ -210,6 +210,17 @@ __device__ __forceinline__ float eos_pressure(const DevParams &p, float rho)
     return 50.0f * p.c0 * rho;
 }
 
+// Programmatic dependent launch (kernels of the per-step chain, launched with
+// launch_pdl): let the next kernel on the stream begin launching, then wait until
+// the previous kernel has completed and its writes are visible.  The first
+// statement of such a kernel, before any memory access, so every kernel body still
+// runs after its predecessor; only launch and block scheduling overlap.  A no-op
+// for a kernel launched without the attribute.
+__device__ __forceinline__ void pdl_entry()
+{
+    asm volatile("griddepcontrol.launch_dependents;\n\tgriddepcontrol.wait;" ::: "memory");
+}
+
 __device__ __forceinline__ void set_error(uint32_t *err, uint32_t bits)
 {
     if (err) atomicOr(err, bits);
