@@ -47,9 +47,9 @@ __device__ __forceinline__ void wendland_run(const DevParams &p, const float4 *_
     const uint32_t code = LIST ? shift_code(sx, sy, sz) : 0u;
     const float2 px = make_float2(pi.x, pi.x), py = make_float2(pi.y, pi.y),
                  pz = make_float2(pi.z, pi.z);
-    const float2 m1 = make_float2(-1.0f, -1.0f), half = make_float2(-0.5f, -0.5f),
-                 one = make_float2(1.0f, 1.0f), two = make_float2(2.0f, 2.0f),
-                 ih = make_float2(p.inv_h, p.inv_h), tiny = make_float2(1e-30f, 1e-30f);
+    const float2 m1 = make_float2(-1.0f, -1.0f), one = make_float2(1.0f, 1.0f),
+                 nh2 = make_float2(-0.5f * p.inv_h, -0.5f * p.inv_h),
+                 h2 = make_float2(2.0f * p.inv_h, 2.0f * p.inv_h), tiny = make_float2(1e-30f, 1e-30f);
     uint32_t j = b;
     for (; j + 1 < e; j += 2) {
         const float4 a = __ldg(spos + j), c = __ldg(spos + j + 1);
@@ -66,11 +66,11 @@ __device__ __forceinline__ void wendland_run(const DevParams &p, const float4 *_
         const float2 d2 = PLANAR ? dxy : __ffma2_rn(rz, rz, dxy);
         const float2 dt = __fadd2_rn(d2, tiny);  // d2 = 0 (the particle itself) gives q = 0
         const float2 rs = make_float2(rsqrtf(dt.x), rsqrtf(dt.y));
-        const float2 q = __fmul2_rn(__fmul2_rn(d2, rs), ih);
-        float2 t = __ffma2_rn(q, half, one);
+        const float2 d = __fmul2_rn(d2, rs);  // |r|; q = |r| / h enters through nh2, h2
+        float2 t = __ffma2_rn(d, nh2, one);   // 1 - q/2
         t = make_float2(fmaxf(t.x, 0.0f), fmaxf(t.y, 0.0f));  // 0 outside the support (q >= 2)
         const float2 t2 = __fmul2_rn(t, t);
-        const float2 w = __fmul2_rn(__fmul2_rn(t2, t2), __ffma2_rn(q, two, one));
+        const float2 w = __fmul2_rn(__fmul2_rn(t2, t2), __ffma2_rn(d, h2, one));  // ... (2q + 1)
         acc = __fadd2_rn(acc, w);
         if (LIST && record) {
             if (interacts<SYS, TRIM>(p, d2.x, a.w)) list_append(nl, i, cnt, j | code);
@@ -82,9 +82,9 @@ __device__ __forceinline__ void wendland_run(const DevParams &p, const float4 *_
         const float3 r = rel<SYS>(pi, pj, sx, sy, sz);
         const float dxy = __fmaf_rn(r.y, r.y, __fmul_rn(r.x, r.x));
         const float d2 = PLANAR ? dxy : __fmaf_rn(r.z, r.z, dxy);
-        const float q = __fmul_rn(__fmul_rn(d2, rsqrtf(__fadd_rn(d2, 1e-30f))), p.inv_h);
-        const float t = fmaxf(__fmaf_rn(q, -0.5f, 1.0f), 0.0f), t2 = __fmul_rn(t, t);
-        const float w = __fmul_rn(__fmul_rn(t2, t2), __fmaf_rn(q, 2.0f, 1.0f));
+        const float d = __fmul_rn(d2, rsqrtf(__fadd_rn(d2, 1e-30f)));
+        const float t = fmaxf(__fmaf_rn(d, -0.5f * p.inv_h, 1.0f), 0.0f), t2 = __fmul_rn(t, t);
+        const float w = __fmul_rn(__fmul_rn(t2, t2), __fmaf_rn(d, 2.0f * p.inv_h, 1.0f));
         acc.x = __fadd_rn(acc.x, w);
         if (LIST && record && interacts<SYS, TRIM>(p, d2, pj.w)) list_append(nl, i, cnt, j | code);
     }

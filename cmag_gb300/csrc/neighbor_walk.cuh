@@ -65,11 +65,11 @@ __device__ __forceinline__ bool row_runs(const DevParams &p, const uint32_t *__r
             dzm = fmaxf(dzm - kMargin, 0.0f);
         }
         dym = fmaxf(dym - kMargin, 0.0f);
-        const float r2 = p.support2_cells - dym * dym - dzm * dzm;
+        const float r2 = __fmaf_rn(-dzm, dzm, __fmaf_rn(-dym, dym, p.support2_cells));
         if (r2 <= 0.0f) return false;
         // conservative half width: the approximate square root errs by far less
         // than the margin
-        const float R = r2 * rsqrtf(r2) + kMargin;
+        const float R = __fmaf_rn(r2, rsqrtf(r2), kMargin);
         xa = max(xa, __float2int_rd(fx - R));
         xb = min(xb, __float2int_rd(fx + R));
         if (xa > xb) return false;
