@@ -135,15 +135,15 @@ __global__ void __launch_bounds__(256, 4)
                     if (!(d2 < p.support2)) return;
                     // pressure + Monaghan viscosity (fluid_kernel.cu:221-237)
                     const float inv_d = rsqrtf(d2);
-                    const float g = kernel_dw_over_r(p, d2 * inv_d * p.inv_h, inv_d);  // dW/dr / r
+                    const float g = kernel_dw_over_r(p, d2 * inv_d, inv_d);  // dW/dr / r
                     const float2 aj = __ldg(aux + j);
                     float s = pterm + aj.x;
                     const float4 vj = __ldg(svel + j);
                     const float vxy = __fmaf_rn(vi.y - vj.y, ry, (vi.x - vj.x) * rx);
                     const float vij = PLANAR ? vxy : __fmaf_rn(vi.z - vj.z, rz, vxy);
                     if (vij < 0.0f) {
-                        const float nu = __fdividef(p.av_coeff, ai.y + aj.y);
-                        s -= __fdividef(nu * vij, d2 + p.av_eps2);
+                        // viscosity 2 alpha h c0 v_ij / ((rho_i + rho_j)(r^2 + eps^2))
+                        s -= __fdividef(p.av_coeff * vij, (ai.y + aj.y) * (d2 + p.av_eps2));
                     }
                     s *= nmass * g;
                     ax = __fmaf_rn(s, rx, ax); ay = __fmaf_rn(s, ry, ay);
@@ -153,7 +153,7 @@ __global__ void __launch_bounds__(256, 4)
                     // pressure + Morris viscosity with wall extrapolation
                     // (poiseuilleFlowKernel.cu:184-208, 236-245)
                     const float inv_d = rsqrtf(d2);
-                    const float g = kernel_dw_over_r(p, d2 * inv_d * p.inv_h, inv_d);
+                    const float g = kernel_dw_over_r(p, d2 * inv_d, inv_d);
                     const float2 aj = __ldg(aux + j);
                     const float4 vj = __ldg(svel + j);
                     float vx, vy, vz;
@@ -176,7 +176,7 @@ __global__ void __launch_bounds__(256, 4)
                     // viscous (PeristalsisViscousForce.cu:206-213) and pressure
                     // (PeristalsisPressureForce.cu:39-43) from one pass
                     const float inv_d = rsqrtf(d2);
-                    const float g = kernel_dw_over_r(p, d2 * inv_d * p.inv_h, inv_d);
+                    const float g = kernel_dw_over_r(p, d2 * inv_d, inv_d);
                     const float2 aj = __ldg(aux + j);
                     const float4 vj = __ldg(svel + j);
                     const float sv = visc_i * aj.y * g;
@@ -212,8 +212,8 @@ __global__ void __launch_bounds__(256, 4)
                 return;
             }
             const float2 inv_d = make_float2(rsqrtf(d2.x), rsqrtf(d2.y));
-            const float2 q = __fmul2_rn(__fmul2_rn(d2, inv_d), make_float2(p.inv_h, p.inv_h));
-            const float2 t = __ffma2_rn(q, make_float2(-0.5f, -0.5f), make_float2(1.0f, 1.0f));
+            const float2 t = __ffma2_rn(__fmul2_rn(d2, inv_d), make_float2(p.nhalf_inv_h, p.nhalf_inv_h),
+                                        make_float2(1.0f, 1.0f));
             const float2 g = __fmul2_rn(make_float2(p.dwr_norm, p.dwr_norm), __fmul2_rn(__fmul2_rn(t, t), t));
             const float2 a0 = __ldg(aux + j0), a1 = __ldg(aux + j1);
             const float4 v0 = __ldg(svel + j0), v1 = __ldg(svel + j1);
@@ -224,12 +224,10 @@ __global__ void __launch_bounds__(256, 4)
             const float2 vij = PLANAR ? vxy
                                       : __ffma2_rn(__fadd2_rn(make_float2(vi.z, vi.z), make_float2(-v0.z, -v1.z)), rz, vxy);
             if (vij.x < 0.0f) {
-                const float nu = __fdividef(p.av_coeff, ai.y + a0.y);
-                sp.x -= __fdividef(nu * vij.x, d2.x + p.av_eps2);
+                sp.x -= __fdividef(p.av_coeff * vij.x, (ai.y + a0.y) * (d2.x + p.av_eps2));
             }
             if (vij.y < 0.0f) {
-                const float nu = __fdividef(p.av_coeff, ai.y + a1.y);
-                sp.y -= __fdividef(nu * vij.y, d2.y + p.av_eps2);
+                sp.y -= __fdividef(p.av_coeff * vij.y, (ai.y + a1.y) * (d2.y + p.av_eps2));
             }
             sp = __fmul2_rn(sp, __fmul2_rn(make_float2(nmass, nmass), g));
             ax = __fmaf_rn(sp.x, rx.x, ax); ay = __fmaf_rn(sp.x, ry.x, ay);
@@ -255,8 +253,8 @@ __global__ void __launch_bounds__(256, 4)
                 return;
             }
             const float2 inv_d = make_float2(rsqrtf(d2.x), rsqrtf(d2.y));
-            const float2 q = __fmul2_rn(__fmul2_rn(d2, inv_d), make_float2(p.inv_h, p.inv_h));
-            const float2 t = __ffma2_rn(q, make_float2(-0.5f, -0.5f), make_float2(1.0f, 1.0f));
+            const float2 t = __ffma2_rn(__fmul2_rn(d2, inv_d), make_float2(p.nhalf_inv_h, p.nhalf_inv_h),
+                                        make_float2(1.0f, 1.0f));
             const float2 g = __fmul2_rn(make_float2(p.dwr_norm, p.dwr_norm), __fmul2_rn(__fmul2_rn(t, t), t));
             const float2 a0 = __ldg(aux + j0), a1 = __ldg(aux + j1);
             const float4 v0 = __ldg(svel + j0), v1 = __ldg(svel + j1);
@@ -291,8 +289,8 @@ __global__ void __launch_bounds__(256, 4)
                 return;
             }
             const float2 inv_d = make_float2(rsqrtf(d2.x), rsqrtf(d2.y));
-            const float2 q = __fmul2_rn(__fmul2_rn(d2, inv_d), make_float2(p.inv_h, p.inv_h));
-            const float2 t = __ffma2_rn(q, make_float2(-0.5f, -0.5f), make_float2(1.0f, 1.0f));
+            const float2 t = __ffma2_rn(__fmul2_rn(d2, inv_d), make_float2(p.nhalf_inv_h, p.nhalf_inv_h),
+                                        make_float2(1.0f, 1.0f));
             const float2 g = __fmul2_rn(make_float2(p.dwr_norm, p.dwr_norm), __fmul2_rn(__fmul2_rn(t, t), t));
             const float2 a0 = __ldg(aux + j0), a1 = __ldg(aux + j1);
             const float4 v0 = __ldg(svel + j0), v1 = __ldg(svel + j1);

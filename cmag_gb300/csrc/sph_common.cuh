@@ -37,6 +37,7 @@ struct DevParams {
     float av_alpha, av_eps2;      // artificial viscosity alpha, 0.001 h^2
     float w_norm, dw_norm;        // kernel normalisations (see kernel_w/kernel_dw)
     float dwr_norm;               // Wendland dW/dr / r = dwr_norm (1 - q/2)^3 (kernel_dw_over_r)
+    float nhalf_inv_h;            // -1 / (2h): 1 - q/2 = 1 + r * nhalf_inv_h
     float wall_bottom, wall_top;  // Poiseuille extrapolation lines
     float amplitude, wave_k, wave_speed, half_fluid_h;  // Peristalsis wall law
     float half_world_x;
@@ -179,16 +180,16 @@ __device__ __forceinline__ float kernel_dw(const DevParams &p, float q)
     return p.dw_norm * (-0.75f * t * t);
 }
 
-// dW/dr / r for 0 < q < 2 (q = r / h, inv_r = 1 / r).  Wendland: since q / r =
+// dW/dr / r at distance r (inv_r = 1 / r, 0 < r < 2h).  Wendland: since q / r =
 // 1 / h, -2.5 dw_norm q (1-q/2)^3 / r = dwr_norm (1-q/2)^3 with dwr_norm =
-// -2.5 dw_norm / h (one multiply instead of three).
-__device__ __forceinline__ float kernel_dw_over_r(const DevParams &p, float q, float inv_r)
+// -2.5 dw_norm / h, and 1 - q/2 = fma(r, -1/(2h), 1).
+__device__ __forceinline__ float kernel_dw_over_r(const DevParams &p, float r, float inv_r)
 {
     if (p.kernel == CMAG_KERNEL_WENDLAND) {
-        const float t = __fmaf_rn(q, -0.5f, 1.0f);
+        const float t = __fmaf_rn(r, p.nhalf_inv_h, 1.0f);
         return p.dwr_norm * (t * t * t);
     }
-    return kernel_dw(p, q) * inv_r;
+    return kernel_dw(p, r * p.inv_h) * inv_r;
 }
 
 // Equation of state (fluid_kernel.cu:168, poiseuilleFlowKernel.cu:181,

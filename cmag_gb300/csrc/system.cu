@@ -177,6 +177,7 @@ DevParams make_dev_params(const cmag_sph_params &p, uint32_t n, const SceneLayou
     d.w_norm = (float)wn;
     d.dw_norm = (float)dwn;
     d.dwr_norm = (float)(-2.5 * dwn / h);
+    d.nhalf_inv_h = -0.5f * d.inv_h;
     d.wall_bottom = p.world_origin[1] + p.boundary_offset * 2.0f * p.particle_radius;
     d.wall_top = d.wall_bottom + p.fluid_size[1] * 2.0f * p.particle_radius;
     d.amplitude = p.amplitude;
