@@ -49,7 +49,7 @@ enum cmag_status {
 
 /* device-side check bits, reported by cmag_system_synchronize() */
 enum cmag_device_error {
-    CMAG_DEVERR_LOOKBACK_TIMEOUT = 1, /* a sort/scan look-back wait hit its spin limit */
+    CMAG_DEVERR_LOOKBACK_TIMEOUT = 1, /* a look-back wait of the radix sort (cmag_sort_particles) hit its spin limit */
     CMAG_DEVERR_RANGE = 2             /* an index left its buffer; access skipped       */
 };
 
