@@ -71,10 +71,13 @@ __device__ __forceinline__ WallSide wall_side(const DevParams &p, float amp, flo
 }
 
 // ------------------------------------------------------------------ force --
-// 256 threads; 5 blocks per SM (at most 48 registers: room to hide the gathers'
-// latency), 4 for 3-D Peristalsis (at most 64: its two 3-D force sums would spill)
+// 256 threads, as many blocks per SM as each family fits without (large) spills,
+// to hide the gathers' latency: DamBreak and planar Poiseuille 6 (40 registers),
+// planar Peristalsis and 3-D Poiseuille 5 (48), 3-D Peristalsis 4 (64: its two
+// 3-D force sums)
 template <int SYS, bool PLANAR, bool TRIM, int G, bool BATCH, bool LIST>
-__global__ void __launch_bounds__(256, (SYS == CMAG_PERISTALSIS && !PLANAR) ? 4 : (SYS == CMAG_DAMBREAK ? 6 : 5))
+__global__ void __launch_bounds__(256, SYS == CMAG_PERISTALSIS ? (PLANAR ? 5 : 4)
+                                                               : ((SYS == CMAG_DAMBREAK || PLANAR) ? 6 : 5))
     k_force(DevParams pv, BatchView bv, const float4 *__restrict__ spos,
             const float4 *__restrict__ svel, const float2 *__restrict__ aux,
             const uint32_t *__restrict__ idx, const uint32_t *__restrict__ off_all,
