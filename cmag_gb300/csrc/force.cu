@@ -316,12 +316,14 @@ __global__ void __launch_bounds__(256, SYS == CMAG_PERISTALSIS ? (PLANAR ? 5 : 4
         auto extrapolated = [&](const float4 &q) {
             return q.w == 1.0f && (q.y > p.wall_top || q.y < p.wall_bottom);
         };
-        // image shift of a list entry (2 bits per axis above the index)
+        // image shift of a list entry (2 bits per axis above the index); the code of
+        // an unshifted entry decodes to exact zeros
         auto entry_shift = [&](uint32_t en) {
             const uint32_t cd = en >> kListIndexBits;
             return make_float3((float)((int)(cd & 3u) - 1) * p.wsx, (float)((int)((cd >> 2) & 3u) - 1) * p.wsy,
-                               (float)((int)((cd >> 4) & 3u) - 1) * p.wsz);
+                               PLANAR ? 0.0f : (float)((int)((cd >> 4) & 3u) - 1) * p.wsz);
         };
+        constexpr uint32_t kNoShift = 1u | (1u << 2) | (1u << 4);
         const uint32_t cnt = LIST ? __ldg(nl.count + i) : 0u;
         if (LIST && cnt <= nl.cap) {
             // the density pass's list: the walk's interacting candidates, same order
@@ -354,7 +356,9 @@ __global__ void __launch_bounds__(256, SYS == CMAG_PERISTALSIS ? (PLANAR ? 5 : 4
                             pair(j1, q1, 0.0f, 0.0f, 0.0f);
                         }
                     } else if (SYS == CMAG_POISEUILLE) {
-                        const float sx0 = entry_shift(c0 << kListIndexBits).x, sx1 = entry_shift(c1 << kListIndexBits).x;
+                        const bool unshifted = c0 == kNoShift && c1 == kNoShift;
+                        const float sx0 = unshifted ? 0.0f : entry_shift(c0 << kListIndexBits).x;
+                        const float sx1 = unshifted ? 0.0f : entry_shift(c1 << kListIndexBits).x;
                         if (!extrapolated(q0) && !extrapolated(q1)) {
                             poi_pair2(j0, q0, sx0, j1, q1, sx1);
                         } else {
@@ -362,7 +366,11 @@ __global__ void __launch_bounds__(256, SYS == CMAG_PERISTALSIS ? (PLANAR ? 5 : 4
                             pair(j1, q1, sx1, 0.0f, 0.0f);
                         }
                     } else {
-                        const float3 s0 = entry_shift(c0 << kListIndexBits), s1 = entry_shift(c1 << kListIndexBits);
+                        float3 s0 = make_float3(0.0f, 0.0f, 0.0f), s1 = s0;
+                        if (!(c0 == kNoShift && c1 == kNoShift)) {  // near a periodic boundary
+                            s0 = entry_shift(c0 << kListIndexBits);
+                            s1 = entry_shift(c1 << kListIndexBits);
+                        }
                         if (!noslip || (q0.w == 0.0f && q1.w == 0.0f)) {
                             peri_pair2(j0, q0, s0, j1, q1, s1);
                         } else {  // wall neighbours of the no-slip extrapolation
