@@ -73,8 +73,9 @@ __device__ __forceinline__ void wendland_run(const DevParams &p, const float4 *_
         const float2 w = __fmul2_rn(__fmul2_rn(t2, t2), __ffma2_rn(d, h2, one));  // ... (2q + 1)
         acc = __fadd2_rn(acc, w);
         if (LIST && record) {
-            if (interacts<SYS, TRIM>(p, d2.x, a.w)) list_append(nl, i, cnt, j | code);
-            if (interacts<SYS, TRIM>(p, d2.y, c.w)) list_append(nl, i, cnt, (j + 1) | code);
+            const uint32_t v = j | code;  // j + 1 < 2^26: the next entry is v + 1
+            if (interacts<SYS, TRIM>(p, d2.x, a.w)) list_append(nl, i, cnt, v);
+            if (interacts<SYS, TRIM>(p, d2.y, c.w)) list_append(nl, i, cnt, v + 1u);
         }
     }
     if (j < e) {  // the same operations as one half of a pair step

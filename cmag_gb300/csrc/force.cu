@@ -72,12 +72,11 @@ __device__ __forceinline__ WallSide wall_side(const DevParams &p, float amp, flo
 
 // ------------------------------------------------------------------ force --
 // 256 threads, as many blocks per SM as each family fits without (large) spills,
-// to hide the gathers' latency: DamBreak and planar Poiseuille 6 (40 registers),
-// planar Peristalsis and 3-D Poiseuille 5 (48), 3-D Peristalsis 4 (64: its two
-// 3-D force sums)
+// to hide the gathers' latency: planar DamBreak and Poiseuille 6 (40 registers),
+// planar Peristalsis and 3-D DamBreak and Poiseuille 5 (48), 3-D Peristalsis 4
+// (64: its two 3-D force sums)
 template <int SYS, bool PLANAR, bool TRIM, int G, bool BATCH, bool LIST>
-__global__ void __launch_bounds__(256, SYS == CMAG_PERISTALSIS ? (PLANAR ? 5 : 4)
-                                                               : ((SYS == CMAG_DAMBREAK || PLANAR) ? 6 : 5))
+__global__ void __launch_bounds__(256, SYS == CMAG_PERISTALSIS ? (PLANAR ? 5 : 4) : (PLANAR ? 6 : 5))
     k_force(DevParams pv, BatchView bv, const float4 *__restrict__ spos,
             const float4 *__restrict__ svel, const float2 *__restrict__ aux,
             const uint32_t *__restrict__ idx, const uint32_t *__restrict__ off_all,
@@ -201,19 +200,34 @@ __global__ void __launch_bounds__(256, SYS == CMAG_PERISTALSIS ? (PLANAR ? 5 : 4
                     if (!PLANAR) bz = __fmaf_rn(sp, rz, bz);
                 }
             };
-        // DamBreak list entries j0, j1 that are both fluid: the pair terms of both in
-        // paired FP32, each operation the scalar pair's (same bits), added to the
-        // sums in list order
-        auto fluid_pair2 = [&](uint32_t j0, const float4 &q0, uint32_t j1, const float4 &q1) {
+        // DamBreak list entries j0, j1, fluid or wall: the pair terms of both in paired
+        // FP32, each operation the scalar pair's (same bits), added in list order.
+        // Wall entries take the Lennard-Jones term; it is computed only when a lane
+        // of the warp has one, so wall neighbours do not split the warp between the
+        // paired and the scalar path.
+        auto dam_pair2 = [&](uint32_t j0, const float4 &q0, uint32_t j1, const float4 &q1) {
             const float2 rx = __fadd2_rn(make_float2(pi.x, pi.x), make_float2(-q0.x, -q1.x));
             const float2 ry = __fadd2_rn(make_float2(pi.y, pi.y), make_float2(-q0.y, -q1.y));
             const float2 rz = __fadd2_rn(make_float2(pi.z, pi.z), make_float2(-q0.z, -q1.z));
             const float2 dxy = __ffma2_rn(ry, ry, __fmul2_rn(rx, rx));
             const float2 d2 = PLANAR ? dxy : __ffma2_rn(rz, rz, dxy);
-            if (!(d2.x > 0.0f && d2.y > 0.0f && d2.x < p.support2 && d2.y < p.support2)) {
-                pair(j0, q0, 0.0f, 0.0f, 0.0f);  // not both plain fluid pairs
+            const bool w0 = q0.w != (float)CMAG_FLUID, w1 = q1.w != (float)CMAG_FLUID;
+            // plain pair terms: d2 > 0, inside the support unless an un-cut wall
+            const bool ok0 = d2.x > 0.0f && (d2.x < p.support2 || (w0 && !TRIM));
+            const bool ok1 = d2.y > 0.0f && (d2.y < p.support2 || (w1 && !TRIM));
+            if (!(ok0 && ok1)) {
+                pair(j0, q0, 0.0f, 0.0f, 0.0f);
                 pair(j1, q1, 0.0f, 0.0f, 0.0f);
                 return;
+            }
+            float2 slj = make_float2(0.0f, 0.0f);
+            if (__any_sync(__activemask(), w0 || w1)) {  // Lennard-Jones (fluid_kernel.cu:199-207)
+                const float2 inv_d2 = make_float2(__frcp_rn(d2.x), __frcp_rn(d2.y));
+                const float2 a2 = __fmul2_rn(make_float2(p.lj_a2, p.lj_a2), inv_d2);
+                const float2 a6 = __fmul2_rn(__fmul2_rn(a2, a2), a2);
+                slj = __fmul2_rn(__fmul2_rn(make_float2(p.lj_D, p.lj_D),
+                                            __ffma2_rn(a6, a6, make_float2(-a6.x, -a6.y))),
+                                 inv_d2);
             }
             const float2 inv_d = make_float2(rsqrtf(d2.x), rsqrtf(d2.y));
             const float2 t = __ffma2_rn(__fmul2_rn(d2, inv_d), make_float2(p.nhalf_inv_h, p.nhalf_inv_h),
@@ -227,17 +241,18 @@ __global__ void __launch_bounds__(256, SYS == CMAG_PERISTALSIS ? (PLANAR ? 5 : 4
             const float2 vxy = __ffma2_rn(dvy, ry, __fmul2_rn(dvx, rx));
             const float2 vij = PLANAR ? vxy
                                       : __ffma2_rn(__fadd2_rn(make_float2(vi.z, vi.z), make_float2(-v0.z, -v1.z)), rz, vxy);
-            if (vij.x < 0.0f) {
+            if (vij.x < 0.0f && !w0) {
                 sp.x -= __fdividef(p.av_coeff * vij.x, (ai.y + a0.y) * (d2.x + p.av_eps2));
             }
-            if (vij.y < 0.0f) {
+            if (vij.y < 0.0f && !w1) {
                 sp.y -= __fdividef(p.av_coeff * vij.y, (ai.y + a1.y) * (d2.y + p.av_eps2));
             }
             sp = __fmul2_rn(sp, __fmul2_rn(make_float2(nmass, nmass), g));
-            ax = __fmaf_rn(sp.x, rx.x, ax); ay = __fmaf_rn(sp.x, ry.x, ay);
-            if (!PLANAR) az = __fmaf_rn(sp.x, rz.x, az);
-            ax = __fmaf_rn(sp.y, rx.y, ax); ay = __fmaf_rn(sp.y, ry.y, ay);
-            if (!PLANAR) az = __fmaf_rn(sp.y, rz.y, az);
+            const float s0 = w0 ? slj.x : sp.x, s1 = w1 ? slj.y : sp.y;
+            ax = __fmaf_rn(s0, rx.x, ax); ay = __fmaf_rn(s0, ry.x, ay);
+            if (!PLANAR) az = __fmaf_rn(s0, rz.x, az);
+            ax = __fmaf_rn(s1, rx.y, ax); ay = __fmaf_rn(s1, ry.y, ay);
+            if (!PLANAR) az = __fmaf_rn(s1, rz.y, az);
         };
         // Peristalsis list entries j0, j1 (image shifts s0, s1): both pair terms in
         // paired FP32, each operation the scalar pair's (same bits), added in order
@@ -349,12 +364,7 @@ __global__ void __launch_bounds__(256, SYS == CMAG_PERISTALSIS ? (PLANAR ? 5 : 4
                     e1 = n1;
                     const float4 q0 = __ldg(spos + j0), q1 = __ldg(spos + j1);
                     if (SYS == CMAG_DAMBREAK) {
-                        if (q0.w == (float)CMAG_FLUID && q1.w == (float)CMAG_FLUID) {
-                            fluid_pair2(j0, q0, j1, q1);
-                        } else {
-                            pair(j0, q0, 0.0f, 0.0f, 0.0f);
-                            pair(j1, q1, 0.0f, 0.0f, 0.0f);
-                        }
+                        dam_pair2(j0, q0, j1, q1);
                     } else if (SYS == CMAG_POISEUILLE) {
                         const bool unshifted = c0 == kNoShift && c1 == kNoShift;
                         const float sx0 = unshifted ? 0.0f : entry_shift(c0 << kListIndexBits).x;
