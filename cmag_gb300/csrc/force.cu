@@ -291,9 +291,14 @@ __global__ void __launch_bounds__(256, SYS == CMAG_PERISTALSIS ? (PLANAR ? 5 : 4
                 az = __fmaf_rn(sv.y, vi.z - v1.z, az); bz = __fmaf_rn(sp.y, rz.y, bz);
             }
         };
-        // Poiseuille list entries j0, j1 (x image shifts sx0, sx1) outside the wall
-        // extrapolation: both pair terms in paired FP32, each operation the scalar
-        // pair's (same bits), added in order
+        // a Poiseuille wall particle beyond the extrapolation lines
+        auto extrapolated = [&](const float4 &q) {
+            return q.w == 1.0f && (q.y > p.wall_top || q.y < p.wall_bottom);
+        };
+        // Poiseuille list entries j0, j1 (x image shifts sx0, sx1): both pair terms in
+        // paired FP32, each operation the scalar pair's (same bits), added in order.
+        // A wall entry beyond an extrapolation line takes beta v_i for v_i - v_j
+        // (computed only when a lane of the warp has one).
         auto poi_pair2 = [&](uint32_t j0, const float4 &q0, float sx0, uint32_t j1, const float4 &q1,
                              float sx1) {
             const float2 tx = __fadd2_rn(make_float2(q0.x, q1.x), make_float2(sx0, sx1));
@@ -313,8 +318,26 @@ __global__ void __launch_bounds__(256, SYS == CMAG_PERISTALSIS ? (PLANAR ? 5 : 4
             const float2 g = __fmul2_rn(make_float2(p.dwr_norm, p.dwr_norm), __fmul2_rn(__fmul2_rn(t, t), t));
             const float2 a0 = __ldg(aux + j0), a1 = __ldg(aux + j1);
             const float4 v0 = __ldg(svel + j0), v1 = __ldg(svel + j1);
-            const float2 vx = __fadd2_rn(make_float2(vi.x, vi.x), make_float2(-v0.x, -v1.x));
-            const float2 vy = __fadd2_rn(make_float2(vi.y, vi.y), make_float2(-v0.y, -v1.y));
+            float2 vx = __fadd2_rn(make_float2(vi.x, vi.x), make_float2(-v0.x, -v1.x));
+            float2 vy = __fadd2_rn(make_float2(vi.y, vi.y), make_float2(-v0.y, -v1.y));
+            float vz0 = vi.z - v0.z, vz1 = vi.z - v1.z;
+            const bool e0 = extrapolated(q0), e1 = extrapolated(q1);
+            if (__any_sync(__activemask(), e0 || e1)) {  // poiseuilleFlowKernel.cu:184-208
+                auto beta_of = [&](const float4 &q) {
+                    const bool top = q.y > p.wall_top;
+                    const float da = top ? p.wall_top - pi.y : pi.y - p.wall_bottom;
+                    const float db = top ? q.y - p.wall_top : p.wall_bottom - q.y;
+                    return fminf(1000.0f, 1.0f + __fdividef(db, da));
+                };
+                if (e0) {
+                    const float b = beta_of(q0);
+                    vx.x = b * vi.x; vy.x = b * vi.y; vz0 = b * vi.z;
+                }
+                if (e1) {
+                    const float b = beta_of(q1);
+                    vx.y = b * vi.x; vy.y = b * vi.y; vz1 = b * vi.z;
+                }
+            }
             const float2 sp = __fmul2_rn(__fmul2_rn(make_float2(nmass, nmass), g),
                                          __fadd2_rn(make_float2(pterm, pterm), make_float2(a0.x, a1.x)));
             const float2 sv = __fmul2_rn(__fmul2_rn(make_float2(visc_i, visc_i), make_float2(a0.y, a1.y)), g);
@@ -323,13 +346,9 @@ __global__ void __launch_bounds__(256, SYS == CMAG_PERISTALSIS ? (PLANAR ? 5 : 4
             ax = __fmaf_rn(sv.y, vx.y, __fmaf_rn(sp.y, rx.y, ax));
             ay = __fmaf_rn(sv.y, vy.y, __fmaf_rn(sp.y, ry.y, ay));
             if (!PLANAR) {
-                az = __fmaf_rn(sv.x, vi.z - v0.z, __fmaf_rn(sp.x, rz.x, az));
-                az = __fmaf_rn(sv.y, vi.z - v1.z, __fmaf_rn(sp.y, rz.y, az));
+                az = __fmaf_rn(sv.x, vz0, __fmaf_rn(sp.x, rz.x, az));
+                az = __fmaf_rn(sv.y, vz1, __fmaf_rn(sp.y, rz.y, az));
             }
-        };
-        // a Poiseuille wall particle beyond the extrapolation lines
-        auto extrapolated = [&](const float4 &q) {
-            return q.w == 1.0f && (q.y > p.wall_top || q.y < p.wall_bottom);
         };
         // image shift of a list entry (2 bits per axis above the index); the code of
         // an unshifted entry decodes to exact zeros
@@ -369,12 +388,7 @@ __global__ void __launch_bounds__(256, SYS == CMAG_PERISTALSIS ? (PLANAR ? 5 : 4
                         const bool unshifted = c0 == kNoShift && c1 == kNoShift;
                         const float sx0 = unshifted ? 0.0f : entry_shift(c0 << kListIndexBits).x;
                         const float sx1 = unshifted ? 0.0f : entry_shift(c1 << kListIndexBits).x;
-                        if (!extrapolated(q0) && !extrapolated(q1)) {
-                            poi_pair2(j0, q0, sx0, j1, q1, sx1);
-                        } else {
-                            pair(j0, q0, sx0, 0.0f, 0.0f);
-                            pair(j1, q1, sx1, 0.0f, 0.0f);
-                        }
+                        poi_pair2(j0, q0, sx0, j1, q1, sx1);
                     } else {
                         float3 s0 = make_float3(0.0f, 0.0f, 0.0f), s1 = s0;
                         if (!(c0 == kNoShift && c1 == kNoShift)) {  // near a periodic boundary
