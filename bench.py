@@ -507,6 +507,8 @@ def main():
     ap.add_argument("--train-seeds", type=int, default=3)
     ap.add_argument("--train-steps", type=int, default=3000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--neighbor-lists", choices=["auto", "on", "off"], default="auto",
+                    help="single-scene workloads: the autotuner's choice, or force interaction lists on/off")
     ap.add_argument("--cpu-steps", type=int, default=1)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -549,6 +551,12 @@ def main():
     # particle of the neighbour loops on this workload
     s.update_n(args.warmup)
     cfg["lanes_density_force"] = list(s.autotune(3))
+    if args.neighbor_lists != "auto" and not batched:
+        # a fixed choice (e.g. for profiles, where ncu's serialised launches skew
+        # the autotuner's timings): one lane per particle with or without lists
+        s.set_groups(1, 1)
+        s.set_neighbor_lists(args.neighbor_lists == "on")
+        cfg["lanes_density_force"] = [1, 1, args.neighbor_lists == "on"]
     s.update_n(2)
     s.synchronize()
 
