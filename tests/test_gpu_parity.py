@@ -187,6 +187,32 @@ def test_interaction_lists_equal_the_walk(gpu, name, cap):
     s2.close()
 
 
+@pytest.mark.parametrize("name", ["dambreak", "peristalsis"])
+def test_state_round_trip_through_host_buffers(gpu, name):
+    """A planar scene reloaded through setArray (whose z checks run on the device)
+    keeps its one-layer search: it steps bit for bit like its twin; getArray fills a
+    caller buffer with the same rows it returns."""
+    s1, _ = SCENES[name]()
+    s2, _ = SCENES[name]()
+    s1.set_groups(1, 1)
+    s2.set_groups(1, 1)
+    s1.update_n(3)
+    s2.update_n(3)
+    s2.load_state(s1.state())
+    s2.set_elapsed_time(s1.getElapsedTime())
+    s1.update_n(5)
+    s2.update_n(5)
+    for a in (cm.POSITION, cm.VELOCITY, cm.MEASURES):
+        assert_int_equal(s2.getArray(a).view(np.uint32), s1.getArray(a).view(np.uint32), "%s array %d" % (name, a))
+    buf = np.full((s1.getNumParticles(), 4), np.nan, np.float32)
+    out = s1.getArray(cm.POSITION, out=buf)
+    assert out is buf and np.array_equal(buf, s1.getArray(cm.POSITION))
+    with pytest.raises(ValueError):
+        s1.getArray(cm.POSITION, out=np.zeros((3, 4), np.float32))
+    s1.close()
+    s2.close()
+
+
 @pytest.mark.parametrize("graphs", [True, False])
 def test_graph_replay_equals_plain_launches(gpu, graphs):
     """A captured-and-replayed step produces the same bits as plain launches."""
