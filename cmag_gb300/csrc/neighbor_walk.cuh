@@ -45,27 +45,55 @@ struct RowRuns {
     float sx0, sx1, sy, sz;
 };
 
-// Row (dy, dz) of particle (fx,fy,fz) (fractional cell coordinates) in cell g.
-// Returns false when the row holds no candidates.
+// What a row walk keeps per z slab of the cell box: the support radius squared
+// (cells) left after the slab's z distance, the slab's table row base and its
+// periodic image shift.
+struct Slab {
+    float r2z;      // support^2 - dz_min^2, in cells^2 (trimming only)
+    uint32_t base;  // wrapped z cell * gy
+    float sz;
+};
+
+// The trim's distance term along one axis: the distance in cells from the
+// particle at f to the band of cells [u, u + 1), less the margin, is
+// max(t, -1 - 2 margin - t, 0) with t = u - f - margin (u above f: the band's
+// near edge; below: its far edge; the particle's own band: 0).
+__device__ __forceinline__ float band_gap(float t)
+{
+    return fmaxf(fmaxf(t, (-1.0f - 2.0f * kMargin) - t), 0.0f);
+}
+
+template <int SYS, bool PLANAR, bool TRIM>
+__device__ __forceinline__ Slab slab_at(const DevParams &p, int dz, int gz, float fz)
+{
+    Slab sl;
+    const int zu = gz + dz;
+    sl.base = (PLANAR ? p.planar_layer : wrap_axis(zu, p.gz)) * p.gy;
+    sl.sz = (SYS == CMAG_PERISTALSIS && !PLANAR) ? (float)eval_shift(zu, p.gz) * p.wsz : 0.0f;
+    if (TRIM) {
+        const float dzm = PLANAR ? 0.0f : band_gap(((float)zu - fz) - kMargin);
+        sl.r2z = __fmaf_rn(-dzm, dzm, p.support2_cells);
+    } else {
+        sl.r2z = 0.0f;
+    }
+    return sl;
+}
+
+// Row (dy, dz) of particle (fx,fy,fz) (fractional cell coordinates) in cell g,
+// with the row's slab terms in sl.  Returns false when the row holds no
+// candidates.
 template <int SYS, bool PLANAR, bool TRIM>
 __device__ __forceinline__ bool row_runs(const DevParams &p, const uint32_t *__restrict__ off,
-                                         int dy, int dz, int3 g, float fx, float fy, float fz,
+                                         int dy, const Slab &sl, int3 g, float fx, float fy,
                                          RowRuns &rr)
 {
     const int c = p.cell_count;
-    const int yu = g.y + dy, zu = g.z + dz;
+    const int yu = g.y + dy;
     int xa = g.x - c, xb = g.x + c;
     if (TRIM) {
-        float dym = 0.0f, dzm = 0.0f;
-        if (dy > 0) dym = (float)yu - fy;
-        if (dy < 0) dym = fy - (float)(yu + 1);
-        if (!PLANAR) {
-            if (dz > 0) dzm = (float)zu - fz;
-            if (dz < 0) dzm = fz - (float)(zu + 1);
-            dzm = fmaxf(dzm - kMargin, 0.0f);
-        }
-        dym = fmaxf(dym - kMargin, 0.0f);
-        const float r2 = __fmaf_rn(-dzm, dzm, __fmaf_rn(-dym, dym, p.support2_cells));
+        const float dym = band_gap(((float)yu - fy) - kMargin);
+        // planar scenes: one slab, its terms straight from the parameters
+        const float r2 = __fmaf_rn(-dym, dym, PLANAR ? p.support2_cells : sl.r2z);
         if (r2 <= 0.0f) return false;
         // conservative half width: the approximate square root errs by far less
         // than the margin
@@ -74,11 +102,11 @@ __device__ __forceinline__ bool row_runs(const DevParams &p, const uint32_t *__r
         xb = min(xb, __float2int_rd(fx + R));
         if (xa > xb) return false;
     }
-    const uint32_t zm = PLANAR ? p.planar_layer : wrap_axis(zu, p.gz);
-    const uint32_t row = (zm * p.gy + wrap_axis(yu, p.gy)) * p.gx - p.scan_base;
+    const uint32_t zbase = PLANAR ? p.planar_layer * p.gy : sl.base;
+    const uint32_t row = (zbase + wrap_axis(yu, p.gy)) * p.gx - p.scan_base;
     if (row >= p.scan_cells) return false;  // outside the offset table: no particles
     rr.sy = (SYS == CMAG_PERISTALSIS) ? (float)eval_shift(yu, p.gy) * p.wsy : 0.0f;
-    rr.sz = (SYS == CMAG_PERISTALSIS && !PLANAR) ? (float)eval_shift(zu, p.gz) * p.wsz : 0.0f;
+    rr.sz = PLANAR ? 0.0f : sl.sz;
     const uint32_t xma = wrap_axis(xa, p.gx);
     const uint32_t len = (uint32_t)(xb - xa);
     rr.sx0 = (SYS == CMAG_DAMBREAK) ? 0.0f : (float)eval_shift(xa, p.gx) * p.wsx;
@@ -97,7 +125,8 @@ __device__ __forceinline__ bool row_runs(const DevParams &p, const uint32_t *__r
 }
 
 // Calls visit_run(b, e, sx, sy, sz) for every run of the rows this lane owns
-// (rows r = lane, lane + G, ... of the (2c+1)^2 box, dy fastest).
+// (rows r = lane, lane + G, ... of the (2c+1)^2 box, dy fastest).  The slab
+// terms are recomputed when a lane's row moves to the next z slab.
 template <int SYS, bool PLANAR, bool TRIM, int G, class VisitRun>
 __device__ __forceinline__ void for_each_run(const DevParams &p, const uint32_t *__restrict__ off,
                                              int lane, int3 g, float3 f, VisitRun &&visit_run)
@@ -107,16 +136,21 @@ __device__ __forceinline__ void for_each_run(const DevParams &p, const uint32_t 
     int dy = (G == 1) ? -c : (lane % w) - c;
     int dz = PLANAR ? 0 : ((G == 1) ? -c : (lane / w) - c);
     const int nrows = rows_of<PLANAR>(c);
+    Slab sl;
+    if (!PLANAR) sl = slab_at<SYS, PLANAR, TRIM>(p, dz, g.z, f.z);
     for (int r = lane; r < nrows; r += G) {
         RowRuns rr;
-        if (row_runs<SYS, PLANAR, TRIM>(p, off, dy, dz, g, f.x, f.y, f.z, rr)) {
+        if (row_runs<SYS, PLANAR, TRIM>(p, off, dy, sl, g, f.x, f.y, rr)) {
             visit_run(rr.b0, rr.e0, rr.sx0, rr.sy, rr.sz);
             if (rr.e1 > rr.b1) visit_run(rr.b1, rr.e1, rr.sx1, rr.sy, rr.sz);
         }
         dy += G;
-        while (dy > c) {
-            dy -= w;
-            ++dz;
+        if (dy > c) {
+            do {
+                dy -= w;
+                ++dz;
+            } while (dy > c);
+            if (!PLANAR) sl = slab_at<SYS, PLANAR, TRIM>(p, dz, g.z, f.z);
         }
     }
 }
