@@ -92,11 +92,11 @@ __device__ __forceinline__ void wendland_run(const DevParams &p, const float4 *_
 }
 
 // ---------------------------------------------------------------- density --
-// 256 threads; a single planar or 3-D DamBreak scene 8 blocks per SM (32
-// registers: the 3-D variants spill a few words to L1 and still run faster than
-// at 6 blocks), the rest 6
+// 256 threads; planar scenes (single or batched) and single 3-D DamBreak scenes
+// 8 blocks per SM (32 registers: the batch and 3-D variants spill a few words to
+// L1 and still run faster than at 6 blocks), the rest 6
 template <int SYS, bool PLANAR, bool TRIM, int G, bool BATCH, bool LIST>
-__global__ void __launch_bounds__(256, (!BATCH && (PLANAR || SYS == CMAG_DAMBREAK)) ? 8 : 6)
+__global__ void __launch_bounds__(256, (PLANAR || (!BATCH && SYS == CMAG_DAMBREAK)) ? 8 : 6)
     k_density(DevParams pv, BatchView bv, const float4 *__restrict__ spos,
               const uint32_t *__restrict__ off_all, float4 *__restrict__ meas,
               float2 *__restrict__ aux, NeighborList nl)
