@@ -172,6 +172,57 @@ def gpu_selector():
         return None
 
 
+DATA = "synthetic (seeded lattices + jitter, seed 1973)"
+
+# C2: the 64x128x64 column in a 256x192x64-cell tank with 3 wall layers
+DAMBREAK3D_TANK, DAMBREAK3D_LAYERS = (256, 192, 64), 3
+
+
+def working_set_note(n, cells):
+    """Working set of the step (seven float4 particle arrays, four uint32 ones,
+    two uint32 cell tables): above the 126 MB L2, so no flush between steps."""
+    mb = (n * (7 * 16 + 4 * 4) + 8 * cells) / 1e6
+    return "inputs larger than L2 (working set %.0f MB)" % mb
+
+
+def workload_config(name, p, n):
+    """The `config` object of a single-scene workload, from its parameter block
+    (both arms print the same one)."""
+    grid = [int(v) for v in p.grid_size]
+    cells = grid[0] * grid[1] * grid[2]
+    if name == "dambreak3d":
+        cfg = {"workload": "dambreak3d", "fluid": [int(v) for v in p.fluid_size],
+               "tank_cells": list(DAMBREAK3D_TANK), "wall_layers": DAMBREAK3D_LAYERS, "particles": n,
+               "h_over_dx": 1.3, "kernel": "wendland-3d", "eos": "tait gamma 7, c0 = 10 sqrt(2gH)",
+               "alpha": round(float(p.av_alpha), 6), "dt": float(p.delta_time), "grid": grid}
+    elif name == "peristalsis":
+        cfg = {"workload": "peristalsis2d", "fluid": [int(p.fluid_size[0]), int(p.fluid_size[1])],
+               "particles": n, "waves": int(p.wave_count), "amplitude_over_R": 0.3, "reynolds": 10,
+               "dt": float(p.delta_time), "grid": grid}
+        cells = grid[0] * grid[1]  # planar: one z layer
+    else:
+        cfg = {"workload": "poiseuille2d", "fluid": [64, 64], "particles": n, "wall_rows": 3,
+               "physics": "cubic spline h = 1.3 dx, Tait gamma 7, c0 = 10 u_max, nu = 1e-6",
+               "dt": float(p.delta_time), "grid": grid}
+        cells = grid[0] * grid[1]
+    cfg["parallelism"] = "replicas1"
+    cfg["l2"] = working_set_note(n, cells)
+    return cfg
+
+
+def batched_config(P, N, F, D, scenes_total=256):
+    table = sum(int(p.grid_size[0]) * int(p.grid_size[1]) for p in P)
+    n = int(sum(N))
+    return {"workload": "batched256", "scenes": scenes_total, "scenes_this_rank": len(P),
+            "families": {"poiseuille": sum(d[0] == "poiseuille" for d in D),
+                         "dambreak": sum(d[0] == "dambreak" for d in D)},
+            "fluid_counts": "log-uniform [4096, 262144] (seed 1973)",
+            "nu": "log-uniform [1e-6, 1e-4]; Poiseuille body force scaled with nu, dam-break "
+                  "artificial viscosity 0.38 sqrt(nu / 1e-5)",
+            "particles": n, "fluid": int(sum(F)), "table_cells": table, "steps_per_graph": 10,
+            "kernel": "wendland-2d", "parallelism": "replicas1", "l2": working_set_note(n, table)}
+
+
 def make_workload(name):
     import cmag_gb300 as cm
     from cmag_gb300 import presets
@@ -179,26 +230,20 @@ def make_workload(name):
         p, n, tank, L = presets.dambreak3d()
         s = cm.DamBreakSystem(params=p, num_particles=n)
         s.scene3d(tank, L, 0.01, 1973)
-        cfg = {"workload": "dambreak3d", "fluid": [64, 128, 64], "tank_cells": list(tank),
-               "wall_layers": L, "particles": n, "h_over_dx": 1.3, "kernel": "wendland-3d",
-               "alpha": 0.01, "dt": float(p.delta_time), "grid": list(p.grid_size)}
-        fluid = 64 * 128 * 64
+        fluid = int(np.prod(p.fluid_size))
     elif name == "peristalsis":
         p = presets.peristalsis_c3()
         s = cm.PeristalsisSystem(params=p)
         s.reset()
         n = s.getNumParticles()
-        fluid = p.fluid_size[0] * p.fluid_size[1]
-        cfg = {"workload": "peristalsis2d", "fluid": [int(p.fluid_size[0]), int(p.fluid_size[1])],
-               "particles": n, "waves": 4, "grid": list(p.grid_size)}
+        fluid = int(p.fluid_size[0]) * int(p.fluid_size[1])
     else:
-        p = presets.poiseuille_c1()
+        p = presets.poiseuille_c1(reference_physics=False)
         s = cm.PoiseuilleFlowSystem(params=p)
         s.reset()
         n = s.getNumParticles()
         fluid = 64 * 64
-        cfg = {"workload": "poiseuille2d", "fluid": [64, 64], "particles": n, "grid": list(p.grid_size)}
-    return s, p, n, fluid, cfg
+    return s, p, n, fluid, workload_config(name, p, n)
 
 
 class BatchedRun:
@@ -260,34 +305,18 @@ class BatchedRun:
 def make_batched(rank, world):
     run = BatchedRun(rank, world)
     groups = run.b.groups()
-    cfg = {"workload": "batched256", "scenes": 256, "scenes_this_rank": len(run.P),
-           "families": {"poiseuille": sum(d[0] == "poiseuille" for d in run.D),
-                        "dambreak": sum(d[0] == "dambreak" for d in run.D)},
-           "fluid_counts": "log-uniform [4096, 262144] (seed 1973)",
-           "nu": "log-uniform [1e-6, 1e-4] (Poiseuille; body force scaled with nu)",
-           "particles": run.n, "fluid": int(sum(run.F)), "table_cells": run.table_cells,
-           "launch_groups": len(groups), "steps_per_graph": 10, "kernel": "wendland-2d"}
+    cfg = batched_config(run.P, run.N, run.F, run.D)
+    cfg["launch_groups"] = len(groups)
     meta = {"force_b": 68, "integrate_b": 112,
             "launches": 1 + 3 + 2 + 2 * len(groups) + 1}
     return run, run.n, int(sum(run.F)), cfg, meta
 
 
-def oracle_state_for(name, p, n):
-    from oracle import oracle as O
-    from cmag_gb300 import presets
-    st = O.OracleState(p, n)
-    if name == "dambreak3d":
-        _, _, tank, L = presets.dambreak3d()
-        st.pos[:] = O.dambreak3d_scene(p, tank, L, 0.01, 1973)
-        st.meas[:, 0] = p.rest_density
-    else:
-        st.reset_reference()
-    return st
-
-
-def cpu_run(name, p, n, fluid, steps, threads):
-    """Oracle port on `threads` host threads: seconds for `steps` full steps."""
-    st = oracle_state_for(name, p, n)
+def cpu_run(name, steps, threads):
+    """Oracle port on `threads` host threads: particle-updates/s and seconds for
+    `steps` full steps of the workload (derived on the oracle alone)."""
+    from oracle import workloads as W
+    _, n, fluid, st = W.workload(name)
     st.step(threads=threads)  # warm (page-in, allocation)
     t0 = time.perf_counter()
     for _ in range(steps):
@@ -318,73 +347,64 @@ def barrier_sum(dist, value):
 
 
 def run_reference(args):
+    """The reference's CPU arm: the oracle's restatement of the reference kernels
+    (the reference itself has no CPU implementation of the step) on all host
+    cores, on a bounded sample of the workload.  Only the oracle is loaded: the
+    workload's parameters and scene come from oracle/workloads.py."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    import cmag_gb300  # noqa: F401  (parameter derivation uses the host part of the ABI)
     from oracle import oracle as O
+    from oracle import workloads as W
     O.build()
-    _, p, n, fluid, cfg = make_workload_cpu(args.workload)
     threads = os.cpu_count() or 1
-    st = oracle_state_for(args.workload, p, n)
-    t0 = time.perf_counter()
-    for _ in range(args.warmup):
-        st.step(threads=threads)
-    per_step = (time.perf_counter() - t0) / max(args.warmup, 1)
-    # bounded sample: at most ~150 s of timed CPU work
-    steps = max(1, min(args.steps, int(150.0 / max(per_step, 1e-6))))
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        st.step(threads=threads)
-    secs = time.perf_counter() - t0
-    value = fluid * steps / secs
+    if args.workload == "batched":
+        P, N, F, D = W.batched_scenes()
+        value, secs, sample = cpu_run_batched(P, N, F, D, threads, budget_s=60.0)
+        steps = 1
+        cfg = batched_config(P, N, F, D)
+    else:
+        p, n, fluid, st = W.workload(args.workload)
+        cfg = workload_config(args.workload, p, n)
+        t0 = time.perf_counter()
+        for _ in range(args.warmup):
+            st.step(threads=threads)
+        per_step = (time.perf_counter() - t0) / max(args.warmup, 1)
+        # bounded sample: at most ~60 s of timed CPU work
+        steps = max(1, min(args.steps, int(60.0 / max(per_step, 1e-6))))
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            st.step(threads=threads)
+        secs = time.perf_counter() - t0
+        value = fluid * steps / secs
+        sample = ("%d full steps of the %d-particle scene (of %d requested), after %d warm-up steps; "
+                  "oracle restatement of the reference kernels in their floating-point order"
+                  % (steps, n, args.steps, args.warmup))
     line = {"metric": METRIC, "value": value, "unit": "particle-updates/s", "n_gpus": args.gpus,
             "steps": steps, "warmup": args.warmup, "ms_per_step": secs * 1e3 / steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic", "config": cfg, "impl": "reference",
+            "data": DATA, "config": cfg, "impl": "reference",
             "cpu_baseline": {"value": value, "unit": "particle-updates/s", "cores": threads,
-                             "kind": "port",
-                             "sample": "%d full steps of the %d-particle scene (of %d requested; "
-                                       "oracle restatement of the reference kernels; the reference "
-                                       "itself is CUDA-only and its host classes need OpenGL)"
-                                       % (steps, n, args.steps)},
+                             "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": "particle-updates/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
 
-def make_workload_cpu(name):
-    """Parameter block and sizes without creating a device solver."""
-    from cmag_gb300 import presets
-    if name == "dambreak3d":
-        p, n, tank, L = presets.dambreak3d()
-        cfg = {"workload": "dambreak3d", "fluid": [64, 128, 64], "tank_cells": list(tank),
-               "wall_layers": L, "particles": n, "h_over_dx": 1.3, "kernel": "wendland-3d",
-               "alpha": 0.01, "dt": float(p.delta_time), "grid": list(p.grid_size)}
-        return None, p, n, 64 * 128 * 64, cfg
-    if name == "peristalsis":
-        p = presets.peristalsis_c3()
-        n = presets.reference_count(p)
-        return None, p, n, int(p.fluid_size[0] * p.fluid_size[1]), {
-            "workload": "peristalsis2d", "particles": n, "grid": list(p.grid_size)}
-    p = presets.poiseuille_c1()
-    n = presets.reference_count(p)
-    return None, p, n, 4096, {"workload": "poiseuille2d", "particles": n, "grid": list(p.grid_size)}
-
-
-def cpu_run_batched(run, threads, budget_s=20.0):
+def cpu_run_batched(P, N, F, D, threads, budget_s=20.0):
     """Oracle port on a bounded sample of the batch: the smallest, median and
     largest scene of each family, one step each after a warm step, repeated
-    while within the time budget.  Returns particle-updates/s and the sample."""
+    while within the time budget.  Returns particle-updates/s, seconds and the
+    sample."""
     from oracle import oracle as O
     picks = []
     for fam in ("poiseuille", "dambreak"):
-        ks = sorted([k for k, d in enumerate(run.D) if d[0] == fam], key=lambda k: run.F[k])
+        ks = sorted([k for k, d in enumerate(D) if d[0] == fam], key=lambda k: F[k])
         if ks:
             picks += sorted({ks[0], ks[len(ks) // 2], ks[-1]})
     states = []
     for k in picks:
-        st = O.OracleState(run.P[k], run.N[k]).reset_reference()
+        st = O.OracleState(P[k], N[k]).reset_reference()
         st.step(threads=threads)
         states.append((k, st))
     fluid = 0
@@ -393,7 +413,7 @@ def cpu_run_batched(run, threads, budget_s=20.0):
     while True:
         for k, st in states:
             st.step(threads=threads)
-            fluid += run.F[k]
+            fluid += F[k]
         rounds += 1
         if time.perf_counter() - t0 > budget_s or rounds >= 5:
             break
@@ -535,28 +555,25 @@ def main():
         s, n, fluid, cfg, meta = make_batched(rank, world)
         p = None
         cfg["parallelism"] = "scenes sharded over %d rank(s)" % world
-        cells = s.table_cells
     else:
         s, p, n, fluid, cfg = make_workload(args.workload)
         cfg["parallelism"] = "replicas%d" % world
-        cells = p.num_grid_cells
         meta = {"force_b": STAGE_BYTES["force"][p.system],
                 "integrate_b": STAGE_BYTES["integrate"][p.system],
                 # hash, 3 scan, 2 sort (with the sorted gather), density, force,
                 # integrate (+ phase and boundary configuration for Peristalsis)
                 "launches": {0: 9, 1: 9, 2: 11}[p.system]}
-    cfg["l2"] = "inputs larger than L2 (working set %.0f MB)" % ((n * (7 * 16 + 4 * 4) + 8 * cells) / 1e6)
 
     # warm-up (graph capture happens on the first step), then pick the lanes per
     # particle of the neighbour loops on this workload
     s.update_n(args.warmup)
-    cfg["lanes_density_force"] = list(s.autotune(3))
+    tuning = {"lanes_density_force_lists": list(s.autotune(3))}
     if args.neighbor_lists != "auto" and not batched:
         # a fixed choice (e.g. for profiles, where ncu's serialised launches skew
         # the autotuner's timings): one lane per particle with or without lists
         s.set_groups(1, 1)
         s.set_neighbor_lists(args.neighbor_lists == "on")
-        cfg["lanes_density_force"] = [1, 1, args.neighbor_lists == "on"]
+        tuning["lanes_density_force_lists"] = [1, 1, args.neighbor_lists == "on"]
     s.update_n(2)
     s.synchronize()
 
@@ -601,11 +618,12 @@ def main():
         try:
             cand, inter = pair_counts(p, s.getArray(cm.POSITION))
             mhz = (clocks or {}).get("sm_mhz") or 2070.0
-            peak_tf = 152 * 128 * 2 * mhz * 1e6 / 1e12
+            sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+            peak_tf = sms * 128 * 2 * mhz * 1e6 / 1e12
             fp32 = {"candidates_per_particle": round(cand, 1), "neighbours_per_particle": round(inter, 1),
                     "peak_tflops": round(peak_tf, 1),
-                    "peak_kind": "nominal: 152 SMs x 128 FP32 lanes x 2 flop x sampled SM clock"}
-            lists = bool(cfg["lanes_density_force"][2])
+                    "peak_kind": "nominal: %d SMs x 128 FP32 lanes x 2 flop x sampled SM clock" % sms}
+            lists = bool(tuning["lanes_density_force_lists"][2])
             fp32["force_path"] = "interaction lists" if lists else "cell walk"
             for k, per_pair in (("density", FLOPS_DENSITY_PAIR), ("force", FLOPS_FORCE_PAIR)):
                 # the list-driven force visits interacting pairs only; the DamBreak
@@ -653,6 +671,7 @@ def main():
         "e2e": {"value": e2e_value, "unit": "particle-updates/s", "h2d_bytes_per_step": io_bytes,
                 "d2h_bytes_per_step": io_bytes, "steps": e2e_steps},
         "gpu_launches": meta["launches"] * args.steps,
+        "tuning": tuning,
         "stage_ms": {k: round(v, 5) for k, v in per_stage.items()},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
@@ -664,9 +683,9 @@ def main():
         from oracle import oracle as O
         O.build()
         if batched:
-            v, dt, sample = cpu_run_batched(s, threads)
+            v, dt, sample = cpu_run_batched(s.P, s.N, s.F, s.D, threads)
         else:
-            v, dt = cpu_run(args.workload, p, n, fluid, args.cpu_steps, threads)
+            v, dt = cpu_run(args.workload, args.cpu_steps, threads)
             sample = "%d full step(s) of the same %d-particle scene" % (args.cpu_steps, n)
         line["cpu_baseline"] = {"value": v, "unit": "particle-updates/s", "cores": threads,
                                 "kind": "port", "seconds": dt, "sample": sample}

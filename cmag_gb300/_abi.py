@@ -8,6 +8,10 @@ CMAG_ERR_NOMEM = 3
 CMAG_ERR_DEVICE = 4
 CMAG_ERR_STATE = 5
 
+# device-side check bits (enum cmag_device_error)
+CMAG_DEVERR_LOOKBACK_TIMEOUT = 1
+CMAG_DEVERR_RANGE = 2
+
 DAMBREAK, POISEUILLE, PERISTALSIS = 0, 1, 2
 KERNEL_WENDLAND, KERNEL_CUBIC_SPLINE = 0, 1
 EOS_REFERENCE, EOS_TAIT = 0, 1

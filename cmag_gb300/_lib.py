@@ -41,6 +41,7 @@ SIGNATURES = {
     "cmag_system_reset": ([c_sys], ctypes.c_int),
     "cmag_dambreak3d_scene": ([c_sys, c_u32p, ctypes.c_uint32, ctypes.c_float, ctypes.c_uint64], ctypes.c_int),
     "cmag_system_update": ([c_sys], ctypes.c_int),
+    "cmag_system_update_dt": ([c_sys, ctypes.c_float], ctypes.c_int),
     "cmag_system_update_n": ([c_sys, ctypes.c_uint32], ctypes.c_int),
     "cmag_system_timed_update": ([c_sys, ctypes.c_uint32, c_f32p], ctypes.c_int),
     "cmag_system_run_stages": ([c_sys, ctypes.c_int32], ctypes.c_int),
@@ -78,6 +79,7 @@ SIGNATURES = {
     "cmag_sort_particles_noalloc": ([c_u32p, c_u32p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_void_p],
                                     ctypes.c_int),
     "cmag_sort_particles_noalloc_error": ([], ctypes.c_char_p),
+    "cmag_testing_set_sort_spin_limit": ([ctypes.c_int32], ctypes.c_int),
     "cmag_system_colors": ([c_sys, c_f32p], ctypes.c_int),
     "cmag_system_render_ppm": ([c_sys, ctypes.c_char_p, c_u32, c_u32], ctypes.c_int),
     # batches

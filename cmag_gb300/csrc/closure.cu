@@ -633,13 +633,14 @@ void dispatch_features(const DevParams &p, const ClosureView &c, const float4 *s
 }
 
 // Each block stages the weight image once (23 KB) and its 4 warps loop over
-// 16-row tiles, so the grid stays at a few blocks per SM (152 SMs) however many
-// rows there are.
+// 16-row tiles, so the grid stays at a few blocks per SM (8 per SM at most)
+// however many rows there are.
 uint32_t mlp_blocks(uint32_t n)
 {
     const uint32_t tiles = (n + 15) / 16;
+    const uint32_t cap = 8u * (uint32_t)device_sm_count();
     uint32_t b = (tiles + 3) / 4;
-    return b < 1 ? 1 : (b > 152 * 8 ? 152 * 8 : b);
+    return b < 1 ? 1 : (b > cap ? cap : b);
 }
 
 }  // namespace

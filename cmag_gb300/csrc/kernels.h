@@ -31,6 +31,19 @@ inline void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t s
 }
 
 
+// Streaming multiprocessors of the current device (grid sizing of grid-stride
+// kernels; 152 on a GB300).
+inline int device_sm_count()
+{
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) {
+        (void)cudaGetLastError();
+        return 152;
+    }
+    return sms;
+}
+
 // ---- onesweep radix sort (sort.cu) ----------------------------------------
 constexpr int kSortThreads = 256;
 constexpr int kSortItems = 16;

@@ -12,8 +12,11 @@
 //   * ranks follow input order inside a warp, warps follow each other inside a
 //     tile and tiles follow tile order, so the sort is stable and equals a stable
 //     sort by key -- bit-identical to the reference's thrust result.
-// Every look-back wait is bounded: after kSpinLimit polls the CTA records
-// CMAG_DEVERR_LOOKBACK_TIMEOUT, treats the missing counts as zero and finishes.
+// Every look-back wait is bounded: after g_spin_limit polls (kSpinLimit unless a
+// test lowered it) the CTA records CMAG_DEVERR_LOOKBACK_TIMEOUT, treats the
+// missing counts as zero and finishes; its scatter then writes only positions
+// below n (underestimated offsets stay in range) and flags any other as
+// CMAG_DEVERR_RANGE.
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -30,6 +33,8 @@ constexpr uint32_t kFlagAgg = 1u << 30;     // tile aggregate published
 constexpr uint32_t kFlagPrefix = 2u << 30;  // inclusive prefix published
 constexpr uint32_t kCountMask = (1u << 30) - 1u;
 constexpr int kSpinLimit = 1 << 22;
+// polls before a look-back wait gives up (cmag_testing_set_sort_spin_limit)
+__device__ int g_spin_limit = kSpinLimit;
 constexpr int kWarps = kSortThreads / 32;
 constexpr uint32_t kInvalidDigit = 256;
 constexpr int kLookback = 16;  // predecessor tiles read per look-back round
@@ -140,6 +145,7 @@ __global__ void __launch_bounds__(kSortThreads)
     // decoupled look-back over the tiles before this one, kLookback tiles per
     // round: the counts add up in the same way, in fewer dependent round trips
     volatile uint32_t *st = status;
+    const int spin_limit = g_spin_limit;
     uint32_t exclusive = 0;
     if (tile == 0) {
         st[d] = kFlagPrefix | run;
@@ -173,7 +179,7 @@ __global__ void __launch_bounds__(kSortThreads)
             if (done) break;
             t -= used;
             if (used == 0) {
-                if (++spins > kSpinLimit) {
+                if (++spins > spin_limit) {
                     set_error(err, CMAG_DEVERR_LOOKBACK_TIMEOUT);
                     break;  // give up: the rest counts as zero
                 }
@@ -224,7 +230,8 @@ void launch_digit_hist(const uint32_t *keys, uint32_t n, int passes, uint32_t *h
 {
     if (n == 0 || passes == 0) return;
     uint32_t blocks = (n + 2047) / 2048;
-    if (blocks > 1216) blocks = 1216;  // 8 waves of 152 SMs
+    const uint32_t cap = 8u * (uint32_t)device_sm_count();  // 8 blocks per SM
+    if (blocks > cap) blocks = cap;
     k_digit_hist<<<blocks, 256, 0, st>>>(keys, n, passes, hist);
 }
 
@@ -250,13 +257,13 @@ void launch_onesweep_pass(const uint32_t *kin, const uint32_t *vin, uint32_t *ko
 // ---------------------------------------------------------------------------
 // Sort without any allocation: fixed scratch in device memory of this library.
 //
-// Some callers cannot call cudaMalloc at the moment they need the sort: code
-// that runs between the begin and end of a CUDA stream capture (allocation
-// calls are not capturable), latency-critical loops where an allocation would
-// stall the device, and hosts whose device memory all comes from their own
-// pool.  For them the sort's workspace lives in one file-scope device array,
-// sized for at most kNoAllocMaxKeys keys and held by every GPU that loads this
-// library until the process exits.
+// Some callers cannot call cudaMalloc at the moment they need the sort:
+// latency-critical loops where an allocation would stall the device, and hosts
+// whose device memory all comes from their own pool (a framework's caching
+// allocator, an embedded runtime with a fixed budget).  For them the sort's
+// workspace lives in one file-scope device array, sized for at most
+// kNoAllocMaxKeys keys and held by every GPU that loads this library until the
+// process exits.
 // ---------------------------------------------------------------------------
 namespace {
 
@@ -270,9 +277,34 @@ constexpr size_t kNoAllocWords = kNoAllocWsWords + 1 + 2 * (size_t)kNoAllocMaxKe
 
 __device__ __align__(256) uint32_t g_noalloc_scratch[kNoAllocWords];
 
-constexpr int kMaxDevices = 64;
+// The array's device address belongs to the CUDA context the module was loaded
+// in (normally the device's primary context).  It is looked up once per context,
+// with that context current, and cached under the context handle, so a host that
+// makes its own context current gets that context's copy.  The driver's
+// cuCtxGetCurrent is reached through the runtime (no link to the driver library).
+typedef int (*CtxGetCurrentFn)(void **ctx);
+CtxGetCurrentFn ctx_get_current()
+{
+    static CtxGetCurrentFn fn = [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            return (CtxGetCurrentFn) nullptr;
+        return reinterpret_cast<CtxGetCurrentFn>(f);
+    }();
+    return fn;
+}
+
+constexpr int kMaxContexts = 64;
+struct ScratchAddr {
+    void *ctx;
+    uint32_t *ptr;
+};
 std::mutex g_noalloc_mu;
-uint32_t *g_noalloc_ptr[kMaxDevices] = {};
+ScratchAddr g_noalloc_addr[kMaxContexts] = {};
+int g_noalloc_used = 0;
 
 thread_local char g_noalloc_msg[256];
 
@@ -283,6 +315,41 @@ int noalloc_fail(int code, const char *msg, cudaError_t e = cudaSuccess)
     else
         std::snprintf(g_noalloc_msg, sizeof(g_noalloc_msg), "%s", msg);
     return code;
+}
+
+// Device address of the scratch array in the current context (set-up on the first
+// call in each context; later calls read the cache).
+int noalloc_scratch(uint32_t **out)
+{
+    void *ctx = nullptr;
+    CtxGetCurrentFn get = ctx_get_current();
+    // no context current yet (the runtime creates the primary one on the lookup
+    // below): nothing to key the cache on this time
+    if (get && get(&ctx) != 0) ctx = nullptr;
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (ctx)
+        for (int k = 0; k < g_noalloc_used; ++k)
+            if (g_noalloc_addr[k].ctx == ctx) {
+                *out = g_noalloc_addr[k].ptr;
+                return CMAG_OK;
+            }
+    void *ptr = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess || !ptr)
+        return noalloc_fail(CMAG_ERR_CUDA, "cudaGetSymbolAddress(scratch)", e);
+    // without a context handle (driver entry point unavailable) nothing is cached
+    if (ctx && g_noalloc_used < kMaxContexts) g_noalloc_addr[g_noalloc_used++] = {ctx, static_cast<uint32_t *>(ptr)};
+    *out = static_cast<uint32_t *>(ptr);
+    return CMAG_OK;
+}
+
+int device_error_fail(uint32_t bits)
+{
+    char msg[160];
+    std::snprintf(msg, sizeof(msg), "sort: device-side check failed (bits 0x%x:%s%s)", bits,
+                  (bits & CMAG_DEVERR_LOOKBACK_TIMEOUT) ? " look-back spin limit reached" : "",
+                  (bits & CMAG_DEVERR_RANGE) ? " scatter index out of range" : "");
+    return noalloc_fail(CMAG_ERR_DEVICE, msg);
 }
 
 }  // namespace
@@ -302,24 +369,8 @@ int cmag_sort_particles_noalloc(uint32_t *d_hash, uint32_t *d_index, uint32_t n,
                             "cmag_sort_particles_noalloc sorts at most 1048576 pairs; use "
                             "cmag_sort_particles for more");
     if (key_bits > 32) return noalloc_fail(CMAG_ERR_INVALID, "key_bits must be at most 32");
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return noalloc_fail(CMAG_ERR_CUDA, "cudaGetDevice", e);
-    if (dev < 0 || dev >= kMaxDevices) return noalloc_fail(CMAG_ERR_INVALID, "device ordinal out of range");
-    uint32_t *base;
-    {
-        // once per device, with that device current: the device address of the
-        // scratch array (the host-side symbol is not a device address)
-        std::lock_guard<std::mutex> lock(g_noalloc_mu);
-        if (!g_noalloc_ptr[dev]) {
-            void *ptr = nullptr;
-            e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-            if (e != cudaSuccess || !ptr)
-                return noalloc_fail(CMAG_ERR_CUDA, "cudaGetSymbolAddress(scratch)", e);
-            g_noalloc_ptr[dev] = static_cast<uint32_t *>(ptr);
-        }
-        base = g_noalloc_ptr[dev];
-    }
+    uint32_t *base = nullptr;
+    if (int rc = noalloc_scratch(&base)) return rc;
     cudaStream_t st = (cudaStream_t)cuda_stream;
     int passes = sort_passes(key_bits);
     if (passes < 1) passes = 1;
@@ -328,7 +379,7 @@ int cmag_sort_particles_noalloc(uint32_t *d_hash, uint32_t *d_index, uint32_t n,
     const size_t clear_words = sort_workspace_words(n, passes);
     uint32_t *err = base + kNoAllocWsWords;
     uint32_t *alt_keys = err + 1, *alt_vals = alt_keys + kNoAllocMaxKeys;
-    e = cudaMemsetAsync(base, 0, clear_words * sizeof(uint32_t), st);
+    cudaError_t e = cudaMemsetAsync(base, 0, clear_words * sizeof(uint32_t), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(err, 0, sizeof(uint32_t), st);
     if (e != cudaSuccess) return noalloc_fail(CMAG_ERR_CUDA, "cudaMemsetAsync", e);
     SortWorkspace sw = sort_workspace_view(base, n);
@@ -338,18 +389,31 @@ int cmag_sort_particles_noalloc(uint32_t *d_hash, uint32_t *d_index, uint32_t n,
         const int src = k & 1, dst = src ^ 1;
         launch_onesweep_pass(kb[src], vb[src], kb[dst], vb[dst], n, k, false, sw, err, st);
     }
+    // a launch that failed leaves its error pending; it is reported but not
+    // cleared (an error left by the caller's earlier work stays the caller's)
+    e = cudaPeekAtLastError();
+    if (e != cudaSuccess) return noalloc_fail(CMAG_ERR_CUDA, "sort launch (or an earlier pending error)", e);
     if (passes & 1) {
         e = cudaMemcpyAsync(d_hash, alt_keys, sizeof(uint32_t) * (size_t)n, cudaMemcpyDeviceToDevice, st);
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(d_index, alt_vals, sizeof(uint32_t) * (size_t)n, cudaMemcpyDeviceToDevice, st);
         if (e != cudaSuccess) return noalloc_fail(CMAG_ERR_CUDA, "cudaMemcpyAsync", e);
     }
+    // wait for the sort and read its device-side check word
     uint32_t bits = 0;
     e = cudaMemcpyAsync(&bits, err, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    if (e == cudaSuccess) e = cudaGetLastError();
     if (e != cudaSuccess) return noalloc_fail(CMAG_ERR_CUDA, "sort", e);
-    if (bits) return noalloc_fail(CMAG_ERR_DEVICE, "sort look-back spin limit reached");
+    if (bits) return device_error_fail(bits);
+    return CMAG_OK;
+}
+
+int cmag_testing_set_sort_spin_limit(int32_t polls)
+{
+    using namespace cmag;
+    const int v = polls < 0 ? kSpinLimit : polls;
+    cudaError_t e = cudaMemcpyToSymbol(g_spin_limit, &v, sizeof(int));
+    if (e != cudaSuccess) return noalloc_fail(CMAG_ERR_CUDA, "cudaMemcpyToSymbol(spin limit)", e);
     return CMAG_OK;
 }
 

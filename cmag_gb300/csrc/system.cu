@@ -884,6 +884,18 @@ int cmag_system_update(cmag_system *s)
     return do_step(s);
 }
 
+int cmag_system_update_dt(cmag_system *s, float dt)
+{
+    if (!s) return fail(nullptr, CMAG_ERR_INVALID, "null handle");
+    if (!(dt > 0.0f) || !std::isfinite(dt)) return fail(s, CMAG_ERR_INVALID, "dt must be positive and finite");
+    if (dt != s->p.delta_time) {
+        // dt travels in the step's parameter block: the captured graph is redone
+        s->p.delta_time = dt;
+        invalidate_graph(s);
+    }
+    return do_step(s);
+}
+
 int cmag_system_update_n(cmag_system *s, uint32_t steps)
 {
     if (!s) return fail(nullptr, CMAG_ERR_INVALID, "null handle");
@@ -1444,7 +1456,11 @@ int cmag_sort_particles(uint32_t *d_hash, uint32_t *d_index, uint32_t n, uint32_
     uint32_t bits = 0;
     CM_CUDA(nullptr, cudaMemcpyAsync(&bits, err, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     CM_CUDA(nullptr, cudaStreamSynchronize(st));
-    if (bits) return fail(nullptr, CMAG_ERR_DEVICE, "sort look-back spin limit reached");
+    if (bits)
+        return fail(nullptr, CMAG_ERR_DEVICE,
+                    std::string("sort: device-side check failed (bits ") + std::to_string(bits) + ":" +
+                        ((bits & CMAG_DEVERR_LOOKBACK_TIMEOUT) ? " look-back spin limit reached" : "") +
+                        ((bits & CMAG_DEVERR_RANGE) ? " scatter index out of range" : "") + ")");
     return CMAG_OK;
 }
 

@@ -196,7 +196,9 @@ def batched_scenes(scenes=256, seed=1973, lo=4096, hi=262144, nu_lo=1e-6, nu_hi=
     = 1.25e-5 m/s; dt = min(1e-4, 0.125 h^2 / nu).
     Dam break (the reference column, DamBreak.Report/XFrontTest.h:17-23): a num x
     2num column (num = sqrt(count / 2)) in a 4num x 2num x 4 grid at radius
-    1/(2 num), gravity -9.8, reference artificial viscosity and walls.  The
+    1/(2 num), gravity -9.8, reference walls, artificial viscosity coefficient
+    0.38 sqrt(nu / 1e-5) from the drawn nu (gravity stays: every column is 1 x 2 m,
+    so scaling g would only rescale time).  The
     reference's particle mass and dt (1e-4) belong to its num = 128 column
     (fluidSystem.cpp:17-77); here the mass scales with the particle area,
     (128 / num)^2, so every column has the reference's rest density, and dt with
@@ -227,6 +229,10 @@ def batched_scenes(scenes=256, seed=1973, lo=4096, hi=262144, nu_lo=1e-6, nu_hi=
             p = dambreak_params((num, 2 * num, 1), 1, (4 * num, 2 * num, 4), 1.0 / (2 * num))
             p.particle_mass = F32(float(p.particle_mass) * (128.0 / num) ** 2)
             p.delta_time = F32(1e-4 * 64 / num)
+            # Monaghan's artificial viscosity is the dam break's only viscosity: its
+            # coefficient follows the drawn nu, log-uniform over [0.12, 1.2] around
+            # the reference's 0.38 (fluid_kernel.cu:229-233) at nu = 1e-5
+            p.av_alpha = F32(0.38 * math.sqrt(nu / 1e-5))
             fluid = 2 * num * num
             desc.append(("dambreak", num, 2 * num, nu))
         out_p.append(p)

@@ -65,8 +65,14 @@ class _System:
         return check(rc, self._h)
 
     # -- reference API --
-    def update(self):
-        self._chk(lib().cmag_system_update(self._h))
+    def update(self, dt=None):
+        """One step (update(), fluidSystem.cpp:257-319); with dt, a step of that
+        length, kept in the parameter block for later steps."""
+        if dt is None:
+            self._chk(lib().cmag_system_update(self._h))
+        else:
+            self._chk(lib().cmag_system_update_dt(self._h, float(dt)))
+            self._p.delta_time = float(dt)
 
     def update_n(self, steps):
         self._chk(lib().cmag_system_update_n(self._h, int(steps)))
@@ -386,8 +392,8 @@ class PeristalsisSystem(_System):
                 ctypes.byref(params)))
         super().__init__(params, num_particles)
 
-    def Update(self):
-        self.update()
+    def Update(self, dt=None):
+        self.update(dt)
 
     def Reset(self):
         self.reset()

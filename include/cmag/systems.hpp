@@ -161,6 +161,8 @@ public:
     enum ParticleArray { POSITION, VELOCITY, MEASURES, ACCELERATION, VELOCITYLEAPFROG };
 
     void update() { cmag::check(cmag_system_update(h_), h_); }
+    // one step of length dt (kept in the parameter block for later update() calls)
+    void update(float dt) { cmag::check(cmag_system_update_dt(h_, dt), h_); }
     void reset() { cmag::check(cmag_system_reset(h_), h_); }
     void setArray(ParticleArray array, const float *data, int start, int count) { setRaw((int)array, data, start, count); }
     float getElapsedTime() const { return elapsed(); }
@@ -185,6 +187,8 @@ public:
     enum ParticleArray { POSITION, VELOCITY, MEASURES, ACCELERATION, VELOCITYLEAPFROG };
 
     void update() { cmag::check(cmag_system_update(h_), h_); }
+    // one step of length dt (kept in the parameter block for later update() calls)
+    void update(float dt) { cmag::check(cmag_system_update_dt(h_, dt), h_); }
     void reset() { cmag::check(cmag_system_reset(h_), h_); }
     void setArray(ParticleArray array, const float *data, int start, int count) { setRaw((int)array, data, start, count); }
     float getElapsedTime() const { return elapsed(); }
@@ -210,6 +214,8 @@ public:
     enum ParticleArray { POSITION, PREDICTEDPOSITION, VELOCITY, MEASURES, VISCOUSFORCE, PRESSUREFORCE, VELOCITYLEAPFROG };
 
     void Update() { cmag::check(cmag_system_update(h_), h_); }
+    // one step of length dt (kept in the parameter block for later Update() calls)
+    void Update(float dt) { cmag::check(cmag_system_update_dt(h_, dt), h_); }
     void Reset() { cmag::check(cmag_system_reset(h_), h_); }
     void setArray(ParticleArray array, const float *data, int start, int count)
     {

@@ -223,6 +223,11 @@ int cmag_dambreak3d_particle_count(const uint32_t fluid_size[3], const uint32_t 
 /* One time step (update/Update: fluidSystem.cpp:257-319,
  * poiseuilleFlowSystem.cpp:212-270, PeristalsisSystem.cpp:320-407). */
 int cmag_system_update(cmag_system *s);
+/* One time step of length dt: sets the parameter block's delta_time to dt (it
+ * stays for later update() calls, as the reference's params.dt does,
+ * fluidSystem.cpp:257,268) and steps.  A dt that differs from the previous one
+ * re-captures the step's CUDA graph on this call. */
+int cmag_system_update_dt(cmag_system *s, float dt);
 /* Run `steps` time steps back to back (replayed as one captured CUDA graph per
  * step when graphs are enabled). */
 int cmag_system_update_n(cmag_system *s, uint32_t steps);
@@ -337,24 +342,35 @@ int cmag_sort_particles(uint32_t *d_hash, uint32_t *d_index, uint32_t n, uint32_
                         void *cuda_stream);
 
 /* The same stable sort without allocating anything, for callers that cannot call
- * cudaMalloc where they sort: inside a CUDA stream capture (allocation is not
- * capturable), in latency-critical loops where an allocation would stall the
- * device, or in hosts whose device memory all comes from their own pool.  No
+ * cudaMalloc where they sort: latency-critical loops where an allocation would
+ * stall the device, and hosts whose device memory all comes from their own pool
+ * (a framework's caching allocator, a runtime with a fixed memory budget).  No
  * counterpart in the reference (its thrust::sort_by_key allocates temporaries).
  *  - Works on at most 1,048,576 pairs; larger n returns CMAG_ERR_INVALID.
  *  - Its workspace (about 9.3 MB: look-back status and alternate key/value
  *    buffers) is a fixed device array inside this library, held by every GPU that
  *    loads the library until the process exits; no cudaMalloc/cudaFree is called.
- *  - The first call on each device looks up that array's device address
- *    (cudaGetSymbolAddress) with the device current; make that first call before
- *    any stream capture.
+ *  - The first call in each CUDA context (normally once per device, in its
+ *    primary context) looks up that array's device address
+ *    (cudaGetSymbolAddress) with the context current and caches it under the
+ *    context; make that first call before any stream capture.
  *  - Every call shares the one array: calls whose work overlaps on the GPU (other
  *    streams, other threads) race and must be serialised by the caller.
- *  - Like cmag_sort_particles it waits for the stream before returning, to report
- *    a failed device-side check; messages: cmag_sort_particles_noalloc_error(). */
+ *  - It waits for the stream before returning, to report a failed device-side
+ *    check (look-back timeout, out-of-range scatter); messages:
+ *    cmag_sort_particles_noalloc_error(). */
 int cmag_sort_particles_noalloc(uint32_t *d_hash, uint32_t *d_index, uint32_t n,
                                 uint32_t key_bits, void *cuda_stream);
 const char *cmag_sort_particles_noalloc_error(void);
+
+/* Testing only (no reference counterpart; the reference's sort has no bounded
+ * waits).  Number of polls after which a look-back wait of the radix sort
+ * (cmag_sort_particles, cmag_sort_particles_noalloc) gives up on the current
+ * device and records CMAG_DEVERR_LOOKBACK_TIMEOUT; negative restores the default
+ * (4,194,304).  0 makes every wait that finds its predecessor tile unpublished
+ * give up at once, so tests can reach the failure path without a real stall: the
+ * sort then returns CMAG_ERR_DEVICE and its output is wrong but stays in bounds. */
+int cmag_testing_set_sort_spin_limit(int32_t polls);
 
 /* ---- headless colours and point view ----------------------------------- */
 /* The Demo programs' colour buffers without OpenGL: per particle (original

@@ -15,8 +15,7 @@ import subprocess
 
 import numpy as np
 
-from cmag_gb300._abi import (DAMBREAK, PERISTALSIS, POISEUILLE, SphParams, STAGE_INTEGRATE, f3,
-                             u3)
+from .params import DAMBREAK, PERISTALSIS, POISEUILLE, STAGE_INTEGRATE, SphParams, f3, u3
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
@@ -39,12 +38,22 @@ def build(quiet=True):
         print(out.stdout)
 
 
-def build_ref(ref_root="/root/reference"):
+def _ref_make_args(ref_root):
+    # the tree: the argument, else what oracle/ref/Makefile resolves (REF=,
+    # CMAG_REFERENCE)
+    return ["make", "-s", "-C", os.path.join(HERE, "ref")] + (["REF=" + ref_root] if ref_root else [])
+
+
+def have_ref(ref_root=None):
+    """Whether the reference tree the recipe reads is present on this host."""
+    return subprocess.run(_ref_make_args(ref_root) + ["have-ref"], capture_output=True).returncode == 0
+
+
+def build_ref(ref_root=None):
     """Compile oracle/_ref from the reference sources, where the tree exists."""
-    if not os.path.isdir(ref_root):
+    if not have_ref(ref_root):
         return False
-    out = subprocess.run(["make", "-C", os.path.join(HERE, "ref"), "REF=" + ref_root],
-                         capture_output=True, text=True)
+    out = subprocess.run(_ref_make_args(ref_root), capture_output=True, text=True)
     if out.returncode != 0:
         raise RuntimeError("oracle/_ref build failed:\n" + out.stdout + out.stderr)
     return True
@@ -56,7 +65,9 @@ def lib():
         if not os.path.exists(LIB_PATH):
             build()
         L = ctypes.CDLL(LIB_PATH)
-        sp = P(SphParams)
+        # parameter blocks by address: the oracle's SphParams or the product's
+        # mirror of the same struct
+        sp = ctypes.c_void_p
         L.orc_dambreak_params.argtypes = [c_u32p, ctypes.c_int32, c_u32p, ctypes.c_float, sp]
         L.orc_poiseuille_params.argtypes = [c_u32p, ctypes.c_int32, c_u32p, ctypes.c_float, sp]
         L.orc_peristalsis_params.argtypes = [ctypes.c_float, c_u32p, ctypes.c_float, ctypes.c_float,

@@ -61,9 +61,10 @@ def configured_walls(pre):
             and pre.phase[3] < np.float32(p.amplitude))
 
 
-def compare_step(gpu, pre, post, label=""):
+def compare_step(gpu, pre, post, label="", threads=1):
     """gpu: dict of the GPU arrays after one step from `pre`; post: the oracle's
-    state after the same step.  Returns the measured error ratios."""
+    state after the same step (threads: host threads of the oracle's force
+    recomputation).  Returns the measured error ratios."""
     from oracle import oracle as O
     p = post.p
     out = {}
@@ -88,7 +89,7 @@ def compare_step(gpu, pre, post, label=""):
     out["p"] = float(dp / bound)
     assert dp <= bound, "%spressure error %g > %g" % (label, dp, bound)
 
-    a, b, sa, sb = post.forces_on(gpu["meas"], spos=gpu["spos"])
+    a, b, sa, sb = post.forces_on(gpu["meas"], spos=gpu["spos"], threads=threads)
     if p.system == _abi.PERISTALSIS:
         pairs = (("vforce", a, sa), ("pforce", b, sb))
     else:

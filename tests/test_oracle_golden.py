@@ -65,3 +65,43 @@ def test_reference_kernels_match_oracle_stepwise(built):
             for k, sc in (("acc", sa), ("vforce", sa), ("pforce", sb)):
                 err = np.abs(getattr(a, k)[:, :3].astype(np.float64) - getattr(b, k)[:, :3])
                 assert (err <= FORCE_TOL * sc[:, :3] + 1e-30).all(), k
+
+
+def test_oracle_parameter_mirror_matches_the_product(built):
+    """The oracle keeps its own ctypes mirror of cmag_sph_params (so its users never
+    import the product); field names, types and offsets equal the product's."""
+    from cmag_gb300 import _abi
+    from oracle import params as OP
+    a, b = _abi.SphParams, OP.SphParams
+    assert [(f, str(t)) for f, t in a._fields_] == [(f, str(t)) for f, t in b._fields_]
+    assert [getattr(a, f).offset for f, _ in a._fields_] == [getattr(b, f).offset for f, _ in b._fields_]
+    import ctypes
+    assert ctypes.sizeof(a) == ctypes.sizeof(b)
+
+
+@pytest.mark.parametrize("name", ["dambreak3d", "peristalsis", "poiseuille", "poiseuille_ref"])
+def test_oracle_workloads_equal_the_presets(built, name):
+    """bench.py's CPU arms derive the workloads on the oracle alone: same bytes as
+    the product's presets (which derive them through the library)."""
+    from cmag_gb300 import presets
+    from oracle import workloads as W
+    if name == "dambreak3d":
+        a, na, _, _ = presets.dambreak3d()
+        b, nb, _, _ = W.dambreak3d()
+        assert na == nb == 954_860
+    elif name == "peristalsis":
+        a, b = presets.peristalsis_c3(), W.peristalsis_c3()
+    else:
+        ref = name == "poiseuille_ref"
+        a, b = presets.poiseuille_c1(reference_physics=ref), W.poiseuille_c1(reference_physics=ref)
+    assert bytes(a) == bytes(b)
+
+
+def test_oracle_batched_scenes_equal_the_presets(built):
+    from cmag_gb300 import presets
+    from oracle import workloads as W
+    a, b = presets.batched_scenes(), W.batched_scenes()
+    assert a[1] == b[1] and a[2] == b[2] and a[3] == b[3]
+    assert all(bytes(x) == bytes(y) for x, y in zip(a[0], b[0]))
+    alphas = [float(p.av_alpha) for p, d in zip(a[0], a[3]) if d[0] == "dambreak"]
+    assert 0.11 < min(alphas) < max(alphas) < 1.21
