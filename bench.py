@@ -325,6 +325,109 @@ def cpu_run(name, steps, threads):
     return fluid * steps / dt, dt
 
 
+def front_of(s, column_width):
+    """Surge front: the largest fluid x over the column width (XFrontTest.h:64-86),
+    from a device reduction."""
+    lo, hi = s.fluid_extent()
+    return float(hi[0]) / column_width
+
+
+def run_to_t1(s, p, kept, t_end=1.0, sample_dt=0.01, column_width=0.5):
+    """The 3-D dam break from its initial state to t_end: device seconds of the
+    steps (CUDA events around chunks of sample_dt), steps, list rebuilds and the
+    surge front at every sample (read between the timed chunks)."""
+    s.scene3d(DAMBREAK3D_TANK, DAMBREAK3D_LAYERS, 0.01, 1973)
+    if kept:
+        s.set_verlet(kept)
+    dt = float(p.delta_time)
+    per = int(round(sample_dt / dt))
+    total = int(round(t_end / dt))
+    s.update_n(1)  # graph capture, outside the timing
+    s.synchronize()
+    r0 = s.verlet()[1] if kept else 0
+    done, ms = 1, 0.0
+    times, fronts = [dt], [front_of(s, column_width)]
+    while done < total:
+        k = min(per, total - done)
+        ms += s.timed_update(k)
+        done += k
+        times.append(done * dt)
+        fronts.append(front_of(s, column_width))
+    s.synchronize()
+    return {"device_s": ms / 1e3, "steps": total, "rebuilds": (s.verlet()[1] - r0) if kept else None,
+            "ms_per_step": ms / (total - 1), "t_end": t_end, "times": times, "fronts": fronts}
+
+
+def reference_gpu_bar(steps=20, warmup=5):
+    """The reference's own DamBreak kernels on this GPU (DamBreak.Core/fluid_kernel.cu
+    built for sm_103a into oracle/_ref, driven in the order of DamBreakSystem::update
+    with thrust::sort_by_key), timed beside the library:
+      * the reference's 2-D dam break at the 3-D workload's fluid count (a 512 x 1024
+        column in a 2048 x 1024 x 4 grid, reference physics in both): the same
+        arithmetic, so the ratio is a like-for-like speed-up;
+      * the 3-D workload's 954,860 particles on a power-of-two 512 x 256 x 128 grid
+        (the reference masks its hash): the reference kernels' own 3-D loops (7^3
+        cells per particle, its 2-D kernel normalisation, alpha 0.38 and uncut wall
+        force: the arithmetic of its 2-D physics on 3-D data), for the cost of the
+        reference's search at this size.
+    Device time per step from CUDA events; stage times from events around stages."""
+    import cmag_gb300 as cm
+    from cmag_gb300 import presets
+    from oracle import ref_gpu as RG
+    if not RG.available():
+        return {"unavailable": "the reference's kernels were not built on this host (the cubin is compiled from "
+                               "the reference sources, which only the build host has)"}
+    out = {}
+    names = ["hash", "sort", "reorder", "density", "force", "integrate"]
+    # (a) like for like: the reference's 2-D dam break, 524,288 fluid particles
+    kw = presets.dambreak_xfront(512)
+    p = presets.dambreak_params(kw["fluid_size"], kw["boundary_offset"], kw["grid_size"], kw["radius"])
+    s = cm.DamBreakSystem(params=p)
+    s.reset()
+    s.removeRightBoundary()
+    ref = RG.RefGpu(s.params, s.getArray(cm.POSITION))
+    ref.steps(warmup)
+    ref_ms = ref.timed_steps(steps)
+    ref_stage = ref.stage_ms(steps)
+    ref.close()
+    s.update_n(warmup)
+    own_ms = s.timed_update(steps)
+    s.set_stage_timing(True)
+    s.update_n(steps)
+    own_stage, tsteps = s.stage_times()
+    s.set_stage_timing(False)
+    n, fluid = s.getNumParticles(), 512 * 1024
+    s.close()
+    out["dambreak2d_512x1024_reference_physics"] = {
+        "particles": n, "fluid": fluid, "grid": list(kw["grid_size"]), "steps": steps,
+        "reference_ms_per_step": ref_ms / steps, "own_ms_per_step": own_ms / steps,
+        "reference_updates_per_s": fluid * steps / (ref_ms / 1e3),
+        "own_updates_per_s": fluid * steps / (own_ms / 1e3),
+        "speedup": ref_ms / own_ms,
+        "reference_stage_ms": {k: round(v / steps, 5) for k, v in zip(names, ref_stage)},
+        "own_stage_ms": {k: round(v / max(tsteps, 1), 5) for k, v in zip(names, own_stage)}}
+    # (b) the 3-D workload's particles through the reference's own loops
+    p3, n3, tank, L = presets.dambreak3d()
+    pr = p3.copy()
+    pr.grid_size[0], pr.grid_size[1], pr.grid_size[2] = 512, 256, 128
+    pos = np.zeros((n3, 4), np.float32)
+    s3 = cm.DamBreakSystem(params=p3, num_particles=n3)
+    s3.scene3d(tank, L, 0.01, 1973)
+    pos[:] = s3.getArray(cm.POSITION)
+    s3.close()
+    ref = RG.RefGpu(pr, pos)
+    ref.steps(2)
+    k3 = max(2, steps // 4)
+    ms3 = ref.timed_steps(k3)
+    st3 = ref.stage_ms(k3)
+    ref.close()
+    out["dambreak3d_954860_reference_loops"] = {
+        "particles": n3, "fluid": 524288, "grid": [512, 256, 128], "steps": k3,
+        "reference_ms_per_step": ms3 / k3, "reference_updates_per_s": 524288 * k3 / (ms3 / 1e3),
+        "reference_stage_ms": {k: round(v / k3, 5) for k, v in zip(names, st3)}}
+    return out
+
+
 def dist_init(n_gpus):
     if n_gpus <= 1 and "RANK" not in os.environ:
         return None
@@ -530,6 +633,13 @@ def main():
     ap.add_argument("--neighbor-lists", choices=["auto", "on", "off"], default="auto",
                     help="single-scene workloads: the autotuner's choice, or force interaction lists on/off")
     ap.add_argument("--cpu-steps", type=int, default=1)
+    ap.add_argument("--verlet", type=float, default=0.4,
+                    help="single scenes: neighbour lists kept over steps with this skin (particle spacings); "
+                         "0: the reference's per-step sort and cell walk")
+    ap.add_argument("--t-start", type=float, default=0.2,
+                    help="dam break: simulated seconds run (untimed, part of the setup) before warm-up")
+    ap.add_argument("--no-t1", action="store_true", help="skip the plain run to t = 1 s")
+    ap.add_argument("--no-ref-gpu", action="store_true", help="skip timing the reference's kernels on the GPU")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -564,10 +674,20 @@ def main():
                 # integrate (+ phase and boundary configuration for Peristalsis)
                 "launches": {0: 9, 1: 9, 2: 11}[p.system]}
 
+    kept = (not batched) and args.verlet > 0 and args.neighbor_lists == "auto"
+    if not batched and args.workload == "dambreak3d" and args.t_start > 0:
+        # the timed steps start from a developed flow (the surge under way), not
+        # from the column at rest
+        s.update_n(int(round(args.t_start / float(p.delta_time))))
+        cfg["t_start"] = args.t_start
+    if kept:
+        s.set_verlet(args.verlet)
     # warm-up (graph capture happens on the first step), then pick the lanes per
     # particle of the neighbour loops on this workload
     s.update_n(args.warmup)
     tuning = {"lanes_density_force_lists": list(s.autotune(3))}
+    if kept:
+        tuning = {"kept_lists_skin": args.verlet}
     if args.neighbor_lists != "auto" and not batched:
         # a fixed choice (e.g. for profiles, where ncu's serialised launches skew
         # the autotuner's timings): one lane per particle with or without lists
@@ -576,6 +696,7 @@ def main():
         tuning["lanes_density_force_lists"] = [1, 1, args.neighbor_lists == "on"]
     s.update_n(2)
     s.synchronize()
+    rebuilds0 = s.verlet()[1] if kept else 0
 
     # ---- device-resident timed region ----
     if dist:
@@ -592,6 +713,8 @@ def main():
     total_fluid = fluid if not dist else int(barrier_sum(dist, fluid))
     value = total_fluid * args.steps / secs if batched else fluid * args.steps * world / secs
     s.synchronize()
+    if kept:
+        tuning["rebuilds_in_timed_steps"] = s.verlet()[1] - rebuilds0
 
     # ---- per-stage times (plain launches, events around each stage) ----
     s.set_stage_timing(True)
@@ -689,6 +812,16 @@ def main():
             sample = "%d full step(s) of the same %d-particle scene" % (args.cpu_steps, n)
         line["cpu_baseline"] = {"value": v, "unit": "particle-updates/s", "cores": threads,
                                 "kind": "port", "seconds": dt, "sample": sample}
+    if not batched and args.workload == "dambreak3d" and rank == 0 and world == 1 and not args.no_ref_gpu:
+        line["reference_gpu"] = reference_gpu_bar()
+        bar = line["reference_gpu"].get("dambreak3d_954860_reference_loops")
+        if bar:
+            line["reference_gpu"]["own_vs_reference_loops"] = value / bar["reference_updates_per_s"]
+    if not batched and args.workload == "dambreak3d" and not args.no_t1:
+        t1 = run_to_t1(s, p, args.verlet if kept else 0.0)
+        line["to_t1"] = {"plain_fine": {k: (round(v, 5) if isinstance(v, float) else v) for k, v in t1.items()
+                                        if k not in ("times", "fronts")},
+                         "fronts_every_0.05s": [round(f, 4) for f in t1["fronts"][::5]]}
     s.close()
     if rank == 0:
         print(json.dumps(line))

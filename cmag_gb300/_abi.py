@@ -110,6 +110,17 @@ class SphParams(ctypes.Structure):
         return int(g[0]) * int(g[1]) * int(g[2])
 
 
+def as_params(p):
+    """p as a SphParams: p itself, or a copy of any object with the struct's bytes
+    (another ctypes mirror of cmag_sph_params)."""
+    if isinstance(p, SphParams):
+        return p
+    b = bytes(p)
+    if len(b) != ctypes.sizeof(SphParams):
+        raise TypeError("not a cmag_sph_params block (%d bytes)" % len(b))
+    return SphParams.from_buffer_copy(b)
+
+
 def u3(v):
     return u32x3(*[int(x) for x in v])
 

@@ -73,6 +73,8 @@ SIGNATURES = {
     "cmag_system_autotune": ([c_sys, ctypes.c_int32], ctypes.c_int),
     "cmag_system_set_neighbor_lists": ([c_sys, ctypes.c_int32], ctypes.c_int),
     "cmag_system_get_neighbor_lists": ([c_sys, P(ctypes.c_int32), c_u32p], ctypes.c_int),
+    "cmag_system_set_verlet": ([c_sys, ctypes.c_float], ctypes.c_int),
+    "cmag_system_get_verlet": ([c_sys, c_f32p, c_u32p], ctypes.c_int),
     "cmag_system_set_stage_timing": ([c_sys, ctypes.c_int32], ctypes.c_int),
     "cmag_system_stage_times": ([c_sys, c_f32p, c_u32p], ctypes.c_int),
     "cmag_sort_particles": ([c_u32p, c_u32p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_void_p], ctypes.c_int),

@@ -24,7 +24,7 @@ class Batch:
         counts = [int(c) for c in counts]
         if len(params) != len(counts):
             raise ValueError("one particle count per scene")
-        arr = (SphParams * len(params))(*[p.copy() for p in params])
+        arr = (SphParams * len(params))(*[_abi.as_params(p).copy() for p in params])
         cnt = (ctypes.c_uint32 * len(counts))(*counts)
         self._h = ctypes.c_void_p()
         check(lib().cmag_batch_create(arr, cnt, len(params), ctypes.byref(self._h)))
@@ -126,7 +126,7 @@ class Batch:
         return p
 
     def set_params(self, scene, p):
-        self._chk(lib().cmag_batch_set_params(self._h, int(scene), ctypes.byref(p)))
+        self._chk(lib().cmag_batch_set_params(self._h, int(scene), ctypes.byref(_abi.as_params(p))))
 
     def elapsed_time(self, scene):
         t = ctypes.c_float()

@@ -11,7 +11,7 @@ SRC = os.path.join(PKG, "csrc")
 OUT_DIR = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libcmag_sph.so")
 
-SOURCES = ["sort.cu", "cells.cu", "density.cu", "force.cu", "integrate.cu", "reduce.cu", "system.cu", "batch.cu", "closure.cu", "closure_api.cu", "render.cu",
+SOURCES = ["sort.cu", "cells.cu", "density.cu", "force.cu", "integrate.cu", "reduce.cu", "system.cu", "batch.cu", "closure.cu", "closure_api.cu", "render.cu", "verlet.cu",
            "host_scenes.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # host code: no fused multiply-add, so host float arithmetic (parameters, scenes,

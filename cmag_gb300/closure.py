@@ -202,6 +202,31 @@ class Pair:
         target_dev[row0:row0 + k] = (interp[:, :3] - a_coarse)[keep]
         return k
 
+    def missed(self, min_shepard=0.5):
+        """The coarse run's missed acceleration at the current pair of states: the
+        fine acceleration field at each coarse fluid particle minus the coarse
+        run's own (device (n, 3)), and whether the fine fluid reaches the particle
+        (device bool (n,))."""
+        import torch
+        self.coarse.set_closure(None)
+        self.fine.run_stages(_abi.STAGE_FORCE)
+        self.coarse.run_stages(_abi.STAGE_FORCE)
+        n = self.nfluid_c
+        a_coarse = torch.from_numpy(self.coarse.getArray(_abi.ACCELERATION)[:n, :3].copy()).cuda()
+        pts = torch.from_numpy(self.coarse.getArray(_abi.POSITION)[:n].copy()).cuda()
+        interp = torch.empty((n, 4), dtype=torch.float32, device="cuda")
+        self.fine.interpolate(_abi.ACCELERATION, pts.data_ptr(), n, interp.data_ptr())
+        return interp[:, :3] - a_coarse, interp[:, 3] >= min_shepard
+
+    def features(self):
+        """The coarse run's closure features at its current state (device (n, 16))."""
+        import torch
+        self.coarse.set_closure(None)
+        self.coarse.run_stages(_abi.STAGE_FORCE)
+        full = torch.empty((self.nc, NFEAT), dtype=torch.float32, device="cuda")
+        self.coarse.closure_features(full.data_ptr())
+        return full[:self.nfluid_c]
+
     def close(self):
         self.fine.close()
         self.coarse.close()
@@ -298,6 +323,45 @@ def collect(pair, seeds, snapshots, every, min_shepard=0.5):
             pair.fine.update_n(every)
             pair.coarse.update_n(every // 2)
             row += pair.sample(feat_dev, target_dev, row, min_shepard)
+    return feat_dev[:row].contiguous(), target_dev[:row].contiguous()
+
+
+def collect_filtered(pair, seeds, snapshots, every, window, min_shepard=0.5):
+    """Training rows with time-filtered targets: along the lockstep fine/coarse
+    runs of each seed (no restarts), the target of a coarse fluid particle is its
+    missed acceleration averaged over the `window` coarse steps that end at the
+    sample (the acoustic part, which the two resolutions do not share, averages
+    out; what the coarse method misses systematically stays), and its features
+    are those at the sample.  `every` fine steps between samples (even, at least
+    2 window).  Returns device (features, targets)."""
+    import torch
+    if every % 2 or every < 2 * window:
+        raise ValueError("`every` must be even and at least 2 * window")
+    n = pair.nfluid_c
+    rows = len(seeds) * snapshots * n
+    feat_dev = torch.empty((rows, NFEAT), dtype=torch.float32, device="cuda")
+    target_dev = torch.empty((rows, NOUT), dtype=torch.float32, device="cuda")
+    row = 0
+    for seed in seeds:
+        pair.start(seed)
+        for _ in range(snapshots):
+            lead = every - 2 * window
+            pair.fine.update_n(lead)
+            pair.coarse.update_n(lead // 2)
+            acc = torch.zeros((n, NOUT), dtype=torch.float32, device="cuda")
+            cnt = torch.zeros(n, dtype=torch.float32, device="cuda")
+            for _w in range(window):
+                pair.fine.update_n(2)
+                pair.coarse.update_n(1)
+                t, keep = pair.missed(min_shepard)
+                kf = keep.float()
+                acc += t * kf[:, None]
+                cnt += kf
+            keep = cnt >= 0.5 * window
+            k = int(keep.sum())
+            feat_dev[row:row + k] = pair.features()[keep]
+            target_dev[row:row + k] = (acc / cnt.clamp_min(1.0)[:, None])[keep]
+            row += k
     return feat_dev[:row].contiguous(), target_dev[:row].contiguous()
 
 

@@ -40,13 +40,15 @@ constexpr uint32_t kScanTile = kScanThreads * kScanItems;
 template <bool BATCH>
 __global__ void __launch_bounds__(256)
     k_hash(DevParams pv, BatchView bv, const float4 *__restrict__ pos, uint32_t *__restrict__ hash,
-           uint32_t *__restrict__ cnt, uint32_t *__restrict__ rank, uint32_t *err)
+           uint32_t *__restrict__ cnt, uint32_t *__restrict__ rank, uint32_t *err,
+           float4 *__restrict__ snap)
 {
     pdl_entry();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= (BATCH ? bv.n_total : pv.n)) return;
     const DevParams &p = BATCH ? bv.scenes[bv.scene_of[i]] : pv;
     const float4 q = pos[i];
+    if (snap) snap[i] = q;  // positions the kept lists are built from
     const int3 g = grid_pos(p, q.x, q.y, q.z);
     const uint32_t hr = grid_hash(p, g.x, g.y, g.z);
     uint32_t rel = hr - p.scan_base;  // wraps for hr < scan_base
@@ -269,13 +271,13 @@ __global__ void k_cell_view(const uint32_t *__restrict__ off, uint32_t scan_base
 }  // namespace
 
 void launch_hash(const DevParams &p, const BatchView &bv, const float4 *pos, uint32_t *hash,
-                 uint32_t *cnt, uint32_t *rank, uint32_t *err, cudaStream_t st)
+                 uint32_t *cnt, uint32_t *rank, uint32_t *err, cudaStream_t st, float4 *snap)
 {
     const uint32_t n = bv.scenes ? bv.n_total : p.n;
     if (n == 0) return;
     const uint32_t blocks = (n + 255) / 256;
-    if (bv.scenes) launch_pdl(k_hash<true>, blocks, 256, 0, st, p, bv, pos, hash, cnt, rank, err);
-    else launch_pdl(k_hash<false>, blocks, 256, 0, st, p, bv, pos, hash, cnt, rank, err);
+    if (bv.scenes) launch_pdl(k_hash<true>, blocks, 256, 0, st, p, bv, pos, hash, cnt, rank, err, snap);
+    else launch_pdl(k_hash<false>, blocks, 256, 0, st, p, bv, pos, hash, cnt, rank, err, snap);
 }
 
 void launch_cell_sort(const uint32_t *hash, const uint32_t *rank, const uint32_t *off,

@@ -28,8 +28,8 @@ using walk::for_each_candidate;
 using walk::for_each_run;
 using walk::frac_cell;
 using walk::group_sum;
-using walk::interacts;
 using walk::list_append;
+using walk::records;
 using walk::rel;
 using walk::shift_code;
 
@@ -74,8 +74,8 @@ __device__ __forceinline__ void wendland_run(const DevParams &p, const float4 *_
         acc = __fadd2_rn(acc, w);
         if (LIST && record) {
             const uint32_t v = j | code;  // j + 1 < 2^26: the next entry is v + 1
-            if (interacts<SYS, TRIM>(p, d2.x, a.w)) list_append(nl, i, cnt, v);
-            if (interacts<SYS, TRIM>(p, d2.y, c.w)) list_append(nl, i, cnt, v + 1u);
+            if (records<SYS, TRIM>(p, i, j, d2.x, a.w)) list_append(nl, i, cnt, v);
+            if (records<SYS, TRIM>(p, i, j + 1, d2.y, c.w)) list_append(nl, i, cnt, v + 1u);
         }
     }
     if (j < e) {  // the same operations as one half of a pair step
@@ -87,7 +87,7 @@ __device__ __forceinline__ void wendland_run(const DevParams &p, const float4 *_
         const float t = fmaxf(__fmaf_rn(d, -0.5f * p.inv_h, 1.0f), 0.0f), t2 = __fmul_rn(t, t);
         const float w = __fmul_rn(__fmul_rn(t2, t2), __fmaf_rn(d, 2.0f * p.inv_h, 1.0f));
         acc.x = __fadd_rn(acc.x, w);
-        if (LIST && record && interacts<SYS, TRIM>(p, d2, pj.w)) list_append(nl, i, cnt, j | code);
+        if (LIST && record && records<SYS, TRIM>(p, i, j, d2, pj.w)) list_append(nl, i, cnt, j | code);
     }
 }
 
@@ -112,8 +112,9 @@ __global__ void __launch_bounds__(256, (PLANAR || (!BATCH && SYS == CMAG_DAMBREA
     const float4 pi = active ? spos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     // Poiseuille walls keep rest density (poiseuilleFlowKernel.cu:154-158)
     const bool pinned = SYS == CMAG_POISEUILLE && pi.w == 1.0f;
-    // lists for every particle whose force is computed (DamBreak: fluid only)
-    const bool record = LIST && active && (SYS != CMAG_DAMBREAK || pi.w == (float)CMAG_FLUID);
+    // lists for every particle whose force is computed (DamBreak: fluid only);
+    // lists kept over several steps serve the density too: every particle
+    const bool record = LIST && active && (p.verlet || SYS != CMAG_DAMBREAK || pi.w == (float)CMAG_FLUID);
     uint32_t cnt = 0;
     float sum = 0.0f;
     if (active && (!pinned || record)) {  // a pinned wall walks only to record its list
@@ -136,12 +137,15 @@ __global__ void __launch_bounds__(256, (PLANAR || (!BATCH && SYS == CMAG_DAMBREA
                     // evaluated for every candidate and selected: no divergent branch
                     const float w = kernel_w(p, fminf(d2 * rsqrtf(fmaxf(d2, 1e-30f)) * p.inv_h, 2.0f));
                     sum += (d2 < p.support2) ? w : 0.0f;
-                    if (LIST && record && interacts<SYS, TRIM>(p, d2, pj.w))
+                    if (LIST && record && records<SYS, TRIM>(p, i, j, d2, pj.w))
                         list_append(nl, i, cnt, j | shift_code(sx, sy, sz));
                 });
         }
     }
-    if (LIST && active) nl.count[i] = cnt;
+    if (LIST && active) {
+        nl.count[i] = cnt;
+        if (cnt > nl.cap && nl.overflow) *nl.overflow = 1u;
+    }
     sum = group_sum<G>(sum);
     if (active && lane == 0) {
         float rho, pr;
@@ -198,6 +202,132 @@ void dispatch(int group, const DevParams &p, const BatchView &bv, const float4 *
     }
 }
 
+// ------------------------------------------------- density from kept lists --
+// Steps between list rebuilds (cmag_system_set_verlet): the density of every
+// particle from its list (all other particles within 2h + skin at the rebuild,
+// sorted indices of the rebuild's order), summed with the walk's arithmetic: the
+// particle itself first (W(0)), then its entries in list order, two per step in
+// paired FP32, zero beyond the support by the clamp of 1 - q/2.  The same pairs
+// as the walk (every particle within 2h has moved less than skin/2 since the
+// rebuild), in another summation order.  One thread per particle, entries of
+// the next step loaded one step ahead.
+template <int SYS, bool PLANAR>
+__global__ void __launch_bounds__(256, 8)
+    k_density_list(DevParams p, const float4 *__restrict__ spos, NeighborList nl,
+                   float4 *__restrict__ meas, float2 *__restrict__ aux)
+{
+    pdl_entry();
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    const float4 pi = spos[i];
+    const bool pinned = SYS == CMAG_POISEUILLE && pi.w == 1.0f;
+    float sum = 0.0f;
+    if (!pinned) {
+        const uint32_t cnt = min(__ldg(nl.count + i), nl.cap);
+        const uint32_t *ep = nl.entry + i;
+        auto shift_of = [&](uint32_t en, float &sx, float &sy, float &sz) {
+            const uint32_t cd = en >> kListIndexBits;
+            sx = (float)((int)(cd & 3u) - 1) * p.wsx;
+            sy = (float)((int)((cd >> 2) & 3u) - 1) * p.wsy;
+            sz = PLANAR ? 0.0f : (float)((int)((cd >> 4) & 3u) - 1) * p.wsz;
+        };
+        if (p.kernel == CMAG_KERNEL_WENDLAND) {
+            const float2 px = make_float2(pi.x, pi.x), py = make_float2(pi.y, pi.y),
+                         pz = make_float2(pi.z, pi.z);
+            const float2 m1 = make_float2(-1.0f, -1.0f), one = make_float2(1.0f, 1.0f),
+                         nh2 = make_float2(-0.5f * p.inv_h, -0.5f * p.inv_h),
+                         h2 = make_float2(2.0f * p.inv_h, 2.0f * p.inv_h),
+                         tiny = make_float2(1e-30f, 1e-30f);
+            float2 acc = make_float2(1.0f, 0.0f);  // the particle itself: W(0) / w_norm = 1
+            uint32_t k = 0;
+            uint32_t e0 = 0, e1 = 0;
+            if (cnt >= 2) {
+                e0 = __ldg(ep);
+                e1 = __ldg(ep + nl.stride);
+            }
+            for (; k + 1 < cnt; k += 2) {
+                uint32_t n0 = 0, n1 = 0;
+                if (k + 3 < cnt) {
+                    n0 = __ldg(ep + (size_t)(k + 2) * nl.stride);
+                    n1 = __ldg(ep + (size_t)(k + 3) * nl.stride);
+                }
+                const float4 a = __ldg(spos + (e0 & kListIndexMask)), c = __ldg(spos + (e1 & kListIndexMask));
+                float2 ax = make_float2(a.x, c.x), ay = make_float2(a.y, c.y), az = make_float2(a.z, c.z);
+                if (SYS != CMAG_DAMBREAK) {
+                    float sx0, sy0, sz0, sx1, sy1, sz1;
+                    shift_of(e0, sx0, sy0, sz0);
+                    shift_of(e1, sx1, sy1, sz1);
+                    ax = __fadd2_rn(ax, make_float2(sx0, sx1));
+                    if (SYS == CMAG_PERISTALSIS) {
+                        ay = __fadd2_rn(ay, make_float2(sy0, sy1));
+                        az = __fadd2_rn(az, make_float2(sz0, sz1));
+                    }
+                }
+                e0 = n0;
+                e1 = n1;
+                const float2 rx = __ffma2_rn(ax, m1, px), ry = __ffma2_rn(ay, m1, py);
+                const float2 dxy = __ffma2_rn(ry, ry, __fmul2_rn(rx, rx));
+                const float2 rz = __ffma2_rn(az, m1, pz);
+                const float2 d2 = PLANAR ? dxy : __ffma2_rn(rz, rz, dxy);
+                const float2 dt = __fadd2_rn(d2, tiny);
+                const float2 rs = make_float2(rsqrtf(dt.x), rsqrtf(dt.y));
+                const float2 d = __fmul2_rn(d2, rs);
+                float2 t = __ffma2_rn(d, nh2, one);
+                t = make_float2(fmaxf(t.x, 0.0f), fmaxf(t.y, 0.0f));
+                const float2 t2 = __fmul2_rn(t, t);
+                const float2 w = __fmul2_rn(__fmul2_rn(t2, t2), __ffma2_rn(d, h2, one));
+                acc = __fadd2_rn(acc, w);
+            }
+            if (k < cnt) {
+                const uint32_t en = __ldg(ep + (size_t)k * nl.stride);
+                float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+                if (SYS != CMAG_DAMBREAK) shift_of(en, sx, sy, sz);
+                const float4 pj = __ldg(spos + (en & kListIndexMask));
+                const float3 r = rel<SYS>(pi, pj, sx, sy, sz);
+                const float dxy = __fmaf_rn(r.y, r.y, __fmul_rn(r.x, r.x));
+                const float d2 = PLANAR ? dxy : __fmaf_rn(r.z, r.z, dxy);
+                const float d = __fmul_rn(d2, rsqrtf(__fadd_rn(d2, 1e-30f)));
+                const float t = fmaxf(__fmaf_rn(d, -0.5f * p.inv_h, 1.0f), 0.0f), t2 = __fmul_rn(t, t);
+                acc.x = __fadd_rn(acc.x, __fmul_rn(__fmul_rn(t2, t2), __fmaf_rn(d, 2.0f * p.inv_h, 1.0f)));
+            }
+            sum = p.w_norm * (acc.x + acc.y);
+        } else {
+            sum = kernel_w(p, 0.0f);  // the particle itself
+            for (uint32_t k = 0; k < cnt; ++k) {
+                const uint32_t en = __ldg(ep + (size_t)k * nl.stride);
+                float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+                if (SYS != CMAG_DAMBREAK) shift_of(en, sx, sy, sz);
+                const float4 pj = __ldg(spos + (en & kListIndexMask));
+                const float3 r = rel<SYS>(pi, pj, sx, sy, sz);
+                const float dxy = __fmaf_rn(r.y, r.y, __fmul_rn(r.x, r.x));
+                const float d2 = PLANAR ? dxy : __fmaf_rn(r.z, r.z, dxy);
+                const float w = kernel_w(p, fminf(d2 * rsqrtf(fmaxf(d2, 1e-30f)) * p.inv_h, 2.0f));
+                sum += (d2 < p.support2) ? w : 0.0f;
+            }
+        }
+    }
+    float rho, pr;
+    if (pinned) {
+        rho = p.rho0;
+        pr = p.p_wall;
+    } else {
+        rho = sum * p.mass;
+        pr = eos_pressure(p, rho);
+    }
+    meas[i] = make_float4(rho, pr, 0.0f, SYS == CMAG_PERISTALSIS ? pi.w : 0.0f);
+    const float inv_rho = 1.0f / rho;
+    aux[i] = make_float2(pr * inv_rho * inv_rho, SYS == CMAG_DAMBREAK ? rho : inv_rho);
+}
+
+template <int SYS>
+void launch_dl(const DevParams &p, const float4 *spos, const NeighborList &nl, float4 *meas, float2 *aux,
+               cudaStream_t st)
+{
+    const uint32_t blocks = (p.n + 255) / 256;
+    if (p.planar) launch_pdl(k_density_list<SYS, true>, blocks, 256, 0, st, p, spos, nl, meas, aux);
+    else launch_pdl(k_density_list<SYS, false>, blocks, 256, 0, st, p, spos, nl, meas, aux);
+}
+
 }  // namespace
 
 // p: the scene's parameters, or for a batch launch group the parameters of any
@@ -210,6 +340,16 @@ void launch_density(const DevParams &p, const BatchView &bv, int group, const fl
     if (p.system == CMAG_DAMBREAK) dispatch<CMAG_DAMBREAK>(group, p, bv, spos, off, meas, aux, nl, st);
     else if (p.system == CMAG_POISEUILLE) dispatch<CMAG_POISEUILLE>(group, p, bv, spos, off, meas, aux, nl, st);
     else dispatch<CMAG_PERISTALSIS>(group, p, bv, spos, off, meas, aux, nl, st);
+}
+
+// Density from the lists kept since the last rebuild (single scenes).
+void launch_density_list(const DevParams &p, const float4 *spos, const NeighborList &nl, float4 *meas,
+                         float2 *aux, cudaStream_t st)
+{
+    if (p.n == 0) return;
+    if (p.system == CMAG_DAMBREAK) launch_dl<CMAG_DAMBREAK>(p, spos, nl, meas, aux, st);
+    else if (p.system == CMAG_POISEUILLE) launch_dl<CMAG_POISEUILLE>(p, spos, nl, meas, aux, st);
+    else launch_dl<CMAG_PERISTALSIS>(p, spos, nl, meas, aux, st);
 }
 
 }  // namespace cmag

@@ -212,14 +212,17 @@ __global__ void __launch_bounds__(256, SYS == CMAG_PERISTALSIS ? (PLANAR ? 5 : 4
             const float2 dxy = __ffma2_rn(ry, ry, __fmul2_rn(rx, rx));
             const float2 d2 = PLANAR ? dxy : __ffma2_rn(rz, rz, dxy);
             const bool w0 = q0.w != (float)CMAG_FLUID, w1 = q1.w != (float)CMAG_FLUID;
-            // plain pair terms: d2 > 0, inside the support unless an un-cut wall
-            const bool ok0 = d2.x > 0.0f && (d2.x < p.support2 || (w0 && !TRIM));
-            const bool ok1 = d2.y > 0.0f && (d2.y < p.support2 || (w1 && !TRIM));
-            if (!(ok0 && ok1)) {
+            // a coincident entry (d2 = 0) has no direction: the scalar path skips it.
+            // Entries beyond the support (lists kept over several steps hold them)
+            // stay on the paired path: 1 - q/2 is clamped at 0 there, which zeroes
+            // their pressure and viscosity terms, and their wall term is masked
+            // unless the wall force has no cut-off.
+            if (!(d2.x > 0.0f && d2.y > 0.0f)) {
                 pair(j0, q0, 0.0f, 0.0f, 0.0f);
                 pair(j1, q1, 0.0f, 0.0f, 0.0f);
                 return;
             }
+            const bool in0 = !TRIM || d2.x < p.support2, in1 = !TRIM || d2.y < p.support2;
             float2 slj = make_float2(0.0f, 0.0f);
             if (__any_sync(__activemask(), w0 || w1)) {  // Lennard-Jones (fluid_kernel.cu:199-207)
                 const float2 inv_d2 = make_float2(__frcp_rn(d2.x), __frcp_rn(d2.y));
@@ -230,8 +233,9 @@ __global__ void __launch_bounds__(256, SYS == CMAG_PERISTALSIS ? (PLANAR ? 5 : 4
                                  inv_d2);
             }
             const float2 inv_d = make_float2(rsqrtf(d2.x), rsqrtf(d2.y));
-            const float2 t = __ffma2_rn(__fmul2_rn(d2, inv_d), make_float2(p.nhalf_inv_h, p.nhalf_inv_h),
-                                        make_float2(1.0f, 1.0f));
+            float2 t = __ffma2_rn(__fmul2_rn(d2, inv_d), make_float2(p.nhalf_inv_h, p.nhalf_inv_h),
+                                  make_float2(1.0f, 1.0f));
+            t = make_float2(fmaxf(t.x, 0.0f), fmaxf(t.y, 0.0f));  // 0 beyond the support
             const float2 g = __fmul2_rn(make_float2(p.dwr_norm, p.dwr_norm), __fmul2_rn(__fmul2_rn(t, t), t));
             const float2 a0 = __ldg(aux + j0), a1 = __ldg(aux + j1);
             const float4 v0 = __ldg(svel + j0), v1 = __ldg(svel + j1);
@@ -248,7 +252,7 @@ __global__ void __launch_bounds__(256, SYS == CMAG_PERISTALSIS ? (PLANAR ? 5 : 4
                 sp.y -= __fdividef(p.av_coeff * vij.y, (ai.y + a1.y) * (d2.y + p.av_eps2));
             }
             sp = __fmul2_rn(sp, __fmul2_rn(make_float2(nmass, nmass), g));
-            const float s0 = w0 ? slj.x : sp.x, s1 = w1 ? slj.y : sp.y;
+            const float s0 = w0 ? (in0 ? slj.x : 0.0f) : sp.x, s1 = w1 ? (in1 ? slj.y : 0.0f) : sp.y;
             ax = __fmaf_rn(s0, rx.x, ax); ay = __fmaf_rn(s0, ry.x, ay);
             if (!PLANAR) az = __fmaf_rn(s0, rz.x, az);
             ax = __fmaf_rn(s1, rx.y, ax); ay = __fmaf_rn(s1, ry.y, ay);
@@ -266,14 +270,17 @@ __global__ void __launch_bounds__(256, SYS == CMAG_PERISTALSIS ? (PLANAR ? 5 : 4
             const float2 rz = __fadd2_rn(make_float2(pi.z, pi.z), make_float2(-tz.x, -tz.y));
             const float2 dxy = __ffma2_rn(ry, ry, __fmul2_rn(rx, rx));
             const float2 d2 = PLANAR ? dxy : __ffma2_rn(rz, rz, dxy);
-            if (!(d2.x > 0.0f && d2.y > 0.0f && d2.x < p.support2 && d2.y < p.support2)) {
+            // coincident entries take the scalar path; entries beyond the support
+            // stay here with 1 - q/2 clamped at 0 (all their terms vanish)
+            if (!(d2.x > 0.0f && d2.y > 0.0f)) {
                 pair(j0, q0, s0.x, s0.y, s0.z);
                 pair(j1, q1, s1.x, s1.y, s1.z);
                 return;
             }
             const float2 inv_d = make_float2(rsqrtf(d2.x), rsqrtf(d2.y));
-            const float2 t = __ffma2_rn(__fmul2_rn(d2, inv_d), make_float2(p.nhalf_inv_h, p.nhalf_inv_h),
-                                        make_float2(1.0f, 1.0f));
+            float2 t = __ffma2_rn(__fmul2_rn(d2, inv_d), make_float2(p.nhalf_inv_h, p.nhalf_inv_h),
+                                  make_float2(1.0f, 1.0f));
+            t = make_float2(fmaxf(t.x, 0.0f), fmaxf(t.y, 0.0f));
             const float2 g = __fmul2_rn(make_float2(p.dwr_norm, p.dwr_norm), __fmul2_rn(__fmul2_rn(t, t), t));
             const float2 a0 = __ldg(aux + j0), a1 = __ldg(aux + j1);
             const float4 v0 = __ldg(svel + j0), v1 = __ldg(svel + j1);
@@ -307,14 +314,17 @@ __global__ void __launch_bounds__(256, SYS == CMAG_PERISTALSIS ? (PLANAR ? 5 : 4
             const float2 rz = __fadd2_rn(make_float2(pi.z, pi.z), make_float2(-q0.z, -q1.z));
             const float2 dxy = __ffma2_rn(ry, ry, __fmul2_rn(rx, rx));
             const float2 d2 = PLANAR ? dxy : __ffma2_rn(rz, rz, dxy);
-            if (!(d2.x > 0.0f && d2.y > 0.0f && d2.x < p.support2 && d2.y < p.support2)) {
+            // coincident entries take the scalar path; entries beyond the support
+            // stay here with 1 - q/2 clamped at 0 (all their terms vanish)
+            if (!(d2.x > 0.0f && d2.y > 0.0f)) {
                 pair(j0, q0, sx0, 0.0f, 0.0f);
                 pair(j1, q1, sx1, 0.0f, 0.0f);
                 return;
             }
             const float2 inv_d = make_float2(rsqrtf(d2.x), rsqrtf(d2.y));
-            const float2 t = __ffma2_rn(__fmul2_rn(d2, inv_d), make_float2(p.nhalf_inv_h, p.nhalf_inv_h),
-                                        make_float2(1.0f, 1.0f));
+            float2 t = __ffma2_rn(__fmul2_rn(d2, inv_d), make_float2(p.nhalf_inv_h, p.nhalf_inv_h),
+                                  make_float2(1.0f, 1.0f));
+            t = make_float2(fmaxf(t.x, 0.0f), fmaxf(t.y, 0.0f));
             const float2 g = __fmul2_rn(make_float2(p.dwr_norm, p.dwr_norm), __fmul2_rn(__fmul2_rn(t, t), t));
             const float2 a0 = __ldg(aux + j0), a1 = __ldg(aux + j1);
             const float4 v0 = __ldg(svel + j0), v1 = __ldg(svel + j1);

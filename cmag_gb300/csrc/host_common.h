@@ -37,9 +37,10 @@ bool planar_allowed(const cmag_sph_params &p, bool z_uniform, bool vz_nonzero);
 SceneLayout layout_for(const cmag_sph_params &p, bool planar, float z_value);
 
 // Interaction-list entries per particle: 1.5 times the lattice neighbour count
-// inside the support (every particle of the searched cell box when rows are not
-// trimmed) plus 32.  Particles with more walk the cells.
-uint32_t list_cap(const cmag_sph_params &p, bool trim);
+// inside the support, or inside 2h + skin (skin in particle spacings) for lists
+// kept over several steps (every particle of the searched cell box when rows are
+// not trimmed), plus 32.  Particles with more walk the cells.
+uint32_t list_cap(const cmag_sph_params &p, bool trim, double skin = 0.0);
 
 // thread-local message returned by cmag_last_error
 void set_last_error(const std::string &msg);

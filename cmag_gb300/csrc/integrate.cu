@@ -56,10 +56,20 @@ __global__ void k_phase_batch(const DevParams *__restrict__ scenes, uint32_t nsc
     if (s < nscenes && scenes[s].system == CMAG_PERISTALSIS) advance_phase(scenes[s], ph + s, k_milli);
 }
 
+// Kept neighbour lists: flag the next step's rebuild when the particle is now
+// more than skin/2 from where the lists were built (a NaN position flags it too).
+__device__ __forceinline__ void check_moved(const DevParams &p, float4 q, float4 b, uint32_t *moved)
+{
+    const float dx = q.x - b.x, dy = q.y - b.y, dz = q.z - b.z;
+    const float d2 = dx * dx + dy * dy + dz * dz;
+    if (!(d2 <= p.vl_move2)) *moved = 1u;
+}
+
 template <bool BATCH>
 __global__ void __launch_bounds__(256)
     k_configure_boundary(DevParams pv, BatchView bv, float4 *__restrict__ pos,
-                         const PhaseState *__restrict__ ph_all)
+                         const PhaseState *__restrict__ ph_all, const float4 *__restrict__ xb,
+                         uint32_t *__restrict__ moved)
 {
     pdl_entry();
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -77,7 +87,10 @@ __global__ void __launch_bounds__(256)
     } else if (q.w < 0.0f) {
         q.y = p.half_fluid_h - wh * get_wave(p, q.x, 0.0f) + p.r * (-q.w - 1.0f);
         pos[i] = q;
+    } else {
+        return;
     }
+    if (xb) check_moved(p, q, xb[i], moved);
 }
 
 template <bool BATCH>
@@ -85,7 +98,8 @@ __global__ void __launch_bounds__(256)
     k_integrate(DevParams pv, BatchView bv, float4 *__restrict__ pos, float4 *__restrict__ vel,
                 float4 *__restrict__ vlf, const float4 *__restrict__ acc,
                 const float4 *__restrict__ vforce, const float4 *__restrict__ pforce,
-                const PhaseState *__restrict__ ph_all)
+                const PhaseState *__restrict__ ph_all, const float4 *__restrict__ xb,
+                uint32_t *__restrict__ moved)
 {
     pdl_entry();
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -111,6 +125,7 @@ __global__ void __launch_bounds__(256)
             if (q.w > 0.0f) q.y = -p.half_fluid_h + p.amplitude * wave - p.r * (q.w - 1.0f);
             else q.y = p.half_fluid_h - p.amplitude * wave + p.r * (-q.w - 1.0f);
             pos[i] = q;
+            if (xb) check_moved(p, q, xb[i], moved);
             return;
         }
         float4 fv = vforce[i], fp = pforce[i];
@@ -138,6 +153,7 @@ __global__ void __launch_bounds__(256)
     }
     pos[i] = q;
     vel[i] = v;
+    if (xb) check_moved(p, q, xb[i], moved);
 }
 
 __global__ void k_gate(DevParams p, float4 *__restrict__ pos, int remove, float dx, float fx, float fy)
@@ -166,24 +182,28 @@ void launch_phase_batch(const DevParams *scenes, uint32_t nscenes, PhaseState *p
 }
 
 void launch_configure_boundary(const DevParams &p, const BatchView &bv, float4 *pos,
-                               const PhaseState *ph, cudaStream_t st)
-{
-    const uint32_t n = bv.scenes ? bv.n_total : p.n;
-    if (n == 0) return;
-    if (bv.scenes) launch_pdl(k_configure_boundary<true>, (n + 255) / 256, 256, 0, st, p, bv, pos, ph);
-    else launch_pdl(k_configure_boundary<false>, (n + 255) / 256, 256, 0, st, p, bv, pos, ph);
-}
-
-void launch_integrate(const DevParams &p, const BatchView &bv, float4 *pos, float4 *vel,
-                      float4 *vlf, const float4 *acc, const float4 *vforce, const float4 *pforce,
-                      const PhaseState *ph, cudaStream_t st)
+                               const PhaseState *ph, cudaStream_t st, const float4 *xb, uint32_t *moved)
 {
     const uint32_t n = bv.scenes ? bv.n_total : p.n;
     if (n == 0) return;
     if (bv.scenes)
-        launch_pdl(k_integrate<true>, (n + 255) / 256, 256, 0, st, p, bv, pos, vel, vlf, acc, vforce, pforce, ph);
+        launch_pdl(k_configure_boundary<true>, (n + 255) / 256, 256, 0, st, p, bv, pos, ph, xb, moved);
     else
-        launch_pdl(k_integrate<false>, (n + 255) / 256, 256, 0, st, p, bv, pos, vel, vlf, acc, vforce, pforce, ph);
+        launch_pdl(k_configure_boundary<false>, (n + 255) / 256, 256, 0, st, p, bv, pos, ph, xb, moved);
+}
+
+void launch_integrate(const DevParams &p, const BatchView &bv, float4 *pos, float4 *vel,
+                      float4 *vlf, const float4 *acc, const float4 *vforce, const float4 *pforce,
+                      const PhaseState *ph, cudaStream_t st, const float4 *xb, uint32_t *moved)
+{
+    const uint32_t n = bv.scenes ? bv.n_total : p.n;
+    if (n == 0) return;
+    if (bv.scenes)
+        launch_pdl(k_integrate<true>, (n + 255) / 256, 256, 0, st, p, bv, pos, vel, vlf, acc, vforce, pforce, ph,
+                   xb, moved);
+    else
+        launch_pdl(k_integrate<false>, (n + 255) / 256, 256, 0, st, p, bv, pos, vel, vlf, acc, vforce, pforce, ph,
+                   xb, moved);
 }
 
 // shiftRightBoundaryD (remove = 0: x += dx) and removeRightBoundaryD

@@ -10,6 +10,11 @@
 
 namespace cmag {
 
+// Launches of this thread without the programmatic-dependent-launch attribute
+// (set while capturing the bodies of a conditional graph node, whose kernels
+// then follow each other with full dependencies).
+inline thread_local bool g_plain_launches = false;
+
 // Launch `kernel` (which begins with pdl_entry()) with programmatic dependent
 // launch allowed: it may start launching while the previous kernel on the stream
 // finishes (in a captured graph too).
@@ -26,7 +31,7 @@ inline void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t s
     cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
     cfg.attrs = attr;
-    cfg.numAttrs = 1;
+    cfg.numAttrs = g_plain_launches ? 0 : 1;
     cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
 }
 
@@ -79,7 +84,8 @@ void launch_onesweep_pass(const uint32_t *kin, const uint32_t *vin, uint32_t *ko
 // particle, its arrival order among the particles of its cell (0, 1, ...; not
 // deterministic).
 void launch_hash(const DevParams &p, const BatchView &bv, const float4 *pos, uint32_t *hash,
-                 uint32_t *cnt, uint32_t *rank, uint32_t *err, cudaStream_t st);
+                 uint32_t *cnt, uint32_t *rank, uint32_t *err, cudaStream_t st,
+                 float4 *snap = nullptr);
 // Stable counting sort of the hashed particles by cell, from the dense offsets
 // (after launch_cell_scan): shash/idx = the hashes and original indices in the
 // order of a stable sort by hash (the radix sort's result exactly), and
@@ -107,6 +113,10 @@ void launch_cell_view(const uint32_t *off, uint32_t scan_base, uint32_t scan_cel
 void launch_density(const DevParams &p, const BatchView &bv, int group, const float4 *spos,
                     const uint32_t *off, float4 *meas, float2 *aux, const NeighborList &nl,
                     cudaStream_t st);
+// Density of every particle from neighbour lists kept since their last rebuild
+// (single scenes; nl.count <= nl.cap for every particle).
+void launch_density_list(const DevParams &p, const float4 *spos, const NeighborList &nl, float4 *meas,
+                         float2 *aux, cudaStream_t st);
 // ph: the Peristalsis phase (one per scene in a batch; read with wall_noslip only)
 void launch_force(const DevParams &p, const BatchView &bv, int group, const float4 *spos,
                   const float4 *svel, const float2 *aux, const uint32_t *idx, const uint32_t *off,
@@ -118,15 +128,40 @@ void launch_force(const DevParams &p, const BatchView &bv, int group, const floa
 // parameters and phase (ph holds one PhaseState per scene).
 void launch_phase(const DevParams &p, PhaseState *ph, float k_milli, cudaStream_t st);
 void launch_configure_boundary(const DevParams &p, const BatchView &bv, float4 *pos,
-                               const PhaseState *ph, cudaStream_t st);
+                               const PhaseState *ph, cudaStream_t st, const float4 *xb = nullptr,
+                               uint32_t *moved = nullptr);
+// xb (may be null): positions at the last rebuild of kept neighbour lists; a
+// particle now more than skin/2 from it sets *moved
 void launch_integrate(const DevParams &p, const BatchView &bv, float4 *pos, float4 *vel,
                       float4 *vlf, const float4 *acc, const float4 *vforce, const float4 *pforce,
-                      const PhaseState *ph, cudaStream_t st);
+                      const PhaseState *ph, cudaStream_t st, const float4 *xb = nullptr,
+                      uint32_t *moved = nullptr);
 // the phase machines of the batch's Peristalsis scenes (one thread per scene)
 void launch_phase_batch(const DevParams *scenes, uint32_t nscenes, PhaseState *ph, float k_milli,
                         cudaStream_t st);
 void launch_gate(const DevParams &p, float4 *pos, int remove, float dx, float fx, float fy,
                  cudaStream_t st);
+
+// ---- neighbour lists kept over several steps (verlet.cu) ------------------------
+// spos[i] = pos[idx[i]], svel[i] = vlf[idx[i]]: the step's positions and leap-frog
+// velocities in the order of the last rebuild.
+void launch_gather_sorted(const uint32_t *idx, const float4 *pos, const float4 *vlf, uint32_t n,
+                          float4 *spos, float4 *svel, cudaStream_t st);
+// Whether this step rebuilds (a particle moved more than skin/2 since the last
+// rebuild, a list overflowed, or the host asked): sets the graph's conditional
+// (cond != 0) and/or decision[0], clears the flags for the next step and counts
+// rebuilds in decision[1].
+struct VerletFlags {
+    uint32_t moved;     // set by integrate (or by the host to force a rebuild)
+    uint32_t overflow;  // set by the rebuilding density pass
+    uint32_t decision;  // this step's choice (1 = rebuild)
+    uint32_t rebuilds;  // rebuilds so far
+};
+void launch_verlet_decide(VerletFlags *flags, unsigned long long cond, int use_cond, cudaStream_t st);
+// positions [start, start + count) were set from the host: *moved = 1 when one
+// lies more than sqrt(move2) from xb
+void launch_verlet_check(const float4 *pos, const float4 *xb, uint32_t start, uint32_t count, float move2,
+                         uint32_t *moved, cudaStream_t st);
 
 // ---- reductions over fluid particles (reduce.cu) -------------------------------
 // out6: order-preserving keys of min x,y,z then max x,y,z (init 0xffffffff, 0)

@@ -216,6 +216,17 @@ __device__ __forceinline__ void list_append(const NeighborList &nl, uint32_t i, 
     ++cnt;
 }
 
+// Whether a list records candidate j (squared distance d2, type w) of particle i:
+// the force's exact pair set (interacts) for per-step lists; for lists kept over
+// several steps every other particle closer than 2h + skin, coincident ones
+// included (the density sums them).
+template <int SYS, bool TRIM>
+__device__ __forceinline__ bool records(const DevParams &p, uint32_t i, uint32_t j, float d2, float w)
+{
+    if (p.verlet) return j != i && d2 < p.list_r2;
+    return interacts<SYS, TRIM>(p, d2, w);
+}
+
 template <int G>
 __device__ __forceinline__ float group_sum(float v)
 {

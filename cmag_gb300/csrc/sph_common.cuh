@@ -56,6 +56,12 @@ struct DevParams {
     // batches: where this scene's cell table and particles start in the shared arrays
     uint32_t table_base;
     uint32_t part_base;
+    // neighbour lists kept over several steps (cmag_system_set_verlet): a list
+    // records every particle j != i closer than sqrt(list_r2) = 2h + skin;
+    // verlet = 0: the per-step lists of the force's exact pair set
+    float list_r2;
+    int32_t verlet;
+    float vl_move2;  // (skin / 2)^2: a larger displacement since the rebuild forces the next one
 };
 
 // Several independent scenes advanced by the same launches: the per-scene
@@ -85,6 +91,7 @@ struct NeighborList {
     uint32_t *count;
     uint32_t cap;
     uint32_t stride;
+    uint32_t *overflow;  // set to 1 when a list outgrew cap (may be null)
 };
 constexpr uint32_t kListIndexBits = 26;
 constexpr uint32_t kListIndexMask = (1u << kListIndexBits) - 1u;

@@ -6,6 +6,7 @@
 // parameter block (the reference keeps one global __constant__ block per library,
 // fluidSystem.cu:17-19) and a CUDA stream.  A step is the reference update()
 // stage sequence; it is captured once as a CUDA graph and replayed.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -61,6 +62,14 @@ struct cmag_system {
     int g_density = 1, g_force = 1;  // lanes per particle (cmag_system_autotune)
     uint32_t *nl_entry = nullptr, *nl_count = nullptr;  // interaction lists (when enabled)
     uint32_t nl_cap = 0;
+    // lists kept over several steps (cmag_system_set_verlet): skin in particle
+    // spacings (0: lists, sort and walk every step), the device flags of the
+    // rebuild choice, positions at the last rebuild (original order), and the
+    // stream that records the rebuild / reuse bodies of the captured step
+    float vl_skin = 0.0f;
+    VerletFlags *vl_flags = nullptr;
+    float4 *vl_xb = nullptr;
+    cudaStream_t vl_side = nullptr;
     cmag_closure *closure = nullptr;   // learned correction added after the force stage
     __nv_bfloat16 *closure_x = nullptr;  // its normalised input rows (n x 16)
 
@@ -237,9 +246,9 @@ SceneLayout layout_for(const cmag_sph_params &p, bool planar, float z_value)
 // Room per particle in the interaction lists: 1.5 times the lattice neighbour
 // count inside the support (or, with the un-cut DamBreak wall force, every
 // particle of the searched cell box) plus 32.  Particles beyond it walk the cells.
-uint32_t list_cap(const cmag_sph_params &p, bool trim)
+uint32_t list_cap(const cmag_sph_params &p, bool trim, double skin)
 {
-    const double dx = 2.0 * p.particle_radius, s = 2.0 * p.smoothing_radius / dx;
+    const double dx = 2.0 * p.particle_radius, s = 2.0 * p.smoothing_radius / dx + skin;
     const bool planar = p.dims == 2;
     double expected = planar ? kPi * s * s : 4.0 / 3.0 * kPi * s * s * s;
     if (!trim) {
@@ -284,7 +293,33 @@ SceneLayout layout_of(const cmag_system *s)
     return l;
 }
 
-DevParams make_dev(const cmag_system *s) { return make_dev_params(s->p, s->n, layout_of(s)); }
+// Kept lists are in use: enabled, with lists allocated, and no learned closure
+// attached (its feature walk needs this step's cell table).
+bool verlet_on(const cmag_system *s) { return s->vl_skin > 0.0f && s->nl_entry && !s->closure; }
+
+DevParams make_dev(const cmag_system *s)
+{
+    DevParams d = make_dev_params(s->p, s->n, layout_of(s));
+    if (verlet_on(s)) {
+        const double half = 0.5 * s->vl_skin * 2.0 * s->p.particle_radius;
+        d.vl_move2 = (float)(half * half);
+    }
+    return d;
+}
+
+// Parameters of the rebuild's density walk: rows trimmed to, and lists recording,
+// every particle within 2h + skin (the density itself still sums q < 2 only).
+DevParams rebuild_params(const cmag_system *s, const DevParams &d)
+{
+    DevParams b = d;
+    const double R = 2.0 * s->p.smoothing_radius + s->vl_skin * 2.0 * s->p.particle_radius;
+    const double rc = R / s->p.cell_size[0];
+    b.verlet = 1;
+    b.list_r2 = (float)(R * R);
+    b.support2_cells = (float)(rc * rc);
+    b.cell_count = std::max(d.cell_count, (int32_t)std::ceil(rc - 1e-6));
+    return b;
+}
 
 NeighborList nl_of(const cmag_system *s)
 {
@@ -294,8 +329,17 @@ NeighborList nl_of(const cmag_system *s)
         nl.count = s->nl_count;
         nl.cap = s->nl_cap;
         nl.stride = s->n;
+        if (verlet_on(s)) nl.overflow = &s->vl_flags->overflow;
     }
     return nl;
+}
+
+// The next step rebuilds the kept lists (positions, parameters or sorted arrays
+// changed behind them).
+void verlet_force(cmag_system *s)
+{
+    if (s->vl_flags && cudaMemsetAsync(&s->vl_flags->moved, 0x01, sizeof(uint32_t), s->stream) != cudaSuccess)
+        (void)cudaGetLastError();
 }
 
 int free_lists(cmag_system *s)
@@ -331,6 +375,7 @@ void invalidate_graph(cmag_system *s)
     if (s->gexec) cudaGraphExecDestroy(s->gexec);
     s->gexec = nullptr;
     s->gvalid = false;
+    verlet_force(s);
 }
 
 // Planar 2-D scenes search and scan only their own z layer (planar_allowed).
@@ -361,9 +406,174 @@ int ensure_events(cmag_system *s, size_t count)
     return CMAG_OK;
 }
 
+// ---- steps on lists kept over several steps ---------------------------------
+// A step either rebuilds (hash, scan, counting sort with the gather, and the
+// density walk over 2h + skin, which records every particle's list and computes
+// the density) or reuses the lists (gather in the rebuild's order, density from
+// the lists); force and integration follow in both.  The choice is made on the
+// device (launch_verlet_decide): in a captured step it selects the body of a
+// conditional graph node, in plain launches the host reads it.
+
+// Peristalsis phase and wall configuration (first in every step); with kept
+// lists the configured walls' displacement is checked like integration's.
+void record_prologue(cmag_system *s, const DevParams &d, cudaStream_t st, bool kept)
+{
+    if (s->p.system != CMAG_PERISTALSIS) return;
+    launch_phase(d, s->phase, s->k_milli, st);
+    launch_configure_boundary(d, BatchView{}, s->pos, s->phase, st, kept ? s->vl_xb : nullptr,
+                              kept ? &s->vl_flags->moved : nullptr);
+}
+
+void record_rebuild(cmag_system *s, const DevParams &d, cudaStream_t st, cudaEvent_t *ev)
+{
+    auto mark = [&](int k) { if (ev) cudaEventRecord(ev[k], st); };
+    launch_hash(d, BatchView{}, s->pos, s->hash[0], s->cnt, s->idx[0], s->err, st, s->vl_xb);
+    launch_cell_scan(s->cnt, s->off, s->scan_cells + 1, s->ws, st);
+    mark(1);
+    launch_cell_sort(s->hash[0], s->idx[0], s->off, s->scan_base, s->n, s->hash[1], s->idx[1], s->idx[0],
+                     s->pos, s->vlf, s->spos, s->svel, s->err, st);
+    mark(2);
+    mark(3);
+    launch_density(rebuild_params(s, d), BatchView{}, 1, s->spos, s->off, s->meas, s->aux, nl_of(s), st);
+    mark(4);
+}
+
+void record_reuse(cmag_system *s, const DevParams &d, cudaStream_t st, cudaEvent_t *ev)
+{
+    auto mark = [&](int k) { if (ev) cudaEventRecord(ev[k], st); };
+    mark(1);
+    mark(2);
+    launch_gather_sorted(s->idx[0], s->pos, s->vlf, s->n, s->spos, s->svel, st);
+    mark(3);
+    launch_density_list(d, s->spos, nl_of(s), s->meas, s->aux, st);
+    mark(4);
+}
+
+void record_kept_tail(cmag_system *s, const DevParams &d, cudaStream_t st, cudaEvent_t *ev,
+                      bool plain_force = false)
+{
+    auto mark = [&](int k) { if (ev) cudaEventRecord(ev[k], st); };
+    g_plain_launches = plain_force;
+    if (s->p.system == CMAG_PERISTALSIS)
+        launch_force(d, BatchView{}, 1, s->spos, s->svel, s->aux, s->idx[0], s->off, s->vforce, s->pforce,
+                     s->phase, nl_of(s), st);
+    else
+        launch_force(d, BatchView{}, 1, s->spos, s->svel, s->aux, s->idx[0], s->off, s->acc, nullptr,
+                     s->phase, nl_of(s), st);
+    g_plain_launches = false;
+    mark(5);
+    launch_integrate(d, BatchView{}, s->pos, s->vel, s->vlf, s->acc, s->vforce, s->pforce, s->phase, st,
+                     s->vl_xb, &s->vl_flags->moved);
+    mark(6);
+}
+
+int ensure_events(cmag_system *s, size_t count);
+
+// one step on kept lists in plain launches (the host waits for the choice)
+int record_kept_host(cmag_system *s, bool timed)
+{
+    const DevParams d = make_dev(s);
+    cudaStream_t st = st_of(s);
+    cudaEvent_t *ev = nullptr;
+    if (timed) {
+        if (ensure_events(s, s->events_used + 7) != CMAG_OK) return CMAG_ERR_CUDA;
+        ev = &s->events[s->events_used];
+        s->events_used += 7;
+    }
+    record_prologue(s, d, st, true);
+    if (ev) cudaEventRecord(ev[0], st);
+    launch_verlet_decide(s->vl_flags, 0ull, 0, st);
+    uint32_t rebuild = 1;
+    CM_CUDA(s, cudaMemcpyAsync(&rebuild, &s->vl_flags->decision, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    CM_CUDA(s, cudaStreamSynchronize(st));
+    if (rebuild) record_rebuild(s, d, st, ev);
+    else record_reuse(s, d, st, ev);
+    record_kept_tail(s, d, st, ev);
+    CM_CUDA(s, cudaGetLastError());
+    return CMAG_OK;
+}
+
+// The step as one graph: prologue, the choice, a conditional node whose bodies
+// are the rebuild and the reuse, then force and integration.  plain_bodies: the
+// bodies' kernels without programmatic dependent launch.
+int capture_kept_graph(cmag_system *s, bool plain_bodies)
+{
+    cudaStream_t st = st_of(s);
+    const DevParams d = make_dev(s);
+    if (!s->vl_side) CM_CUDA(s, cudaStreamCreateWithFlags(&s->vl_side, cudaStreamNonBlocking));
+    CM_CUDA(s, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = cudaSuccess;
+    cudaGraph_t g = nullptr;
+    cudaGraphNode_t cnode = nullptr;
+    const char *what = "capture";
+    do {
+        record_prologue(s, d, st, true);
+        cudaStreamCaptureStatus cs;
+        cudaGraph_t cg = nullptr;
+        const cudaGraphNode_t *deps = nullptr;
+        const cudaGraphEdgeData *edges = nullptr;  // queried (a programmatic edge is not lost)
+        size_t nd = 0;
+        what = "cudaStreamGetCaptureInfo";
+        if ((e = cudaStreamGetCaptureInfo(st, &cs, nullptr, &cg, &deps, &edges, &nd)) != cudaSuccess) break;
+        cudaGraphConditionalHandle h;
+        what = "cudaGraphConditionalHandleCreate";
+        if ((e = cudaGraphConditionalHandleCreate(&h, cg, 0, 0)) != cudaSuccess) break;
+        launch_verlet_decide(s->vl_flags, (unsigned long long)h, 1, st);
+        what = "cudaStreamGetCaptureInfo";
+        if ((e = cudaStreamGetCaptureInfo(st, &cs, nullptr, &cg, &deps, &edges, &nd)) != cudaSuccess) break;
+        cudaGraphNodeParams cp = {};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = h;
+        cp.conditional.type = cudaGraphCondTypeIf;
+        cp.conditional.size = 2;  // body 0: rebuild (condition 1); body 1: reuse
+        what = "cudaGraphAddNode(conditional)";
+        if ((e = cudaGraphAddNode(&cnode, cg, deps, nullptr, nd, &cp)) != cudaSuccess) break;
+        g_plain_launches = plain_bodies;
+        for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
+            what = "cudaStreamBeginCaptureToGraph";
+            e = cudaStreamBeginCaptureToGraph(s->vl_side, cp.conditional.phGraph_out[b], nullptr, nullptr, 0,
+                                              cudaStreamCaptureModeThreadLocal);
+            if (e != cudaSuccess) break;
+            if (b == 0) record_rebuild(s, d, s->vl_side, nullptr);
+            else record_reuse(s, d, s->vl_side, nullptr);
+            cudaGraph_t body = nullptr;
+            what = "body capture";
+            e = cudaStreamEndCapture(s->vl_side, &body);
+        }
+        g_plain_launches = false;
+        if (e != cudaSuccess) break;
+        what = "cudaStreamUpdateCaptureDependencies";
+        if ((e = cudaStreamUpdateCaptureDependencies(st, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies)) !=
+            cudaSuccess)
+            break;
+        // the force kernel follows the conditional node with a full dependency
+        record_kept_tail(s, d, st, nullptr, true);
+        what = "launch";
+        e = cudaGetLastError();
+    } while (false);
+    cudaError_t e2 = cudaStreamEndCapture(st, &g);
+    if (e == cudaSuccess) {
+        e = e2;
+        what = "stream capture";
+    }
+    if (e == cudaSuccess) {
+        what = "graph instantiate";
+        e = cudaGraphInstantiate(&s->gexec, g, 0);
+    }
+    if (g) cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        s->gexec = nullptr;
+        return fail(s, CMAG_ERR_CUDA, std::string("kept-list step graph: ") + what + ": " + cudaGetErrorString(e));
+    }
+    s->gvalid = true;
+    return CMAG_OK;
+}
+
 // Enqueue the stages of one step up to and including `last` on the stream.
 int record_step(cmag_system *s, int last, bool timed)
 {
+    if (verlet_on(s) && last >= CMAG_STAGE_INTEGRATE) return record_kept_host(s, timed);
     const DevParams d = make_dev(s);
     cudaStream_t st = st_of(s);
     const cmag_sph_params &p = s->p;
@@ -410,6 +620,8 @@ int record_step(cmag_system *s, int last, bool timed)
         launch_integrate(d, BatchView{}, s->pos, s->vel, s->vlf, s->acc, s->vforce, s->pforce, s->phase, st);
     mark(6);
     CM_CUDA(s, cudaGetLastError());
+    // the sorted order (and the lists) of this step replace the kept ones
+    if (s->vl_flags) verlet_force(s);
     return CMAG_OK;
 }
 
@@ -451,6 +663,11 @@ int upload_phase(cmag_system *s)
 int capture_graph(cmag_system *s)
 {
     invalidate_graph(s);
+    if (verlet_on(s)) {
+        // conditional bodies with programmatic dependent launch, else without
+        if (capture_kept_graph(s, false) == CMAG_OK) return CMAG_OK;
+        return capture_kept_graph(s, true);
+    }
     cudaStream_t st = st_of(s);
     CM_CUDA(s, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     int rc = record_step(s, CMAG_STAGE_INTEGRATE, false);
@@ -511,10 +728,11 @@ void free_all(cmag_system *s)
     void *ptrs[] = {s->pos, s->vel, s->vlf, s->meas, s->acc, s->vforce, s->pforce, s->pred,
                     s->spos, s->svel, s->hash[0], s->hash[1], s->idx[0], s->idx[1], s->cnt,
                     s->off, s->aux, s->ws, s->err, s->phase, s->view_cs, s->view_ce, s->red,
-                    s->zflag, s->closure_x};
+                    s->zflag, s->closure_x, s->vl_flags, s->vl_xb};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     free_lists(s);
+    if (s->vl_side) cudaStreamDestroy(s->vl_side);
     if (s->own_stream) cudaStreamDestroy(s->own_stream);
 }
 
@@ -749,6 +967,13 @@ int cmag_system_set_array(cmag_system *s, int32_t array, const float *host, uint
         else if (start == 0 && count == s->n && array == CMAG_VELOCITY) s->vz_nonzero = false;
     }
     refresh_layout(s);
+    // kept lists depend on positions only: a rebuild when an uploaded position
+    // lies more than skin/2 from where the lists were built
+    if (pos_up && verlet_on(s)) {
+        launch_verlet_check(s->pos, s->vl_xb, start, count, make_dev(s).vl_move2, &s->vl_flags->moved,
+                            st_of(s));
+        CM_CUDA(s, cudaGetLastError());
+    }
     return CMAG_OK;
 }
 
@@ -1172,6 +1397,7 @@ int cmag_system_autotune(cmag_system *s, int32_t reps)
 {
     if (!s) return fail(nullptr, CMAG_ERR_INVALID, "null handle");
     if (reps < 1) reps = 1;
+    if (s->vl_skin > 0.0f) return CMAG_OK;  // kept lists: one lane per particle, nothing to choose
     // hash, sort and gather of the current state, then time each variant
     PhaseState saved = s->host_phase;
     int rc = record_step(s, CMAG_STAGE_REORDER, false);
@@ -1246,9 +1472,55 @@ int cmag_system_set_neighbor_lists(cmag_system *s, int32_t enable)
 {
     if (!s) return fail(nullptr, CMAG_ERR_INVALID, "null handle");
     if (enable < 0) return fail(s, CMAG_ERR_INVALID, "enable must be 0, 1 or an entry count");
+    s->vl_skin = 0.0f;  // per-step lists (or none): lists are no longer kept
     int rc = enable ? alloc_lists(s, enable > 1 ? (uint32_t)enable : 0u) : free_lists(s);
     invalidate_graph(s);
     return rc;
+}
+
+int cmag_system_set_verlet(cmag_system *s, float skin)
+{
+    if (!s) return fail(nullptr, CMAG_ERR_INVALID, "null handle");
+    if (!(skin >= 0.0f) || skin > 4.0f) return fail(s, CMAG_ERR_INVALID, "skin must be in [0, 4] particle spacings");
+    if (skin == 0.0f) {
+        s->vl_skin = 0.0f;
+        invalidate_graph(s);
+        return CMAG_OK;
+    }
+    const DevParams d = make_dev_params(s->p, s->n, layout_of(s));
+    if (!d.trim)
+        return fail(s, CMAG_ERR_INVALID,
+                    "kept lists need a cut-off on every interaction (DamBreak: lj_cutoff = 1) and cubic cells");
+    const double rc = (2.0 * s->p.smoothing_radius + skin * 2.0 * s->p.particle_radius) / s->p.cell_size[0];
+    const uint32_t cb = (uint32_t)std::ceil(rc - 1e-6);
+    for (int k = 0; k < (s->planar ? 2 : 3); ++k)
+        if (s->p.grid_size[k] < 2 * cb + 1)
+            return fail(s, CMAG_ERR_INVALID, "grid too small for the list radius 2h + skin");
+    if (!s->vl_flags) {
+        CM_CUDA(s, cudaMalloc((void **)&s->vl_flags, sizeof(VerletFlags)));
+        CM_CUDA(s, cudaMemset(s->vl_flags, 0, sizeof(VerletFlags)));
+    }
+    if (!s->vl_xb) CM_CUDA(s, cudaMalloc((void **)&s->vl_xb, sizeof(float4) * (size_t)s->n));
+    const uint32_t cap = list_cap(s->p, true, skin);
+    if (int rc2 = alloc_lists(s, cap)) return rc2;
+    s->vl_skin = skin;
+    invalidate_graph(s);  // and the next step rebuilds
+    return CMAG_OK;
+}
+
+int cmag_system_get_verlet(cmag_system *s, float *skin, uint32_t *rebuilds)
+{
+    if (!s) return fail(nullptr, CMAG_ERR_INVALID, "null handle");
+    if (skin) *skin = s->vl_skin;
+    if (rebuilds) {
+        VerletFlags f{};
+        if (s->vl_flags) {
+            CM_CUDA(s, cudaMemcpyAsync(&f, s->vl_flags, sizeof(f), cudaMemcpyDeviceToHost, st_of(s)));
+            CM_CUDA(s, cudaStreamSynchronize(st_of(s)));
+        }
+        *rebuilds = f.rebuilds;
+    }
+    return CMAG_OK;
 }
 
 int cmag_system_get_neighbor_lists(const cmag_system *s, int32_t *enabled, uint32_t *cap)

@@ -57,7 +57,7 @@ def peristalsis_params(dt, fluid_size, amplitude, wave_speed, soundspeed, gravit
 
 def reference_count(p):
     n = ctypes.c_uint32()
-    check(lib().cmag_reference_particle_count(ctypes.byref(p), ctypes.byref(n)))
+    check(lib().cmag_reference_particle_count(ctypes.byref(_abi.as_params(p)), ctypes.byref(n)))
     return n.value
 
 
@@ -191,7 +191,9 @@ def batched_scenes(scenes=256, seed=1973, lo=4096, hi=262144, nu_lo=1e-6, nu_hi=
 
     Poiseuille (the reference channel, Poiseuille.Report/dump.h): fy rows across a
     1 mm channel (fy = sqrt(count)), fx = count / fy columns along the periodic x
-    axis, 3 wall rows each side, grid (fx, fy + 12, 4); mu = 1000 nu and the body
+    axis, 3 wall rows each side, grid (fx, fy + 12, 4); the reference particle mass
+    scaled with the particle area, (58 / fy)^2, for the reference's rest density;
+    mu = 1000 nu and the body
     force 1e-4 nu / 1e-6, so every channel has the reference's u_max = F l^2 / (8 nu)
     = 1.25e-5 m/s; dt = min(1e-4, 0.125 h^2 / nu).
     Dam break (the reference column, DamBreak.Report/XFrontTest.h:17-23): a num x
@@ -218,6 +220,10 @@ def batched_scenes(scenes=256, seed=1973, lo=4096, hi=262144, nu_lo=1e-6, nu_hi=
             fx = max(16, int(round(target / fy)))
             r = 1.0 / (2 * fy * 1000)
             p = poiseuille_params((fx, fy, 1), off, (fx, fy + 2 * off + 6, 4), r)
+            # the reference's particle mass belongs to its 58-row channel
+            # (poiseuilleFlowSystem.cpp:48-49); it scales with the particle area
+            # so every channel has the reference's rest density
+            p.particle_mass = F32(float(p.particle_mass) * (58.0 / fy) ** 2)
             p.mu = F32(1000.0 * nu)
             p.gravity[0] = F32(1e-4 * nu / 1e-6)
             h = float(p.smoothing_radius)

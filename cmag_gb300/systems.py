@@ -34,7 +34,7 @@ class _System:
 
     def __init__(self, params, num_particles=None):
         L = lib()
-        self._p = params.copy()
+        self._p = _abi.as_params(params).copy()
         if num_particles is None:
             n = ctypes.c_uint32()
             check(L.cmag_reference_particle_count(ctypes.byref(self._p), ctypes.byref(n)))
@@ -152,7 +152,7 @@ class _System:
         return p
 
     def set_params(self, p):
-        self._chk(lib().cmag_system_set_params(self._h, ctypes.byref(p)))
+        self._chk(lib().cmag_system_set_params(self._h, ctypes.byref(_abi.as_params(p))))
 
     @property
     def numGridCells(self):
@@ -215,6 +215,17 @@ class _System:
         (density lanes, force lanes, lists on)."""
         self._chk(lib().cmag_system_autotune(self._h, int(reps)))
         return self.groups() + (self.neighbor_lists()[0],)
+
+    def set_verlet(self, skin):
+        """Neighbour lists kept over several steps with this skin (in particle
+        spacings; 0: the reference's per-step sort and walk)."""
+        self._chk(lib().cmag_system_set_verlet(self._h, float(skin)))
+
+    def verlet(self):
+        """(skin, rebuilds so far)."""
+        sk, nb = ctypes.c_float(), ctypes.c_uint32()
+        self._chk(lib().cmag_system_get_verlet(self._h, ctypes.byref(sk), ctypes.byref(nb)))
+        return sk.value, nb.value
 
     def set_neighbor_lists(self, enable, cap=None):
         """Interaction lists on/off; cap: entries per particle (default automatic)."""

@@ -316,6 +316,29 @@ int cmag_system_get_groups(const cmag_system *s, int32_t *density_lanes, int32_t
  * a particle with more neighbours walks the cells).  Fewer than 2^26 particles. */
 int cmag_system_set_neighbor_lists(cmag_system *s, int32_t enable);
 int cmag_system_get_neighbor_lists(const cmag_system *s, int32_t *enabled, uint32_t *cap);
+/* Neighbour lists kept over several steps.  No counterpart in the reference,
+ * which hashes, sorts and walks the 7^3 neighbour cells on every step
+ * (fluidSystem.cpp:257-319).  skin > 0 (in particle spacings 2r, at most 4):
+ * a rebuild step hashes and sorts as the reference does and records, for every
+ * particle, all other particles within 2h + skin; the following steps gather the
+ * current positions in that order and sum density and forces over the lists,
+ * testing q < 2 per pair, until some particle has moved more than skin/2 since
+ * the rebuild (checked on the device by integration), which makes the next step
+ * a rebuild.  Every pair within 2h is therefore visited, as the reference's
+ * walk does, in another summation order (results within FP32 rounding of it).
+ *  - Between rebuilds the sorted-order arrays (HASH, INDEX, CELLSTART/END,
+ *    CELLOFFSET, SORTEDPOSITION, SORTEDVELOCITY, MEASURES) keep the order of
+ *    the last rebuild; SORTEDPOSITION/SORTEDVELOCITY hold the step's positions
+ *    and leap-frog velocities in that order.  skin 0 restores the reference's
+ *    per-step sort.
+ *  - Needs a cut-off on every interaction (DamBreak: lj_cutoff = 1).  Setting
+ *    arrays or parameters forces a rebuild; a list that outgrows its room makes
+ *    every step a rebuild until it fits again.  Not used while a learned closure
+ *    is attached (its features walk this step's cells).
+ *  - Memory: the interaction lists at radius 2h + skin plus 16 bytes per particle.
+ * get_verlet: the skin (0: off) and the number of rebuilds so far. */
+int cmag_system_set_verlet(cmag_system *s, float skin);
+int cmag_system_get_verlet(cmag_system *s, float *skin, uint32_t *rebuilds);
 /* Autotune: on the current state, time the density and force kernels for every
  * lane count and with interaction lists (`reps` launches each) and keep the
  * fastest.  Both kernels are recomputed from scratch every step; the choice

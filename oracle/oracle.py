@@ -59,6 +59,27 @@ def build_ref(ref_root=None):
     return True
 
 
+REF_GPU_CUBIN = os.path.join(REF_DIR, "ref_dambreak_sm103a.cubin")
+REF_GPU_LIB = os.path.join(REF_DIR, "libref_gpu.so")
+
+
+def build_ref_gpu(ref_root=None):
+    """The reference's DamBreak kernels for the GPU: the cubin where the reference
+    tree exists, and the launcher wherever the cubin exists.  Returns whether
+    the launcher is ready."""
+    if have_ref(ref_root):
+        out = subprocess.run(_ref_make_args(ref_root) + ["gpu-cubin"], capture_output=True, text=True)
+        if out.returncode != 0:
+            raise RuntimeError("reference cubin build failed:\n" + out.stdout + out.stderr)
+    if not os.path.exists(REF_GPU_CUBIN):
+        return False
+    out = subprocess.run(["make", "-s", "-C", os.path.join(HERE, "ref"), "gpu-launcher"], capture_output=True,
+                         text=True)
+    if out.returncode != 0:
+        raise RuntimeError("reference GPU launcher build failed:\n" + out.stdout + out.stderr)
+    return True
+
+
 def lib():
     global _lib
     if _lib is None:

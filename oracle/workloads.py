@@ -145,6 +145,10 @@ def batched_scenes(scenes=256, seed=1973, lo=4096, hi=262144, nu_lo=1e-6, nu_hi=
             fx = max(16, int(round(target / fy)))
             r = 1.0 / (2 * fy * 1000)
             p = O.poiseuille_params((fx, fy, 1), off, (fx, fy + 2 * off + 6, 4), r)
+            # the reference's particle mass belongs to its 58-row channel
+            # (poiseuilleFlowSystem.cpp:48-49); it scales with the particle area
+            # so every channel has the reference's rest density
+            p.particle_mass = F32(float(p.particle_mass) * (58.0 / fy) ** 2)
             p.mu = F32(1000.0 * nu)
             p.gravity[0] = F32(1e-4 * nu / 1e-6)
             h = float(p.smoothing_radius)

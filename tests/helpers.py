@@ -115,3 +115,61 @@ def compare_step(gpu, pre, post, label="", threads=1):
         out[name] = float((err / (TOL_ULP * mag + 1e-30)).max())
         assert out[name] <= 1.0, "%s%s error %g of its bound" % (label, name, out[name])
     return out
+
+
+def compare_step_kept(gpu, pre, post, label="", threads=1):
+    """compare_step for a solver on kept neighbour lists (cmag_system_set_verlet):
+    its sorted arrays keep the order of the last list rebuild, so density and
+    pressure are compared per particle (original order, through each side's
+    sorted index) and the oracle recomputes the forces on the GPU's measures
+    brought into the oracle's sorted order.  gpu: a state() dict."""
+    from oracle import oracle as O
+    p = post.p
+    out = {}
+    n = post.n
+    meas_orig = np.zeros((n, 4), np.float32)
+    meas_orig[gpu["idx"]] = gpu["meas"]
+    want_orig = np.zeros((n, 4), np.float32)
+    want_orig[post.idx] = post.meas
+    # the gathers in the rebuild's order hold the step's positions and velocities
+    spos_orig = np.zeros((n, 4), np.float32)
+    spos_orig[gpu["idx"]] = gpu["spos"]
+    assert_int_equal(spos_orig.view(np.uint32), pre.pos.view(np.uint32), label + "gathered positions")
+    svel_orig = np.zeros((n, 4), np.float32)
+    svel_orig[gpu["idx"]] = gpu["svel"]
+    assert_int_equal(svel_orig.view(np.uint32), pre.vlf.view(np.uint32), label + "gathered leap-frog velocities")
+
+    rho0 = float(p.rest_density)
+    out["rho"] = rel_err(meas_orig[:, 0], want_orig[:, 0], rho0)
+    assert out["rho"] <= TOL_RHO, "%sdensity error %g" % (label, out["rho"])
+    pmax = float(np.abs(want_orig[:, 1]).max()) + 1e-30
+    dp = np.abs(meas_orig[:, 1].astype(np.float64) - want_orig[:, 1]).max()
+    bound = TOL_P * pmax + eos_slope(p) * TOL_RHO * rho0
+    out["p"] = float(dp / bound)
+    assert dp <= bound, "%spressure error %g > %g" % (label, dp, bound)
+
+    meas_oracle_order = np.ascontiguousarray(meas_orig[post.idx])
+    a, b, sa, sb = post.forces_on(meas_oracle_order, threads=threads)
+    if p.system == _abi.PERISTALSIS:
+        pairs = (("vforce", a, sa), ("pforce", b, sb))
+    else:
+        pairs = (("acc", a, sa),)
+    for name, want, sc in pairs:
+        err = np.abs(gpu[name][:, :3].astype(np.float64) - want[:, :3])
+        scale = sc[:, :3].astype(np.float64) + 1e-30
+        out[name] = float((err / scale).max())
+        assert out[name] <= TOL_TERM, "%s%s error %g of its conditioning scale" % (label, name, out[name])
+
+    zeros = np.zeros_like(gpu["pos"])
+    pos, vel, vlf = O.integrate_from(pre, post, gpu.get("acc", zeros), gpu.get("vforce", zeros),
+                                     gpu.get("pforce", zeros))
+    dt = float(p.delta_time)
+    g = np.abs(np.asarray(list(p.gravity), np.float64))
+    accm = sum(np.abs(gpu[k][:, :3].astype(np.float64)) for k in ("acc", "vforce", "pforce") if k in gpu)
+    vmag = np.abs(pre.vel[:, :3].astype(np.float64)) + (g + accm) * dt
+    for name, want, mag in (("vel", vel, vmag), ("vlf", vlf, vmag),
+                            ("pos", pos, np.abs(pre.pos[:, :3].astype(np.float64)) + vmag * dt)):
+        err = np.abs(gpu[name][:, :3].astype(np.float64) - want[:, :3])
+        out[name] = float((err / (TOL_ULP * mag + 1e-30)).max())
+        assert out[name] <= 1.0, "%s%s error %g of its bound" % (label, name, out[name])
+    return out

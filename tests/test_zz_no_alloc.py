@@ -1,9 +1,10 @@
 """cmag_sort_particles_noalloc: the stable (hash, index) sort for callers that
-cannot allocate device memory where they sort (inside a stream capture, in a
-latency-critical loop, or under a host's own memory pool).  Its workspace is a
-fixed array inside the library.  The test calls it through the C ABI twice in a
-row (the shared scratch keeps the first call's contents) and checks each result
-against the allocating entry point, bit for bit, as the sort is integer work.
+cannot allocate device memory where they sort (a latency-critical loop where an
+allocation would stall the device, or a host whose device memory all comes from
+its own pool).  Its workspace is a fixed array inside the library.  The test
+calls it through the C ABI twice in a row (the shared scratch keeps the first
+call's contents) and checks each result against the allocating entry point, bit
+for bit, as the sort is integer work.
 This file sorts last on purpose: run alone or after every other test, it must
 pass either way."""
 import ctypes
