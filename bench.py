@@ -307,9 +307,20 @@ def make_batched(rank, world):
     groups = run.b.groups()
     cfg = batched_config(run.P, run.N, run.F, run.D)
     cfg["launch_groups"] = len(groups)
-    meta = {"force_b": 68, "integrate_b": 112,
-            "launches": 1 + 3 + 2 + 2 * len(groups) + 1}
+    meta = {"force_b": 68, "integrate_b": 112, "groups": groups}
     return run, run.n, int(sum(run.F)), cfg, meta
+
+
+def merged_runs(groups, key):
+    """Neighbour-loop launches per stage: consecutive launch groups with the same
+    kernel variant (family, search shape, lists, lanes `key`) share one launch."""
+    runs, prev = 0, None
+    for g in groups:
+        v = (g["system"], g["planar"], g["trim"], g["lists"], g[key])
+        if v != prev:
+            runs += 1
+        prev = v
+    return runs
 
 
 def cpu_run(name, steps, threads):
@@ -326,10 +337,11 @@ def cpu_run(name, steps, threads):
 
 
 def front_of(s, column_width):
-    """Surge front: the largest fluid x over the column width (XFrontTest.h:64-86),
-    from a device reduction."""
+    """Surge front over the initial column width: the largest fluid x
+    (XFrontTest.h:64-86, a device reduction) plus the particle radius, i.e. the
+    free surface, so that runs at different spacings compare."""
     lo, hi = s.fluid_extent()
-    return float(hi[0]) / column_width
+    return (float(hi[0]) + float(s.params.particle_radius)) / column_width
 
 
 def run_to_t1(s, p, kept, t_end=1.0, sample_dt=0.01, column_width=0.5):
@@ -426,6 +438,95 @@ def reference_gpu_bar(steps=20, warmup=5):
         "reference_ms_per_step": ms3 / k3, "reference_updates_per_s": 524288 * k3 / (ms3 / 1e3),
         "reference_stage_ms": {k: round(v / k3, 5) for k, v in zip(names, st3)}}
     return out
+
+
+def front_errors(fronts, fine, tank_over_column):
+    """Max and mean relative front error against the fine run while the fine front
+    is short of the far wall (95 % of the tank length)."""
+    fronts, fine = np.asarray(fronts), np.asarray(fine)
+    m = min(len(fronts), len(fine))
+    fronts, fine = fronts[:m], fine[:m]
+    judged = fine < 0.95 * tank_over_column
+    err = np.abs(fronts - fine) / fine
+    return float(err[judged].max()), float(err[judged].mean())
+
+
+def learned_to_t1(fine, t_end=1.0, seed=1973):
+    """The learned coarse form (32x64x32 fluid, dt 1e-4, the closure trained by
+    cmag_gb300/train_closure.py on other seeds) and the plain coarse run, from the
+    block means of the fine initial state of `seed`, to t_end: device seconds and
+    surge-front errors against the plain fine run (`fine`: run_to_t1's result for
+    the same seed, fronts every 0.01 s)."""
+    from cmag_gb300 import train_closure as TC
+    from cmag_gb300.closure import Pair, rollout
+    if not os.path.exists(TC.DEFAULT_OUT):
+        return {"unavailable": "no trained closure (%s)" % os.path.relpath(TC.DEFAULT_OUT, HERE)}
+    c, rec = TC.load()
+    pair = Pair()
+    tank_over_column = pair.tank_f[0] / pair.fluid_f[0]
+    out = {"strength": rec["strength"], "train_seeds": len(rec["train_seeds"]),
+           "validation_seed": rec["validation_seed"], "held_out_seed": seed,
+           "validation_front_err": rec["validation_front_err"], "window_coarse_steps": rec["window_coarse_steps"]}
+    for name in ("coarse", "coarse_closure"):
+        pair.coarse.set_closure(c if name == "coarse_closure" and rec["strength"] > 0 else None)
+        pair.start(seed)
+        pair.coarse.update_n(1)  # graph capture, outside the timing
+        pair.start(seed)
+        secs, times, fronts = rollout(pair.coarse, t_end, 0.01, TC.COLUMN_WIDTH)
+        emax, emean = front_errors(fronts, fine["fronts"], tank_over_column)
+        out[name] = {"device_s": secs, "steps": int(round(t_end / float(pair.pc.delta_time))),
+                     "front_err_max": emax, "front_err_mean": emean,
+                     "speedup_vs_fine": fine["device_s"] / secs,
+                     "meets_2pct_front": emax <= 0.02}
+    pair.coarse.set_closure(None)
+    pair.close()
+    c.close()
+    return out
+
+
+def batched_to_t1(steps=10):
+    """The batch's 128 dam-break scenes to t = 1 s (per-scene dt), batched against
+    one scene at a time (each alone, at its autotuned best): device seconds
+    extrapolated from `steps` measured steps of each configuration (the batch
+    steps every scene until the last reaches t = 1 s; alone, each scene stops at
+    its own).  A scene's batched trajectory is its lone trajectory bit for bit,
+    so the surge-front error of batching is zero."""
+    import cmag_gb300 as cm
+    from cmag_gb300 import presets
+    from cmag_gb300.batch import Batch
+    P, N, F, D = presets.batched_scenes()
+    ks = [k for k in range(len(P)) if D[k][0] == "dambreak"]
+    Pd, Nd = [P[k] for k in ks], [N[k] for k in ks]
+    b = Batch(Pd, Nd)
+    for k in range(len(Pd)):
+        b.reset(k)
+        b.dambreak_remove_right_boundary(k)
+    b.set_graphs(True, 10)
+    b.update_n(10)
+    b.autotune(2)
+    b.update_n(10)
+    ms_b = b.timed_update(steps) / steps
+    b.close()
+    t_single = []
+    for k in ks:
+        s = cm.DamBreakSystem(params=P[k], num_particles=N[k])
+        s.reset()
+        s.removeRightBoundary()
+        s.update_n(3)
+        s.autotune(2)
+        s.update_n(3)
+        t_single.append(s.timed_update(steps) / steps)
+        s.close()
+    to_t1 = [int(np.ceil(1.0 / float(P[k].delta_time))) for k in ks]
+    plain_s = sum(n * t for n, t in zip(to_t1, t_single)) / 1e3
+    batched_s = max(to_t1) * ms_b / 1e3
+    return {"scenes": len(ks), "particles": int(sum(Nd)), "fluid": int(sum(F[k] for k in ks)),
+            "steps_to_t1": [min(to_t1), max(to_t1)], "measured_steps": steps,
+            "batch_ms_per_step": ms_b, "sum_of_single_ms_per_step": float(sum(t_single)),
+            "plain_device_s_to_t1": plain_s, "batched_device_s_to_t1": batched_s,
+            "speedup": plain_s / batched_s, "front_err_vs_plain": 0.0,
+            "note": "device seconds extrapolated from measured per-step times; batched trajectories are "
+                    "bit-identical to the lone runs (tests/test_gpu_batch.py)"}
 
 
 def dist_init(n_gpus):
@@ -632,14 +733,17 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--neighbor-lists", choices=["auto", "on", "off"], default="auto",
                     help="single-scene workloads: the autotuner's choice, or force interaction lists on/off")
-    ap.add_argument("--cpu-steps", type=int, default=1)
-    ap.add_argument("--verlet", type=float, default=0.4,
+    ap.add_argument("--cpu-steps", type=int, default=20,
+                    help="full steps of the CPU baseline sample (about 10 s on 16 cores for the dam break)")
+    ap.add_argument("--verlet", type=float, default=0.0,
                     help="single scenes: neighbour lists kept over steps with this skin (particle spacings); "
                          "0: the reference's per-step sort and cell walk")
     ap.add_argument("--t-start", type=float, default=0.2,
                     help="dam break: simulated seconds run (untimed, part of the setup) before warm-up")
     ap.add_argument("--no-t1", action="store_true", help="skip the plain run to t = 1 s")
     ap.add_argument("--no-ref-gpu", action="store_true", help="skip timing the reference's kernels on the GPU")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned coarse run to t = 1 s")
+    ap.add_argument("--no-batched-t1", action="store_true", help="skip the batched dam breaks to t = 1 s")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -686,6 +790,11 @@ def main():
     # particle of the neighbour loops on this workload
     s.update_n(args.warmup)
     tuning = {"lanes_density_force_lists": list(s.autotune(3))}
+    if batched:
+        groups = s.b.groups()
+        meta["launches"] = 1 + 3 + 2 + merged_runs(groups, "density_lanes") + merged_runs(groups, "force_lanes") + 1
+        tuning["launch_groups"] = len(groups)
+        tuning["neighbour_launches_per_step"] = meta["launches"] - 7
     if kept:
         tuning = {"kept_lists_skin": args.verlet}
     if args.neighbor_lists != "auto" and not batched:
@@ -746,7 +855,7 @@ def main():
             fp32 = {"candidates_per_particle": round(cand, 1), "neighbours_per_particle": round(inter, 1),
                     "peak_tflops": round(peak_tf, 1),
                     "peak_kind": "nominal: %d SMs x 128 FP32 lanes x 2 flop x sampled SM clock" % sms}
-            lists = bool(tuning["lanes_density_force_lists"][2])
+            lists = bool(tuning.get("lanes_density_force_lists", [1, 1, True])[2])
             fp32["force_path"] = "interaction lists" if lists else "cell walk"
             for k, per_pair in (("density", FLOPS_DENSITY_PAIR), ("force", FLOPS_FORCE_PAIR)):
                 # the list-driven force visits interacting pairs only; the DamBreak
@@ -809,7 +918,8 @@ def main():
             v, dt, sample = cpu_run_batched(s.P, s.N, s.F, s.D, threads)
         else:
             v, dt = cpu_run(args.workload, args.cpu_steps, threads)
-            sample = "%d full step(s) of the same %d-particle scene" % (args.cpu_steps, n)
+            sample = ("%d full step(s) of the same %d-particle scene from its initial state (oracle "
+                      "restatement of the reference kernels, all host threads)" % (args.cpu_steps, n))
         line["cpu_baseline"] = {"value": v, "unit": "particle-updates/s", "cores": threads,
                                 "kind": "port", "seconds": dt, "sample": sample}
     if not batched and args.workload == "dambreak3d" and rank == 0 and world == 1 and not args.no_ref_gpu:
@@ -817,12 +927,21 @@ def main():
         bar = line["reference_gpu"].get("dambreak3d_954860_reference_loops")
         if bar:
             line["reference_gpu"]["own_vs_reference_loops"] = value / bar["reference_updates_per_s"]
-    if not batched and args.workload == "dambreak3d" and not args.no_t1:
+    if not batched and args.workload == "dambreak3d" and not args.no_t1 and world == 1:
+        # the metric's second half: wall-time to t = 1 s at <= 2 % front error,
+        # plain fine vs learned coarse vs batched
         t1 = run_to_t1(s, p, args.verlet if kept else 0.0)
         line["to_t1"] = {"plain_fine": {k: (round(v, 5) if isinstance(v, float) else v) for k, v in t1.items()
                                         if k not in ("times", "fronts")},
                          "fronts_every_0.05s": [round(f, 4) for f in t1["fronts"][::5]]}
-    s.close()
+        s.close()
+        s = None
+        if not args.no_learned:
+            line["to_t1"]["learned_coarse"] = learned_to_t1(t1)
+        if not args.no_batched_t1:
+            line["to_t1"]["batched_dambreak128"] = batched_to_t1()
+    if s is not None:
+        s.close()
     if rank == 0:
         print(json.dumps(line))
     if dist:

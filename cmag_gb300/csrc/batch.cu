@@ -242,21 +242,36 @@ bool alloc_lists(cmag_batch *b)
     return true;
 }
 
-// Neighbour-loop launches of every group: groups after the first run on side
+// Neighbour-loop launches of every group.  Consecutive groups that run the same
+// kernel variant (family, search shape, lanes per particle, lists) are one launch
+// over their joined particle range: every particle reads its own scene's
+// parameters, so merging changes no result.  Launches after the first run on side
 // streams forked from the main stream and joined before the next stage.
 int launch_groups(cmag_batch *b, bool force)
 {
     cudaStream_t st = b->stream;
     const BatchView base = view_of(b);
     const size_t ng = b->groups.size();
-    if (ng > 1) CB_CUDA(b, cudaEventRecord(b->fork, st));
-    for (size_t g = 0; g < ng; ++g) {
-        LaunchGroup &lg = b->groups[g];
-        cudaStream_t gs = (g == 0) ? st : lg.side;
-        if (g > 0) CB_CUDA(b, cudaStreamWaitEvent(gs, b->fork, 0));
+    auto same_variant = [&](const LaunchGroup &a, const LaunchGroup &c) {
+        return a.system == c.system && a.planar == c.planar && a.trim == c.trim && a.lists == c.lists &&
+               (force ? a.g_force == c.g_force : a.g_density == c.g_density) && a.first + a.count == c.first;
+    };
+    std::vector<std::pair<size_t, size_t>> runs;  // [first group, end group)
+    for (size_t g = 0; g < ng;) {
+        size_t e = g + 1;
+        while (e < ng && same_variant(b->groups[e - 1], b->groups[e])) ++e;
+        runs.emplace_back(g, e);
+        g = e;
+    }
+    if (runs.size() > 1) CB_CUDA(b, cudaEventRecord(b->fork, st));
+    for (size_t r = 0; r < runs.size(); ++r) {
+        LaunchGroup &lg = b->groups[runs[r].first];
+        const LaunchGroup &last = b->groups[runs[r].second - 1];
+        cudaStream_t gs = (r == 0) ? st : lg.side;
+        if (r > 0) CB_CUDA(b, cudaStreamWaitEvent(gs, b->fork, 0));
         BatchView v = base;
         v.first = lg.first;
-        v.count = lg.count;
+        v.count = last.first + last.count - lg.first;
         const DevParams &rep = b->host_dev[lg.slot_first];
         const NeighborList nl = lg.lists ? lists_of(b) : NeighborList{};
         if (force) {
@@ -266,7 +281,7 @@ int launch_groups(cmag_batch *b, bool force)
         } else {
             launch_density(rep, v, lg.g_density, b->spos, b->off, b->meas, b->aux, nl, gs);
         }
-        if (g > 0) {
+        if (r > 0) {
             CB_CUDA(b, cudaEventRecord(lg.done, gs));
             CB_CUDA(b, cudaStreamWaitEvent(st, lg.done, 0));
         }

@@ -55,7 +55,7 @@ def test_poiseuille_profile_matches_analytic_series(harness, tmp_path):
         exact = poiseuille_series(y, t)
         errs[t] = float(np.abs(u - exact).max() / np.abs(exact).max())
     print("max |u - series| / max|series| per time:", errs)
-    assert all(e < 0.05 for e in errs.values()), errs
+    assert all(e < 0.02 for e in errs.values()), errs
 
 
 def test_dambreak_front_and_height(harness, tmp_path):
