@@ -940,6 +940,9 @@ def main():
                       "restatement of the reference kernels, all host threads)" % (args.cpu_steps, n))
         line["cpu_baseline"] = {"value": v, "unit": "particle-updates/s", "cores": threads,
                                 "kind": "port", "seconds": dt, "sample": sample}
+        if not batched:
+            v1, dt1 = cpu_run(args.workload, 1, 1)
+            line["cpu_baseline"]["one_core"] = {"value": v1, "seconds": dt1, "sample": "1 full step, 1 thread"}
     if not batched and args.workload == "dambreak3d" and rank == 0 and world == 1 and not args.no_ref_gpu:
         line["reference_gpu"] = reference_gpu_bar()
         bar = line["reference_gpu"].get("dambreak3d_954860_reference_loops")

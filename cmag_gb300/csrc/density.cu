@@ -33,12 +33,17 @@ using walk::records;
 using walk::rel;
 using walk::shift_code;
 
+// Interaction lists the density pass records (template LIST): 0 none, 1 the
+// force's exact pair set of this step, 2 lists kept over several steps (every
+// particle within 2h + skin, for density and force).
+constexpr int kNoList = 0, kStepList = 1, kKeptList = 2;
+
 // Un-normalised Wendland sum over candidates [b, e) of one run, two candidates
 // per step in paired FP32 (FFMA2/FMUL2/FADD2: two FP32 operations per issued
 // instruction on sm_100+), scalar tail.  Adds max(1 - q/2, 0)^4 (2q + 1): zero
 // outside the support without a compare and select (the loop is bound by the
 // integer/compare pipe, not by FP32).
-template <int SYS, bool PLANAR, bool TRIM, bool LIST>
+template <int SYS, bool PLANAR, bool TRIM, int LIST>
 __device__ __forceinline__ void wendland_run(const DevParams &p, const float4 *__restrict__ spos,
                                              uint32_t b, uint32_t e, float4 pi, float sx, float sy,
                                              float sz, float2 &acc, bool record, uint32_t i,
@@ -74,8 +79,8 @@ __device__ __forceinline__ void wendland_run(const DevParams &p, const float4 *_
         acc = __fadd2_rn(acc, w);
         if (LIST && record) {
             const uint32_t v = j | code;  // j + 1 < 2^26: the next entry is v + 1
-            if (records<SYS, TRIM>(p, i, j, d2.x, a.w)) list_append(nl, i, cnt, v);
-            if (records<SYS, TRIM>(p, i, j + 1, d2.y, c.w)) list_append(nl, i, cnt, v + 1u);
+            if (records<SYS, TRIM, LIST == kKeptList>(p, i, j, d2.x, a.w)) list_append(nl, i, cnt, v);
+            if (records<SYS, TRIM, LIST == kKeptList>(p, i, j + 1, d2.y, c.w)) list_append(nl, i, cnt, v + 1u);
         }
     }
     if (j < e) {  // the same operations as one half of a pair step
@@ -87,7 +92,8 @@ __device__ __forceinline__ void wendland_run(const DevParams &p, const float4 *_
         const float t = fmaxf(__fmaf_rn(d, -0.5f * p.inv_h, 1.0f), 0.0f), t2 = __fmul_rn(t, t);
         const float w = __fmul_rn(__fmul_rn(t2, t2), __fmaf_rn(d, 2.0f * p.inv_h, 1.0f));
         acc.x = __fadd_rn(acc.x, w);
-        if (LIST && record && records<SYS, TRIM>(p, i, j, d2, pj.w)) list_append(nl, i, cnt, j | code);
+        if (LIST && record && records<SYS, TRIM, LIST == kKeptList>(p, i, j, d2, pj.w))
+            list_append(nl, i, cnt, j | code);
     }
 }
 
@@ -95,7 +101,7 @@ __device__ __forceinline__ void wendland_run(const DevParams &p, const float4 *_
 // 256 threads; planar scenes (single or batched) and single 3-D DamBreak scenes
 // 8 blocks per SM (32 registers: the batch and 3-D variants spill a few words to
 // L1 and still run faster than at 6 blocks), the rest 6
-template <int SYS, bool PLANAR, bool TRIM, int G, bool BATCH, bool LIST>
+template <int SYS, bool PLANAR, bool TRIM, int G, bool BATCH, int LIST>
 __global__ void __launch_bounds__(256, (PLANAR || (!BATCH && SYS == CMAG_DAMBREAK)) ? 8 : 6)
     k_density(DevParams pv, BatchView bv, const float4 *__restrict__ spos,
               const uint32_t *__restrict__ off_all, float4 *__restrict__ meas,
@@ -114,7 +120,7 @@ __global__ void __launch_bounds__(256, (PLANAR || (!BATCH && SYS == CMAG_DAMBREA
     const bool pinned = SYS == CMAG_POISEUILLE && pi.w == 1.0f;
     // lists for every particle whose force is computed (DamBreak: fluid only);
     // lists kept over several steps serve the density too: every particle
-    const bool record = LIST && active && (p.verlet || SYS != CMAG_DAMBREAK || pi.w == (float)CMAG_FLUID);
+    const bool record = LIST && active && (LIST == kKeptList || SYS != CMAG_DAMBREAK || pi.w == (float)CMAG_FLUID);
     uint32_t cnt = 0;
     float sum = 0.0f;
     if (active && (!pinned || record)) {  // a pinned wall walks only to record its list
@@ -137,7 +143,7 @@ __global__ void __launch_bounds__(256, (PLANAR || (!BATCH && SYS == CMAG_DAMBREA
                     // evaluated for every candidate and selected: no divergent branch
                     const float w = kernel_w(p, fminf(d2 * rsqrtf(fmaxf(d2, 1e-30f)) * p.inv_h, 2.0f));
                     sum += (d2 < p.support2) ? w : 0.0f;
-                    if (LIST && record && records<SYS, TRIM>(p, i, j, d2, pj.w))
+                    if (LIST && record && records<SYS, TRIM, LIST == kKeptList>(p, i, j, d2, pj.w))
                         list_append(nl, i, cnt, j | shift_code(sx, sy, sz));
                 });
         }
@@ -162,7 +168,7 @@ __global__ void __launch_bounds__(256, (PLANAR || (!BATCH && SYS == CMAG_DAMBREA
     }
 }
 
-template <int SYS, bool PLANAR, bool TRIM, int G, bool LIST>
+template <int SYS, bool PLANAR, bool TRIM, int G, int LIST>
 void launch_d(const DevParams &p, const BatchView &bv, const float4 *spos, const uint32_t *off,
               float4 *meas, float2 *aux, const NeighborList &nl, cudaStream_t st)
 {
@@ -179,13 +185,14 @@ void dispatch_g(int group, const DevParams &p, const BatchView &bv, const float4
                 const uint32_t *off, float4 *meas, float2 *aux, const NeighborList &nl, cudaStream_t st)
 {
     if (nl.entry) {  // lists: one lane per particle
-        launch_d<SYS, PLANAR, TRIM, 1, true>(p, bv, spos, off, meas, aux, nl, st);
+        if (p.verlet) launch_d<SYS, PLANAR, TRIM, 1, kKeptList>(p, bv, spos, off, meas, aux, nl, st);
+        else launch_d<SYS, PLANAR, TRIM, 1, kStepList>(p, bv, spos, off, meas, aux, nl, st);
         return;
     }
     switch (group) {
-    case 2: launch_d<SYS, PLANAR, TRIM, 2, false>(p, bv, spos, off, meas, aux, nl, st); break;
-    case 4: launch_d<SYS, PLANAR, TRIM, 4, false>(p, bv, spos, off, meas, aux, nl, st); break;
-    default: launch_d<SYS, PLANAR, TRIM, 1, false>(p, bv, spos, off, meas, aux, nl, st); break;
+    case 2: launch_d<SYS, PLANAR, TRIM, 2, kNoList>(p, bv, spos, off, meas, aux, nl, st); break;
+    case 4: launch_d<SYS, PLANAR, TRIM, 4, kNoList>(p, bv, spos, off, meas, aux, nl, st); break;
+    default: launch_d<SYS, PLANAR, TRIM, 1, kNoList>(p, bv, spos, off, meas, aux, nl, st); break;
     }
 }
 

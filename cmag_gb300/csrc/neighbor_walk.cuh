@@ -220,10 +220,10 @@ __device__ __forceinline__ void list_append(const NeighborList &nl, uint32_t i, 
 // the force's exact pair set (interacts) for per-step lists; for lists kept over
 // several steps every other particle closer than 2h + skin, coincident ones
 // included (the density sums them).
-template <int SYS, bool TRIM>
+template <int SYS, bool TRIM, bool KEEP>
 __device__ __forceinline__ bool records(const DevParams &p, uint32_t i, uint32_t j, float d2, float w)
 {
-    if (p.verlet) return j != i && d2 < p.list_r2;
+    if (KEEP) return j != i && d2 < p.list_r2;
     return interacts<SYS, TRIM>(p, d2, w);
 }
 

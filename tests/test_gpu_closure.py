@@ -191,3 +191,39 @@ def test_trained_closure_gains_over_plain_coarse(gpu):
           "coarse+closure", np.round(f_closure, 3))
     assert np.isfinite(f_closure).all()
     pair.close()
+
+
+def test_shipped_closure_improves_held_out_front(gpu):
+    """A posteriori, on the benchmark's own coarse dam break: the closure shipped in
+    cmag_gb300/data (trained by cmag_gb300/train_closure.py on seeds 2001-2020,
+    strength chosen on seed 998) brings the coarse run's surge front closer to the
+    plain fine run's on the held-out seed 1973 than the plain coarse method does
+    (mean relative error while the surge crosses the tank), and the coarse run with
+    it still takes less device time than the fine run."""
+    import os
+    from cmag_gb300 import train_closure as TC
+    if not os.path.exists(TC.DEFAULT_OUT):
+        pytest.fail("no trained closure at %s" % TC.DEFAULT_OUT)
+    c, rec = TC.load()
+    assert rec["strength"] > 0.0 and 1973 not in rec["train_seeds"] and rec["validation_seed"] != 1973
+    pair = Pair()
+    width, t_end = TC.COLUMN_WIDTH, 0.45
+    tank_over_column = pair.tank_f[0] / pair.fluid_f[0]
+    pair.start(1973)
+    t_fine, _, f_fine = rollout(pair.fine, t_end, 0.01, width)
+    pair.start(1973)
+    _, _, f_plain = rollout(pair.coarse, t_end, 0.01, width)
+    pair.start(1973)
+    pair.coarse.set_closure(c)
+    t_closure, _, f_closure = rollout(pair.coarse, t_end, 0.01, width)
+    pair.coarse.set_closure(None)
+    judged = f_fine < 0.95 * tank_over_column
+    e_plain = np.abs(f_plain - f_fine)[judged] / f_fine[judged]
+    e_closure = np.abs(f_closure - f_fine)[judged] / f_fine[judged]
+    print("held-out front error (mean, max): plain coarse %.4f %.4f, with closure %.4f %.4f; "
+          "device s: fine %.2f, coarse + closure %.2f"
+          % (e_plain.mean(), e_plain.max(), e_closure.mean(), e_closure.max(), t_fine, t_closure))
+    assert e_closure.mean() < e_plain.mean()
+    assert t_closure < t_fine
+    pair.close()
+    c.close()

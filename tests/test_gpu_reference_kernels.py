@@ -79,20 +79,24 @@ def test_library_equals_reference_kernels_one_step(gpu, num):
     err = np.abs(got["acc"][fluid, :3].astype(np.float64) - ref_acc[fluid, :3])
     worst = float((err / (sa[fluid, :3] + 1e-30)).max())
     assert worst <= 2 * TOL_TERM, "accelerations differ from the reference kernels by %g of the scale" % worst
+    # positions after the step: the acceleration differences above times dt^2,
+    # i.e. a few ulp of the coordinates
     ref_pos = ref.get(cm.POSITION)
     fin = np.isfinite(ref_pos).all(axis=1)
-    pos_err = np.abs(got["pos"][fin, :3] - ref_pos[fin, :3]).max() / (2.0 * float(p.particle_radius))
-    print("num=%d: |drho|/rho %.2e, acc %.2e of scale, |dx|/dx %.2e, reference NaN rows %d"
-          % (num, drho, worst, pos_err, nan_rows))
-    assert pos_err < 1e-5
+    dpos = np.abs(got["pos"][fin, :3].astype(np.float64) - ref_pos[fin, :3])
+    ulps = float((dpos / (np.spacing(np.abs(ref_pos[fin, :3])).astype(np.float64) + 1e-30)).max())
+    print("num=%d: |drho|/rho %.2e, acc %.2e of scale, position %.1f ulp, reference NaN rows %d"
+          % (num, drho, worst, ulps, nan_rows))
+    assert ulps <= 4.0
     ref.close()
     s.close()
 
 
 def test_dambreak_front_follows_the_reference_kernels(gpu):
-    """XFrontTest's quantity (the surge front, XFrontTest.h:64-86) on the reference's
-    own 2-D dam break (a 64 x 128 column released at t = 0), the library against the
-    reference's kernels step for step on the GPU: the fronts agree within 1 % of
+    """XFrontTest's quantity (the surge front, XFrontTest.h:64-86: the largest fluid x,
+    here in column widths from the world origin) on the reference's own 2-D dam
+    break (a 64 x 128 column released at t = 0), the library against the
+    reference's kernels run side by side on the GPU: the fronts agree within 1 % of
     the column width while the surge crosses the tank (the two runs round
     differently, so they drift apart only through the flow's own sensitivity)."""
     if not RG.available():
@@ -113,7 +117,7 @@ def test_dambreak_front_follows_the_reference_kernels(gpu):
     fronts = np.array(fronts)
     dev = np.abs(fronts[:, 0] - fronts[:, 1])
     print("fronts (library, reference kernels) every 0.01 s:", np.round(fronts, 3).tolist())
-    assert fronts[-1, 0] > 1.5, "the surge did not advance"
+    assert fronts[-1, 0] - fronts[0, 0] > 1.5, "the surge did not advance"
     assert dev.max() < 0.01, "fronts differ by %.3f column widths" % dev.max()
     ref.close()
     s.close()
