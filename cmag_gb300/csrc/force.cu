@@ -245,11 +245,14 @@ __global__ void __launch_bounds__(256, SYS == CMAG_PERISTALSIS ? (PLANAR ? 5 : 4
             const float2 vxy = __ffma2_rn(dvy, ry, __fmul2_rn(dvx, rx));
             const float2 vij = PLANAR ? vxy
                                       : __ffma2_rn(__fadd2_rn(make_float2(vi.z, vi.z), make_float2(-v0.z, -v1.z)), rz, vxy);
-            if (vij.x < 0.0f && !w0) {
-                sp.x -= __fdividef(p.av_coeff * vij.x, (ai.y + a0.y) * (d2.x + p.av_eps2));
-            }
-            if (vij.y < 0.0f && !w1) {
-                sp.y -= __fdividef(p.av_coeff * vij.y, (ai.y + a1.y) * (d2.y + p.av_eps2));
+            {
+                // Monaghan viscosity of approaching fluid pairs, evaluated for both and
+                // selected (no divergent branch; the selected values are the scalar
+                // pair's)
+                const float av0 = __fdividef(p.av_coeff * vij.x, (ai.y + a0.y) * (d2.x + p.av_eps2));
+                const float av1 = __fdividef(p.av_coeff * vij.y, (ai.y + a1.y) * (d2.y + p.av_eps2));
+                sp.x = (vij.x < 0.0f && !w0) ? sp.x - av0 : sp.x;
+                sp.y = (vij.y < 0.0f && !w1) ? sp.y - av1 : sp.y;
             }
             sp = __fmul2_rn(sp, __fmul2_rn(make_float2(nmass, nmass), g));
             const float s0 = w0 ? (in0 ? slj.x : 0.0f) : sp.x, s1 = w1 ? (in1 ? slj.y : 0.0f) : sp.y;
