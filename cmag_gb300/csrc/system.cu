@@ -22,6 +22,9 @@
 
 using namespace cmag;
 
+// arrays moved by one cmag_system_set_arrays / get_arrays call at most
+constexpr uint32_t kMaxArraysPerCall = 8;
+
 struct cmag_system {
     cmag_sph_params p{};
     uint32_t n = 0;
@@ -40,7 +43,7 @@ struct cmag_system {
     uint32_t *ws = nullptr;  // cell scan: per-tile counts and their prefixes
     size_t ws_words = 0;
     uint32_t *err = nullptr;
-    uint32_t *zflag = nullptr;  // set_array: whether uploaded z components differ
+    uint32_t *zflag = nullptr;  // set_array(s): whether uploaded z components differ (one word per array)
     PhaseState *phase = nullptr;
     uint32_t *view_cs = nullptr, *view_ce = nullptr;
     uint32_t *red = nullptr;  // reduction results: 6 extent keys, pad, 4 doubles, 1 count
@@ -904,7 +907,7 @@ int cmag_system_create(const cmag_sph_params *params, uint32_t n, cmag_system **
     step(dalloc(s, &s->phase, sizeof(PhaseState)));
     // 6 extent keys + pad (32 B), 4 doubles (32 B), 1 count (8 B)
     step(dalloc(s, &s->red, 128));
-    step(dalloc(s, &s->zflag, sizeof(uint32_t)));
+    step(dalloc(s, &s->zflag, kMaxArraysPerCall * sizeof(uint32_t)));
     if (rc != CMAG_OK) {
         std::string msg = s->last_error;
         free_all(s);
@@ -974,6 +977,69 @@ int cmag_system_set_array(cmag_system *s, int32_t array, const float *host, uint
                             st_of(s));
         CM_CUDA(s, cudaGetLastError());
     }
+    return CMAG_OK;
+}
+
+int cmag_system_set_arrays(cmag_system *s, uint32_t count, const int32_t *arrays, const float *const *host)
+{
+    if (!s || (count && (!arrays || !host))) return fail(s, CMAG_ERR_INVALID, "null argument");
+    if (count > kMaxArraysPerCall) return fail(s, CMAG_ERR_INVALID, "at most 8 arrays per call");
+    float4 *d[kMaxArraysPerCall];
+    for (uint32_t k = 0; k < count; ++k) {
+        d[k] = float_array(s, arrays[k]);
+        if (!d[k] || !host[k]) return fail(s, CMAG_ERR_INVALID, "not a settable float4 array: " + std::to_string(arrays[k]));
+    }
+    if (s->n == 0) return CMAG_OK;
+    for (uint32_t k = 0; k < count; ++k)
+        CM_CUDA(s, cudaMemcpyAsync(d[k], host[k], sizeof(float4) * (size_t)s->n, cudaMemcpyHostToDevice, st_of(s)));
+    // the z checks of set_array, one flag word per array, read back together
+    uint32_t differs[kMaxArraysPerCall] = {};
+    bool checked = false;
+    for (uint32_t k = 0; k < count; ++k) {
+        const bool pos_up = arrays[k] == CMAG_POSITION;
+        const bool vel_up = arrays[k] == CMAG_VELOCITY || arrays[k] == CMAG_VELOCITYLEAPFROG;
+        if (s->p.dims == 2 && (pos_up || vel_up)) {
+            launch_z_differs(d[k], s->n, pos_up ? host[k][2] : 0.0f, s->zflag + k, st_of(s));
+            checked = true;
+        }
+    }
+    if (checked) {
+        CM_CUDA(s, cudaGetLastError());
+        CM_CUDA(s, cudaMemcpyAsync(differs, s->zflag, sizeof(uint32_t) * count, cudaMemcpyDeviceToHost, st_of(s)));
+    }
+    CM_CUDA(s, cudaStreamSynchronize(st_of(s)));
+    bool pos_any = false;
+    for (uint32_t k = 0; k < count; ++k) {
+        const int32_t a = arrays[k];
+        if (s->p.dims != 2) {
+            s->z_uniform = false;
+        } else if (a == CMAG_POSITION) {
+            s->z_uniform = !differs[k];
+            s->z_value = host[k][2];
+        } else if (a == CMAG_VELOCITY || a == CMAG_VELOCITYLEAPFROG) {
+            if (differs[k]) s->vz_nonzero = true;
+            else if (a == CMAG_VELOCITY) s->vz_nonzero = false;
+        }
+        pos_any = pos_any || a == CMAG_POSITION;
+    }
+    refresh_layout(s);
+    if (pos_any && verlet_on(s)) {
+        launch_verlet_check(s->pos, s->vl_xb, 0, s->n, make_dev(s).vl_move2, &s->vl_flags->moved, st_of(s));
+        CM_CUDA(s, cudaGetLastError());
+    }
+    return CMAG_OK;
+}
+
+int cmag_system_get_arrays(cmag_system *s, uint32_t count, const int32_t *arrays, float *const *host)
+{
+    if (!s || (count && (!arrays || !host))) return fail(s, CMAG_ERR_INVALID, "null argument");
+    if (count > kMaxArraysPerCall) return fail(s, CMAG_ERR_INVALID, "at most 8 arrays per call");
+    for (uint32_t k = 0; k < count; ++k) {
+        float4 *d = float_array(s, arrays[k]);
+        if (!d || !host[k]) return fail(s, CMAG_ERR_INVALID, "not a float4 array: " + std::to_string(arrays[k]));
+        CM_CUDA(s, cudaMemcpyAsync(host[k], d, sizeof(float4) * (size_t)s->n, cudaMemcpyDeviceToHost, st_of(s)));
+    }
+    CM_CUDA(s, cudaStreamSynchronize(st_of(s)));
     return CMAG_OK;
 }
 

@@ -110,6 +110,35 @@ class _System:
         self._chk(lib().cmag_system_get_array(self._h, int(array), _fp(out), int(start), count))
         return out
 
+    def setArrays(self, arrays):
+        """Whole float4 arrays {array id: (n, 4) float32} in one call (one
+        synchronisation)."""
+        ids = list(arrays)
+        data = [np.ascontiguousarray(arrays[a], dtype=np.float32).reshape(-1, 4) for a in ids]
+        for a in data:
+            if a.shape[0] != self.numParticles:
+                raise ValueError("setArrays takes whole arrays of %d rows" % self.numParticles)
+        ids_c = (ctypes.c_int32 * len(ids))(*ids)
+        ptrs = (c_f32p * len(ids))(*[_fp(a) for a in data])
+        self._chk(lib().cmag_system_set_arrays(self._h, len(ids), ids_c, ptrs))
+
+    def getArrays(self, arrays):
+        """Whole float4 arrays in one call: {array id: out} with `out` None or a
+        C-contiguous float32 (n, 4) array (e.g. pinned memory); returns the dict
+        of filled arrays."""
+        out = {}
+        for a, buf in arrays.items():
+            if buf is None:
+                buf = np.empty((self.numParticles, 4), np.float32)
+            elif buf.dtype != np.float32 or buf.shape != (self.numParticles, 4) or not buf.flags.c_contiguous:
+                raise ValueError("out must be a C-contiguous float32 array of shape (%d, 4)" % self.numParticles)
+            out[a] = buf
+        ids = list(out)
+        ids_c = (ctypes.c_int32 * len(ids))(*ids)
+        ptrs = (c_f32p * len(ids))(*[_fp(out[a]) for a in ids])
+        self._chk(lib().cmag_system_get_arrays(self._h, len(ids), ids_c, ptrs))
+        return out
+
     def getUintArray(self, array, start=0, count=None):
         if count is None:
             if array in (_abi.CELLSTART, _abi.CELLEND):

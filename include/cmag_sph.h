@@ -257,6 +257,12 @@ int cmag_system_get_array(cmag_system *s, int32_t array, float *host, uint32_t s
                           uint32_t count);
 int cmag_system_get_uint_array(cmag_system *s, int32_t array, uint32_t *host, uint32_t start,
                                uint32_t count);
+/* Several whole float4 arrays (num_particles x 4 floats each) in one call: host[k]
+ * is array arrays[k]; one copy per array and one synchronisation for all (at most
+ * 8 arrays).  No reference counterpart (its setArray moves one array per call,
+ * fluidSystem.cpp:321-355, and reading goes through getCuda* pointers). */
+int cmag_system_set_arrays(cmag_system *s, uint32_t count, const int32_t *arrays, const float *const *host);
+int cmag_system_get_arrays(cmag_system *s, uint32_t count, const int32_t *arrays, float *const *host);
 /* Borrowed device pointer of an array (getCudaPosVBO, getCudaMeasures, ...);
  * valid until destroy.  NULL for unknown arrays. */
 void *cmag_system_device_array(cmag_system *s, int32_t array);

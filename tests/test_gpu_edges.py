@@ -167,3 +167,40 @@ def test_tiny_scenes(gpu, n):
     g, pre, nxt = _one_step(s, ref)
     print(n, compare_step(g, pre, nxt, label="n=%d: " % n))
     s.close()
+
+
+def test_multi_array_transfer_equals_single_arrays(gpu):
+    """setArrays / getArrays (one synchronisation for several arrays) leave the
+    solver in the state the per-array calls leave: the same trajectory bit for
+    bit, and a z velocity uploaded with the positions still switches a 2-D scene
+    off its single-layer search."""
+    a, _ = _dambreak()
+    b, _ = _dambreak()
+    for s in (a, b):
+        s.removeRightBoundary()
+        s.update_n(20)
+    ids = (cm.POSITION, cm.VELOCITY, cm.VELOCITYLEAPFROG)
+    host = {k: a.getArray(k) for k in ids}
+    got = b.getArrays({k: None for k in ids})
+    for k in ids:
+        assert np.array_equal(got[k].view(np.uint32), host[k].view(np.uint32))
+    # a small z velocity on one fluid particle: both must take the 3-D walk
+    host[cm.VELOCITY][5, 2] = 1e-3
+    for k in ids:
+        a.setArray(k, host[k])
+    b.setArrays(host)
+    for s in (a, b):
+        s.update()
+    # the 3-D walk scans the whole grid: its dense cell offsets cover every cell
+    # (a single-layer scan window holds one z layer of them)
+    for s in (a, b):
+        assert len(s.getUintArray(_abi.CELLOFFSET, count=s.numGridCells + 1)) == s.numGridCells + 1
+    for s in (a, b):
+        s.update_n(4)
+    got = b.getArrays({k: None for k in ids})
+    for k in ids:
+        assert np.array_equal(got[k].view(np.uint32), a.getArray(k).view(np.uint32)), k
+    with pytest.raises(Exception):
+        b.setArrays({cm.POSITION: host[cm.POSITION][:-1]})
+    a.close()
+    b.close()
