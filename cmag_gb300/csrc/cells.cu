@@ -60,6 +60,7 @@ __global__ void __launch_bounds__(256)
     hash[i] = BATCH ? slot : p.scan_base + rel;  // = hr inside the table
     const uint32_t r = atomicAdd(cnt + slot, 1u);
     if (rank) rank[i] = r;
+    if (!BATCH && p.wc_mark) wall_cache_note(p, i, q, g);
 }
 
 // The 16 counts of cells [first, first + 16) (zeros past m).
@@ -109,9 +110,20 @@ __global__ void __launch_bounds__(kScanThreads)
 // Scan, step 2: exclusive scan of the tile counts in place, by one block: each
 // thread sums a contiguous chunk of tiles, the block scans the chunk sums, and
 // each thread rewrites its chunk from its offset.
-__global__ void __launch_bounds__(1024) k_tile_prefix(uint32_t *__restrict__ tot, uint32_t tiles)
+// wc_state (a single scene's wall density cache, or null): the step stamp
+// advances, and a new epoch starts when the hash pass saw a non-fluid particle
+// move (the hash pass has completed; the density pass follows).
+__global__ void __launch_bounds__(1024) k_tile_prefix(uint32_t *__restrict__ tot, uint32_t tiles,
+                                                      uint32_t *__restrict__ wc_state)
 {
     pdl_entry();
+    if (wc_state && threadIdx.x == 0) {
+        wc_state[kWcStamp] += 1u;
+        if (wc_state[kWcMoved]) {
+            wc_state[kWcEpoch] += 1u;
+            wc_state[kWcMoved] = 0u;
+        }
+    }
     __shared__ uint32_t s_warp[32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t per = (tiles + blockDim.x - 1) / blockDim.x;
@@ -293,12 +305,13 @@ void launch_cell_sort(const uint32_t *hash, const uint32_t *rank, const uint32_t
 
 size_t cell_scan_workspace_words(uint32_t m) { return (m + kScanTile - 1) / kScanTile; }
 
-void launch_cell_scan(uint32_t *cnt, uint32_t *off, uint32_t m, uint32_t *ws, cudaStream_t st)
+void launch_cell_scan(uint32_t *cnt, uint32_t *off, uint32_t m, uint32_t *ws, cudaStream_t st,
+                      uint32_t *wc_state)
 {
     const uint32_t tiles = (m + kScanTile - 1) / kScanTile;
     if (tiles == 0) return;
     launch_pdl(k_tile_sum, tiles, kScanThreads, 0, st, cnt, m, ws);
-    launch_pdl(k_tile_prefix, 1, 1024, 0, st, ws, tiles);
+    launch_pdl(k_tile_prefix, 1, 1024, 0, st, ws, tiles, wc_state);
     launch_pdl(k_cell_offsets, tiles, kScanThreads, 0, st, cnt, off, m, ws);
 }
 

@@ -121,9 +121,28 @@ __global__ void __launch_bounds__(256, (PLANAR || (!BATCH && SYS == CMAG_DAMBREA
     // lists for every particle whose force is computed (DamBreak: fluid only);
     // lists kept over several steps serve the density too: every particle
     const bool record = LIST && active && (LIST == kKeptList || SYS != CMAG_DAMBREAK || pi.w == (float)CMAG_FLUID);
+    // A single DamBreak scene's non-fluid particle with no fluid particle in its
+    // cell box: its walk would visit non-fluid particles only, which have not
+    // moved since the epoch began, in the same runs and order, so its sum has the
+    // bits of the walk of any step of the epoch.  wc: 0 walk as usual, 1 walk and
+    // keep the result, 2 take the kept result.
+    constexpr bool WC = SYS == CMAG_DAMBREAK && !BATCH && LIST != kKeptList;
+    uint32_t wc = 0;
+    if (WC && p.wc_entry && active && pi.w != (float)CMAG_FLUID &&
+        !walk::fluid_near(p, grid_pos(p, pi.x, pi.y, pi.z))) {
+        const float4 e = p.wc_entry[p.wc_idx[i]];
+        wc = __float_as_uint(e.z) == p.wc_state[kWcEpoch] ? 2u : 1u;
+        if (G == 1 && wc == 2u) {  // (lanes of a group leave together only at G = 1)
+            meas[i] = make_float4(e.x, e.y, 0.0f, 0.0f);
+            const float inv_rho = 1.0f / e.x;
+            aux[i] = make_float2(e.y * inv_rho * inv_rho, e.x);
+            if (LIST) nl.count[i] = 0;
+            return;
+        }
+    }
     uint32_t cnt = 0;
     float sum = 0.0f;
-    if (active && (!pinned || record)) {  // a pinned wall walks only to record its list
+    if (active && (!pinned || record) && wc != 2u) {  // a pinned wall walks only to record its list
         const int3 g = grid_pos(p, pi.x, pi.y, pi.z);
         if (p.kernel == CMAG_KERNEL_WENDLAND) {
             float2 acc = make_float2(0.0f, 0.0f);
@@ -158,6 +177,10 @@ __global__ void __launch_bounds__(256, (PLANAR || (!BATCH && SYS == CMAG_DAMBREA
         if (pinned) {
             rho = p.rho0;
             pr = p.p_wall;
+        } else if (WC && wc == 2u) {
+            const float4 e = p.wc_entry[p.wc_idx[i]];
+            rho = e.x;
+            pr = e.y;
         } else {
             rho = sum * p.mass;
             pr = eos_pressure(p, rho);
@@ -165,6 +188,8 @@ __global__ void __launch_bounds__(256, (PLANAR || (!BATCH && SYS == CMAG_DAMBREA
         meas[i] = make_float4(rho, pr, 0.0f, SYS == CMAG_PERISTALSIS ? pi.w : 0.0f);
         const float inv_rho = 1.0f / rho;
         aux[i] = make_float2(pr * inv_rho * inv_rho, SYS == CMAG_DAMBREAK ? rho : inv_rho);
+        if (WC && wc == 1u)
+            p.wc_entry[p.wc_idx[i]] = make_float4(rho, pr, __uint_as_float(p.wc_state[kWcEpoch]), 0.0f);
     }
 }
 

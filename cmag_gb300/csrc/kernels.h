@@ -99,7 +99,10 @@ void launch_cell_sort(const uint32_t *hash, const uint32_t *rank, const uint32_t
 // every tile from its prefix), clearing cnt for the next step.  ws must hold
 // cell_scan_workspace_words(m) words (no clearing needed).
 size_t cell_scan_workspace_words(uint32_t m);
-void launch_cell_scan(uint32_t *cnt, uint32_t *off, uint32_t m, uint32_t *ws, cudaStream_t st);
+// wc_state: a single scene's wall density cache state (DevParams::wc_state) or
+// null; its step stamp and epoch advance in the scan (after the hash pass).
+void launch_cell_scan(uint32_t *cnt, uint32_t *off, uint32_t m, uint32_t *ws, cudaStream_t st,
+                      uint32_t *wc_state = nullptr);
 // Reference cellStart/cellEnd view of the dense offsets.
 void launch_cell_view(const uint32_t *off, uint32_t scan_base, uint32_t scan_cells,
                       uint64_t ncells, uint32_t *cell_start, uint32_t *cell_end, cudaStream_t st);

@@ -37,6 +37,60 @@ __device__ __forceinline__ uint32_t wrap_axis(int v, uint32_t n)
     return (uint32_t)(m < 0 ? m + (int)n : m);
 }
 
+// Wall density cache, density side: whether a fluid particle was hashed this
+// step into any 4x4x4 block that holds a cell of the box of cells g - c .. g + c
+// (wrapped per axis like the walk's rows).  Per axis the box's cells are one
+// wrapped range, i.e. at most two ranges of blocks.
+struct BlockSpan {
+    uint32_t a0, a1, b0, b1;  // blocks [a0, a1] and [b0, b1] (b0 > b1: none)
+};
+
+__device__ __forceinline__ BlockSpan box_blocks(int v, int c, uint32_t n)
+{
+    BlockSpan r;
+    r.b0 = 1;
+    r.b1 = 0;
+    const uint32_t len = 2u * (uint32_t)c + 1u;
+    if (len >= n) {
+        r.a0 = 0;
+        r.a1 = (n - 1u) >> 2;
+        return r;
+    }
+    const uint32_t s = wrap_axis(v - c, n);
+    r.a0 = s >> 2;
+    if (s + len <= n) {
+        r.a1 = (s + len - 1u) >> 2;
+    } else {
+        r.a1 = (n - 1u) >> 2;
+        r.b0 = 0;
+        r.b1 = (s + len - 1u - n) >> 2;
+    }
+    return r;
+}
+
+__device__ __forceinline__ bool fluid_near(const DevParams &p, int3 g)
+{
+    const int c = p.cell_count;
+    const BlockSpan X = box_blocks(g.x, c, p.gx), Y = box_blocks(g.y, c, p.gy), Z = box_blocks(g.z, c, p.gz);
+    const uint32_t stamp = p.wc_state[kWcStamp];
+    for (int zs = 0; zs < 2; ++zs) {
+        const uint32_t z0 = zs ? Z.b0 : Z.a0, z1 = zs ? Z.b1 : Z.a1;
+        for (uint32_t z = z0; z <= z1; ++z)
+            for (int ys = 0; ys < 2; ++ys) {
+                const uint32_t y0 = ys ? Y.b0 : Y.a0, y1 = ys ? Y.b1 : Y.a1;
+                for (uint32_t y = y0; y <= y1; ++y) {
+                    const uint32_t *row = p.wc_mark + (z * p.wc_nby + y) * p.wc_nbx;
+                    for (int xs = 0; xs < 2; ++xs) {
+                        const uint32_t x0 = xs ? X.b0 : X.a0, x1 = xs ? X.b1 : X.a1;
+                        for (uint32_t x = x0; x <= x1; ++x)
+                            if (row[x] == stamp) return true;
+                    }
+                }
+            }
+    }
+    return false;
+}
+
 // The runs of one row of the cell box: [b0, e0) with x image shift sx0 and,
 // when the row wraps in x, [b1, e1) with sx1 (empty otherwise); sy, sz: the
 // row's image shifts.

@@ -62,7 +62,23 @@ struct DevParams {
     float list_r2;
     int32_t verlet;
     float vl_move2;  // (skin / 2)^2: a larger displacement since the rebuild forces the next one
+    // DamBreak, single scene: the density of a non-fluid particle with no fluid
+    // particle in its searched cell box depends only on the non-fluid particles,
+    // which stay put, so it is kept over steps (null: not kept).  Per particle in
+    // original order: wc_entry = (rho, p, epoch bits, 0) and wc_snap = the
+    // position it had at the last hash; per 4x4x4 block of cells: wc_mark = the
+    // stamp of the last step a fluid particle was hashed into it; wc_state = {step
+    // stamp, epoch, non-fluid particles moved}.
+    float4 *wc_entry;
+    float4 *wc_snap;
+    uint32_t *wc_mark;
+    uint32_t *wc_state;
+    const uint32_t *wc_idx;  // sorted -> original index
+    uint32_t wc_nbx, wc_nby, wc_nbz;
 };
+
+// wc_state words
+constexpr int kWcStamp = 0, kWcEpoch = 1, kWcMoved = 2;
 
 // Several independent scenes advanced by the same launches: the per-scene
 // parameter blocks and the scene of every particle.  Scene s owns particles
@@ -148,6 +164,27 @@ __device__ __forceinline__ uint32_t grid_hash(const DevParams &p, int gx, int gy
     const uint32_t x = wrap_cell(gx, p.gx, p.pow2_grid), y = wrap_cell(gy, p.gy, p.pow2_grid),
                    z = wrap_cell(gz, p.gz, p.pow2_grid);
     return (z * p.gy) * p.gx + y * p.gx + x;
+}
+
+// Wall density cache, hash side (DevParams::wc_*): a fluid particle stamps its
+// 4x4x4 cell block with this step's stamp; a non-fluid particle whose position
+// or type differs from its snapshot takes the new one and marks the cached
+// densities stale (the next scan kernel starts a new epoch).  g: the particle's
+// unwrapped cell.
+__device__ __forceinline__ void wall_cache_note(const DevParams &p, uint32_t i, float4 q, int3 g)
+{
+    if (q.w == (float)CMAG_FLUID) {
+        const uint32_t bx = wrap_cell(g.x, p.gx, p.pow2_grid) >> 2, by = wrap_cell(g.y, p.gy, p.pow2_grid) >> 2,
+                       bz = wrap_cell(g.z, p.gz, p.pow2_grid) >> 2;
+        p.wc_mark[(bz * p.wc_nby + by) * p.wc_nbx + bx] = p.wc_state[kWcStamp] + 1u;
+    } else {
+        const float4 s = p.wc_snap[i];
+        if (__float_as_uint(s.x) != __float_as_uint(q.x) || __float_as_uint(s.y) != __float_as_uint(q.y) ||
+            __float_as_uint(s.z) != __float_as_uint(q.z) || __float_as_uint(s.w) != __float_as_uint(q.w)) {
+            p.wc_snap[i] = q;
+            p.wc_state[kWcMoved] = 1u;
+        }
+    }
 }
 
 // EvaluateShift, PeristalsisUtil.cu:4-11

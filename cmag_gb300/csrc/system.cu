@@ -73,6 +73,12 @@ struct cmag_system {
     VerletFlags *vl_flags = nullptr;
     float4 *vl_xb = nullptr;
     cudaStream_t vl_side = nullptr;
+    // DamBreak: densities of non-fluid particles far from the fluid kept over
+    // steps (DevParams::wc_*); wc_on: in use (cmag_system_set_wall_cache)
+    float4 *wc_entry = nullptr, *wc_snap = nullptr;
+    uint32_t *wc_mark = nullptr, *wc_state = nullptr;
+    uint32_t wc_nb[3] = {0, 0, 0};
+    bool wc_on = false;
     cmag_closure *closure = nullptr;   // learned correction added after the force stage
     __nv_bfloat16 *closure_x = nullptr;  // its normalised input rows (n x 16)
 
@@ -306,8 +312,25 @@ DevParams make_dev(const cmag_system *s)
     if (verlet_on(s)) {
         const double half = 0.5 * s->vl_skin * 2.0 * s->p.particle_radius;
         d.vl_move2 = (float)(half * half);
+    } else if (s->wc_on && s->wc_entry) {
+        d.wc_entry = s->wc_entry;
+        d.wc_snap = s->wc_snap;
+        d.wc_mark = s->wc_mark;
+        d.wc_state = s->wc_state;
+        d.wc_idx = s->idx[0];  // the counting sort's sorted -> original index
+        d.wc_nbx = s->wc_nb[0];
+        d.wc_nby = s->wc_nb[1];
+        d.wc_nbz = s->wc_nb[2];
     }
     return d;
+}
+
+// The kept wall densities are stale: the next step's scan starts a new epoch.
+void wall_cache_reset(cmag_system *s)
+{
+    if (s->wc_state &&
+        cudaMemsetAsync(s->wc_state + kWcMoved, 0x01, sizeof(uint32_t), s->stream) != cudaSuccess)
+        (void)cudaGetLastError();
 }
 
 // Parameters of the rebuild's density walk: rows trimmed to, and lists recording,
@@ -373,12 +396,16 @@ int alloc_lists(cmag_system *s, uint32_t cap = 0)
     return CMAG_OK;
 }
 
+// Every change of parameters, lanes, lists or layout comes through here: the
+// captured step is re-recorded, kept lists are rebuilt and kept wall densities
+// recomputed.
 void invalidate_graph(cmag_system *s)
 {
     if (s->gexec) cudaGraphExecDestroy(s->gexec);
     s->gexec = nullptr;
     s->gvalid = false;
     verlet_force(s);
+    wall_cache_reset(s);
 }
 
 // Planar 2-D scenes search and scan only their own z layer (planar_allowed).
@@ -596,7 +623,7 @@ int record_step(cmag_system *s, int last, bool timed)
     // hash + per-cell counts (and each particle's arrival rank in its cell), dense
     // offsets, then the stable counting sort by cell
     launch_hash(d, BatchView{}, s->pos, s->hash[0], s->cnt, s->idx[0], s->err, st);
-    launch_cell_scan(s->cnt, s->off, s->scan_cells + 1, s->ws, st);
+    launch_cell_scan(s->cnt, s->off, s->scan_cells + 1, s->ws, st, d.wc_state);
     mark(1);
     if (last >= CMAG_STAGE_SORT)
         launch_cell_sort(s->hash[0], s->idx[0], s->off, s->scan_base, s->n, s->hash[1], s->idx[1],
@@ -731,7 +758,8 @@ void free_all(cmag_system *s)
     void *ptrs[] = {s->pos, s->vel, s->vlf, s->meas, s->acc, s->vforce, s->pforce, s->pred,
                     s->spos, s->svel, s->hash[0], s->hash[1], s->idx[0], s->idx[1], s->cnt,
                     s->off, s->aux, s->ws, s->err, s->phase, s->view_cs, s->view_ce, s->red,
-                    s->zflag, s->closure_x, s->vl_flags, s->vl_xb};
+                    s->zflag, s->closure_x, s->vl_flags, s->vl_xb, s->wc_entry, s->wc_snap,
+                    s->wc_mark, s->wc_state};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     free_lists(s);
@@ -908,6 +936,14 @@ int cmag_system_create(const cmag_sph_params *params, uint32_t n, cmag_system **
     // 6 extent keys + pad (32 B), 4 doubles (32 B), 1 count (8 B)
     step(dalloc(s, &s->red, 128));
     step(dalloc(s, &s->zflag, kMaxArraysPerCall * sizeof(uint32_t)));
+    if (params->system == CMAG_DAMBREAK) {
+        for (int a = 0; a < 3; ++a) s->wc_nb[a] = (params->grid_size[a] + 3u) / 4u;
+        step(dalloc(s, &s->wc_entry, f4));
+        step(dalloc(s, &s->wc_snap, f4));
+        step(dalloc(s, &s->wc_mark, sizeof(uint32_t) * (size_t)s->wc_nb[0] * s->wc_nb[1] * s->wc_nb[2]));
+        step(dalloc(s, &s->wc_state, 4 * sizeof(uint32_t)));
+        s->wc_on = true;
+    }
     if (rc != CMAG_OK) {
         std::string msg = s->last_error;
         free_all(s);
@@ -915,9 +951,19 @@ int cmag_system_create(const cmag_sph_params *params, uint32_t n, cmag_system **
         set_last_error(msg);
         return rc;
     }
+    // the clears above ran on the legacy stream, which the instance's
+    // non-blocking stream does not wait for
+    e = cudaStreamSynchronize(cudaStreamLegacy);
+    if (e != cudaSuccess) {
+        fail(nullptr, CMAG_ERR_CUDA, std::string("cudaStreamSynchronize: ") + cudaGetErrorString(e));
+        free_all(s);
+        delete s;
+        return CMAG_ERR_CUDA;
+    }
     s->host_phase.is_bc = params->is_boundary_configuration;
     s->host_phase.time_relax = 1000 * params->delta_time;
     upload_phase(s);
+    wall_cache_reset(s);
     refresh_layout(s);
     *out = s;
     return CMAG_OK;
@@ -1472,7 +1518,9 @@ int cmag_system_autotune(cmag_system *s, int32_t reps)
         s->host_phase = saved;
         if ((rc = upload_phase(s))) return rc;
     }
-    const DevParams d = make_dev(s);
+    DevParams d = make_dev(s);
+    // trials walk every particle (kept wall densities belong to one lane count)
+    d.wc_entry = nullptr;
     cudaStream_t st = st_of(s);
     cudaEvent_t a, b;
     CM_CUDA(s, cudaEventCreate(&a));
@@ -1586,6 +1634,24 @@ int cmag_system_get_verlet(cmag_system *s, float *skin, uint32_t *rebuilds)
         }
         *rebuilds = f.rebuilds;
     }
+    return CMAG_OK;
+}
+
+int cmag_system_set_wall_cache(cmag_system *s, int32_t enable)
+{
+    if (!s) return fail(nullptr, CMAG_ERR_INVALID, "null handle");
+    if (enable && !s->wc_entry) return fail(s, CMAG_ERR_STATE, "wall densities are kept for dam-break systems only");
+    if ((enable != 0) != s->wc_on) {
+        s->wc_on = enable != 0;
+        invalidate_graph(s);
+    }
+    return CMAG_OK;
+}
+
+int cmag_system_get_wall_cache(const cmag_system *s, int32_t *enabled)
+{
+    if (!s || !enabled) return fail(nullptr, CMAG_ERR_INVALID, "null argument");
+    *enabled = s->wc_on ? 1 : 0;
     return CMAG_OK;
 }
 

@@ -267,6 +267,16 @@ class _System:
         self._chk(lib().cmag_system_get_neighbor_lists(self._h, ctypes.byref(e), ctypes.byref(c)))
         return bool(e.value), c.value
 
+    def set_wall_cache(self, enable):
+        """DamBreak: keep the densities of non-fluid particles far from the fluid
+        over steps (on by default; the results are the same bits either way)."""
+        self._chk(lib().cmag_system_set_wall_cache(self._h, int(bool(enable))))
+
+    def wall_cache(self):
+        e = ctypes.c_int32()
+        self._chk(lib().cmag_system_get_wall_cache(self._h, ctypes.byref(e)))
+        return bool(e.value)
+
     def set_stage_timing(self, enable):
         self._chk(lib().cmag_system_set_stage_timing(self._h, int(bool(enable))))
 

@@ -322,6 +322,15 @@ int cmag_system_get_groups(const cmag_system *s, int32_t *density_lanes, int32_t
  * a particle with more neighbours walks the cells).  Fewer than 2^26 particles. */
 int cmag_system_set_neighbor_lists(cmag_system *s, int32_t enable);
 int cmag_system_get_neighbor_lists(const cmag_system *s, int32_t *enabled, uint32_t *cap);
+/* DamBreak systems: the density of a non-fluid particle with no fluid particle in
+ * its searched cell box is kept over steps and reused (its walk would visit the
+ * same non-fluid particles in the same order, so the reused value has the bits
+ * the walk would give).  A non-fluid particle that moves or changes type, and any
+ * change of parameters, lanes or lists, starts over.  On by default for DamBreak
+ * (memory: num_particles x 32 bytes + 4 bytes per 4x4x4 cells); other families
+ * have nothing to keep and refuse enable = 1 with CMAG_ERR_STATE. */
+int cmag_system_set_wall_cache(cmag_system *s, int32_t enable);
+int cmag_system_get_wall_cache(const cmag_system *s, int32_t *enabled);
 /* Neighbour lists kept over several steps.  No counterpart in the reference,
  * which hashes, sorts and walks the 7^3 neighbour cells on every step
  * (fluidSystem.cpp:257-319).  skin > 0 (in particle spacings 2r, at most 4):
