@@ -51,7 +51,8 @@ def test_wall_cache_same_bits_3d(gpu, lists):
         same_bits(a, b, "3-D dam break, %d steps" % (100 * (k + 1)))
     lo, hi = a.fluid_extent()
     dx = 2 * float(a.params.particle_radius)
-    assert hi[0] > 24 * dx, "the surge front is at %.1f dx of the 40 dx tank" % (hi[0] / dx)
+    # the 12 dx column has spread along the floor past 16 dx of the 40 dx tank
+    assert hi[0] > 16 * dx, "the surge front is at %.1f dx" % (hi[0] / dx)
     a.close()
     b.close()
 
