@@ -47,6 +47,8 @@ SIGNATURES = {
     "cmag_system_run_stages": ([c_sys, ctypes.c_int32], ctypes.c_int),
     "cmag_system_set_array": ([c_sys, ctypes.c_int32, c_f32p, ctypes.c_uint32, ctypes.c_uint32], ctypes.c_int),
     "cmag_system_get_array": ([c_sys, ctypes.c_int32, c_f32p, ctypes.c_uint32, ctypes.c_uint32], ctypes.c_int),
+    "cmag_batch_set_wall_cache": ([c_bat, ctypes.c_int32], ctypes.c_int),
+    "cmag_batch_get_wall_cache": ([c_bat, P(ctypes.c_int32)], ctypes.c_int),
     "cmag_system_set_wall_cache": ([c_sys, ctypes.c_int32], ctypes.c_int),
     "cmag_system_get_wall_cache": ([c_sys, P(ctypes.c_int32)], ctypes.c_int),
     "cmag_system_set_arrays": ([c_sys, ctypes.c_uint32, P(ctypes.c_int32), P(c_f32p)], ctypes.c_int),

@@ -206,6 +206,15 @@ class Batch:
     def autotune(self, reps=3):
         self._chk(lib().cmag_batch_autotune(self._h, int(reps)))
 
+    def set_wall_cache(self, enable):
+        """Kept densities of dam-break walls (same bits either way; on by default)."""
+        self._chk(lib().cmag_batch_set_wall_cache(self._h, int(bool(enable))))
+
+    def wall_cache(self):
+        e = ctypes.c_int32()
+        self._chk(lib().cmag_batch_get_wall_cache(self._h, ctypes.byref(e)))
+        return bool(e.value)
+
     def set_stage_timing(self, enable):
         self._chk(lib().cmag_batch_set_stage_timing(self._h, int(bool(enable))))
 

@@ -45,6 +45,8 @@ struct BatchScene {
     float elapsed = 0.0f;
     PhaseState host_phase{};
     uint32_t group = 0;
+    uint32_t mark_base = 0;        // DamBreak: first word of its cell-block stamps
+    uint32_t nb[3] = {0, 0, 0};    // 4x4x4 cell blocks per axis
 };
 
 struct LaunchGroup {
@@ -90,6 +92,11 @@ struct cmag_batch {
     PhaseState *phase = nullptr;
     DevParams *dev = nullptr;
     uint16_t *scene_of = nullptr;
+    // kept densities of dam-break walls (DevParams::wc_*; one epoch for the batch)
+    float4 *wc_entry = nullptr, *wc_snap = nullptr;
+    uint32_t *wc_mark = nullptr, *wc_state = nullptr;
+    uint64_t wc_marks = 0;
+    bool wc_on = false;
     float2 *zexpect = nullptr;  // whole-batch uploads: z each planar slot must keep
     uint32_t *zflags = nullptr;
     bool dev_dirty = true;
@@ -133,6 +140,16 @@ uint32_t size_bucket(uint32_t n) { return log2u(n) / 2; }
 
 bool planar_slot_for(const cmag_sph_params &p) { return planar_allowed(p, true, false); }
 
+// The kept wall densities are stale: the next step's scan starts a new epoch.
+void wall_cache_reset(cmag_batch *b)
+{
+    if (b->wc_state &&
+        cudaMemsetAsync(b->wc_state + kWcMoved, 0x01, sizeof(uint32_t), b->stream) != cudaSuccess)
+        (void)cudaGetLastError();
+}
+
+// lanes, lists or streams changed: the captured steps are re-recorded and the
+// kept wall densities recomputed
 void invalidate_graphs(cmag_batch *b)
 {
     for (int k = 0; k < 2; ++k) {
@@ -140,6 +157,7 @@ void invalidate_graphs(cmag_batch *b)
         b->gexec[k] = nullptr;
         b->gsteps[k] = 0;
     }
+    wall_cache_reset(b);
 }
 
 DevParams scene_dev(const cmag_batch *b, const BatchScene &s)
@@ -147,14 +165,25 @@ DevParams scene_dev(const cmag_batch *b, const BatchScene &s)
     DevParams d = make_dev_params(s.p, s.n, s.lay);
     d.table_base = s.table_base;
     d.part_base = s.part_base;
-    (void)b;
+    if (b->wc_on && b->wc_entry && s.p.system == CMAG_DAMBREAK) {
+        d.wc_entry = b->wc_entry;  // original order of the whole batch
+        d.wc_snap = b->wc_snap;
+        d.wc_mark = b->wc_mark + s.mark_base;
+        d.wc_state = b->wc_state;
+        d.wc_idx = b->idx[0];  // the counting sort's sorted -> original index
+        d.wc_nbx = s.nb[0];
+        d.wc_nby = s.nb[1];
+        d.wc_nbz = s.nb[2];
+    }
     return d;
 }
 
+// parameters changed (in any scene): upload them, recompute kept wall densities
 void refresh_dev(cmag_batch *b)
 {
     for (size_t k = 0; k < b->sc.size(); ++k) b->host_dev[k] = scene_dev(b, b->sc[k]);
     b->dev_dirty = true;
+    wall_cache_reset(b);
 }
 
 int upload_dev(cmag_batch *b)
@@ -308,7 +337,7 @@ int record_step(cmag_batch *b, int last, bool timed)
     mark(0);
     // keys = table slots: hash + counts + arrival ranks, offsets, counting sort
     launch_hash(rep, v, b->pos, b->hash[0], b->cnt, b->idx[0], b->err, st);
-    launch_cell_scan(b->cnt, b->off, b->table_total + 1, b->ws, st);
+    launch_cell_scan(b->cnt, b->off, b->table_total + 1, b->ws, st, b->wc_on ? b->wc_state : nullptr);
     mark(1);
     if (last >= CMAG_STAGE_SORT)
         launch_cell_sort(b->hash[0], b->idx[0], b->off, 0u, b->n_total, b->hash[1], b->idx[1],
@@ -422,7 +451,7 @@ void free_all(cmag_batch *b)
     void *ptrs[] = {b->pos, b->vel, b->vlf, b->meas, b->acc, b->vforce, b->pforce, b->pred,
                     b->spos, b->svel, b->hash[0], b->hash[1], b->idx[0], b->idx[1], b->cnt,
                     b->off, b->ws, b->err, b->red, b->aux, b->phase, b->dev, b->scene_of,
-                    b->zexpect, b->zflags};
+                    b->zexpect, b->zflags, b->wc_entry, b->wc_snap, b->wc_mark, b->wc_state};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     free_lists(b);
@@ -540,6 +569,15 @@ int cmag_batch_create(const cmag_sph_params *params, const uint32_t *counts, uin
         part += s.n;
         table += s.table_cells;
         if (s.p.system == CMAG_PERISTALSIS) b->any_peristalsis = true;
+        if (s.p.system == CMAG_DAMBREAK) {
+            s.mark_base = (uint32_t)b->wc_marks;
+            for (int a = 0; a < 3; ++a) s.nb[a] = (s.p.grid_size[a] + 3u) / 4u;
+            b->wc_marks += (uint64_t)s.nb[0] * s.nb[1] * s.nb[2];
+        }
+    }
+    if (b->wc_marks >= (1ull << 32)) {
+        delete b;
+        return bfail(nullptr, CMAG_ERR_INVALID, "the dam-break scenes' cell blocks exceed 2^32");
     }
     if (table >= (1ull << 32) - 1) {
         delete b;
@@ -625,7 +663,17 @@ int cmag_batch_create(const cmag_sph_params *params, const uint32_t *counts, uin
         step(dalloc(b, &b->scene_of, sizeof(uint16_t) * n));
         step(dalloc(b, &b->zexpect, sizeof(float2) * (size_t)scenes));
         step(dalloc(b, &b->zflags, sizeof(uint32_t) * (size_t)scenes));
+        if (b->wc_marks) {
+            step(dalloc(b, &b->wc_entry, f4));
+            step(dalloc(b, &b->wc_snap, f4));
+            step(dalloc(b, &b->wc_mark, sizeof(uint32_t) * b->wc_marks));
+            step(dalloc(b, &b->wc_state, 4 * sizeof(uint32_t)));
+            b->wc_on = true;
+        }
     }
+    // the clears above ran on the legacy stream, which the batch's non-blocking
+    // stream does not wait for
+    if (rc == CMAG_OK) cuda(cudaStreamSynchronize(cudaStreamLegacy), "cudaStreamSynchronize");
     if (rc == CMAG_OK) {
         std::vector<uint16_t> so(n);
         for (uint32_t k = 0; k < scenes; ++k)
@@ -633,7 +681,10 @@ int cmag_batch_create(const cmag_sph_params *params, const uint32_t *counts, uin
         cudaError_t e = cudaMemcpy(b->scene_of, so.data(), sizeof(uint16_t) * n, cudaMemcpyHostToDevice);
         cuda(e, "cudaMemcpy");
     }
-    if (rc == CMAG_OK) step(upload_dev(b));
+    if (rc == CMAG_OK) {
+        refresh_dev(b);  // with the kept wall densities' arrays
+        step(upload_dev(b));
+    }
     if (rc == CMAG_OK) step(upload_phase(b));
     if (rc != CMAG_OK) {
         std::string msg = b->last_error;
@@ -1279,6 +1330,25 @@ int cmag_batch_autotune(cmag_batch *b, int32_t reps)
     CB_CUDA(b, cudaStreamSynchronize(st));
     b->last_stage = CMAG_STAGE_FORCE;
     invalidate_graphs(b);
+    return CMAG_OK;
+}
+
+int cmag_batch_set_wall_cache(cmag_batch *b, int32_t enable)
+{
+    if (!b) return bfail(nullptr, CMAG_ERR_INVALID, "null handle");
+    if (enable && !b->wc_entry) return bfail(b, CMAG_ERR_STATE, "the batch holds no dam-break scene");
+    if ((enable != 0) != b->wc_on) {
+        b->wc_on = enable != 0;
+        refresh_dev(b);
+        invalidate_graphs(b);
+    }
+    return CMAG_OK;
+}
+
+int cmag_batch_get_wall_cache(const cmag_batch *b, int32_t *enabled)
+{
+    if (!b || !enabled) return bfail(nullptr, CMAG_ERR_INVALID, "null argument");
+    *enabled = b->wc_on ? 1 : 0;
     return CMAG_OK;
 }
 

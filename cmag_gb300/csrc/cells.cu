@@ -60,7 +60,7 @@ __global__ void __launch_bounds__(256)
     hash[i] = BATCH ? slot : p.scan_base + rel;  // = hr inside the table
     const uint32_t r = atomicAdd(cnt + slot, 1u);
     if (rank) rank[i] = r;
-    if (!BATCH && p.wc_mark) wall_cache_note(p, i, q, g);
+    if (p.wc_mark) wall_cache_note(p, i, q, g);
 }
 
 // The 16 counts of cells [first, first + 16) (zeros past m).

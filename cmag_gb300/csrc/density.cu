@@ -121,12 +121,12 @@ __global__ void __launch_bounds__(256, (PLANAR || (!BATCH && SYS == CMAG_DAMBREA
     // lists for every particle whose force is computed (DamBreak: fluid only);
     // lists kept over several steps serve the density too: every particle
     const bool record = LIST && active && (LIST == kKeptList || SYS != CMAG_DAMBREAK || pi.w == (float)CMAG_FLUID);
-    // A single DamBreak scene's non-fluid particle with no fluid particle in its
-    // cell box: its walk would visit non-fluid particles only, which have not
-    // moved since the epoch began, in the same runs and order, so its sum has the
-    // bits of the walk of any step of the epoch.  wc: 0 walk as usual, 1 walk and
-    // keep the result, 2 take the kept result.
-    constexpr bool WC = SYS == CMAG_DAMBREAK && !BATCH && LIST != kKeptList;
+    // A DamBreak scene's non-fluid particle with no fluid particle in its cell
+    // box: its walk would visit non-fluid particles only, which have not moved
+    // since the epoch began, in the same runs and order, so its sum has the bits
+    // of the walk of any step of the epoch.  wc: 0 walk as usual, 1 walk and keep
+    // the result, 2 take the kept result.
+    constexpr bool WC = SYS == CMAG_DAMBREAK && LIST != kKeptList;
     uint32_t wc = 0;
     if (WC && p.wc_entry && active && pi.w != (float)CMAG_FLUID &&
         !walk::fluid_near(p, grid_pos(p, pi.x, pi.y, pi.z))) {

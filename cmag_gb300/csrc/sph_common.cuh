@@ -62,13 +62,14 @@ struct DevParams {
     float list_r2;
     int32_t verlet;
     float vl_move2;  // (skin / 2)^2: a larger displacement since the rebuild forces the next one
-    // DamBreak, single scene: the density of a non-fluid particle with no fluid
-    // particle in its searched cell box depends only on the non-fluid particles,
-    // which stay put, so it is kept over steps (null: not kept).  Per particle in
-    // original order: wc_entry = (rho, p, epoch bits, 0) and wc_snap = the
-    // position it had at the last hash; per 4x4x4 block of cells: wc_mark = the
-    // stamp of the last step a fluid particle was hashed into it; wc_state = {step
-    // stamp, epoch, non-fluid particles moved}.
+    // DamBreak: the density of a non-fluid particle with no fluid particle in its
+    // searched cell box depends only on the non-fluid particles, which stay put,
+    // so it is kept over steps (null: not kept).  Per particle in original order
+    // (of the whole batch in a batch): wc_entry = (rho, p, epoch bits, 0) and
+    // wc_snap = the position it had at the last hash; per 4x4x4 block of the
+    // scene's cells: wc_mark = the stamp of the last step a fluid particle was
+    // hashed into it; wc_state = {step stamp, epoch, non-fluid particles moved}
+    // (one for all scenes of a batch).
     float4 *wc_entry;
     float4 *wc_snap;
     uint32_t *wc_mark;

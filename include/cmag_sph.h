@@ -512,6 +512,11 @@ int cmag_batch_set_group_lanes(cmag_batch *b, uint32_t group, int32_t density_la
 int cmag_batch_set_group_lists(cmag_batch *b, uint32_t group, int32_t enable);
 /* per launch group, the fastest lanes per particle for density and force */
 int cmag_batch_autotune(cmag_batch *b, int32_t reps);
+/* Kept densities of dam-break walls in every DamBreak scene of the batch, as
+ * cmag_system_set_wall_cache (same bits either way; on by default when the batch
+ * holds a dam-break scene, which enable = 1 requires). */
+int cmag_batch_set_wall_cache(cmag_batch *b, int32_t enable);
+int cmag_batch_get_wall_cache(const cmag_batch *b, int32_t *enabled);
 int cmag_batch_set_stage_timing(cmag_batch *b, int32_t enable);
 int cmag_batch_stage_times(cmag_batch *b, float ms_out[6], uint32_t *steps_out);
 const char *cmag_batch_last_error(const cmag_batch *b);

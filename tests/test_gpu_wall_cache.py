@@ -134,3 +134,41 @@ def test_wall_cache_refused_elsewhere(gpu):
         s.set_wall_cache(True)
     s.set_wall_cache(False)
     s.close()
+
+
+def test_wall_cache_batch_same_bits(gpu):
+    """A reduced copy of the benchmark's batch (16 scenes: channels and released
+    2-D dam breaks, whose gate particles are parked on one point) with and
+    without the kept wall densities, then after a change of one group's lanes."""
+    from cmag_gb300.batch import Batch
+    P, N, _, _ = presets.batched_scenes(scenes=16, seed=7, lo=2048, hi=16384)
+    pair = []
+    for on in (True, False):
+        b = Batch(P, N)
+        for k, p in enumerate(P):
+            b.reset(k)
+            if p.system == _abi.DAMBREAK:
+                b.dambreak_remove_right_boundary(k)
+        assert b.wall_cache()
+        b.set_wall_cache(on)
+        assert b.wall_cache() == on
+        b.set_graphs(True, 5)
+        pair.append(b)
+    a, b = pair
+
+    def same(label):
+        for arr in ARRAYS:
+            x, y = a.get_array_all(arr), b.get_array_all(arr)
+            bad = np.flatnonzero((x.view(np.uint32) != y.view(np.uint32)).any(axis=1))
+            assert bad.size == 0, "%s: array %d differs in %d rows" % (label, arr, bad.size)
+
+    for s in (a, b):
+        s.update_n(60)
+    same("batch, 60 steps")
+    g = next(k for k, gr in enumerate(a.groups()) if gr["system"] == _abi.DAMBREAK)
+    for s in (a, b):
+        s.set_group_lanes(g, 2, 2)
+        s.update_n(20)
+    same("batch, 20 steps at two lanes")
+    a.close()
+    b.close()
