@@ -74,9 +74,12 @@ __device__ __forceinline__ WallSide wall_side(const DevParams &p, float amp, flo
 // 256 threads, as many blocks per SM as each family fits without (large) spills,
 // to hide the gathers' latency: planar DamBreak and Poiseuille 6 (40 registers),
 // planar Peristalsis and 3-D DamBreak and Poiseuille 5 (48), 3-D Peristalsis 4
-// (64: its two 3-D force sums)
+// (64: its two 3-D force sums).  A single 3-D scene's list-driven force runs at 4
+// (56 registers): the registers hold more of the pair steps in flight than the
+// fifth block's warps (3-D dam break 0.167 -> 0.163 ms; 6 blocks spill, 0.220 ms).
 template <int SYS, bool PLANAR, bool TRIM, int G, bool BATCH, bool LIST>
-__global__ void __launch_bounds__(256, SYS == CMAG_PERISTALSIS ? (PLANAR ? 5 : 4) : (PLANAR ? 6 : 5))
+__global__ void __launch_bounds__(256, SYS == CMAG_PERISTALSIS ? (PLANAR ? 5 : 4)
+                                                               : (PLANAR ? 6 : ((LIST && !BATCH) ? 4 : 5)))
     k_force(DevParams pv, BatchView bv, const float4 *__restrict__ spos,
             const float4 *__restrict__ svel, const float2 *__restrict__ aux,
             const uint32_t *__restrict__ idx, const uint32_t *__restrict__ off_all,
