@@ -232,12 +232,24 @@ class Pair:
         self.coarse.close()
 
 
-def normalization_from(feat_dev, target_dev):
-    """Feature mean / inverse std and the target scale over a dataset."""
-    f = feat_dev.double()
-    mean = f.mean(0)
-    std = f.std(0).clamp_min(1e-6)
-    scale = float(target_dev.double().pow(2).mean().sqrt().clamp_min(1e-9))
+def normalization_from(feat_dev, target_dev, chunk=1 << 24):
+    """Feature mean / inverse std and the target scale over a dataset (sums in
+    FP64, a chunk of rows at a time, so the data set is never copied whole)."""
+    import torch
+    n = feat_dev.shape[0]
+    s1 = torch.zeros(feat_dev.shape[1], dtype=torch.float64, device=feat_dev.device)
+    s2 = torch.zeros_like(s1)
+    t2 = torch.zeros((), dtype=torch.float64, device=feat_dev.device)
+    for a in range(0, n, chunk):
+        f = feat_dev[a:a + chunk].double()
+        s1 += f.sum(0)
+        s2 += f.pow(2).sum(0)
+        t2 += target_dev[a:a + chunk].double().pow(2).sum()
+    mean = s1 / n
+    # unbiased variance, as torch.std
+    var = ((s2 - n * mean * mean) / max(n - 1, 1)).clamp_min(0.0)
+    std = var.sqrt().clamp_min(1e-6)
+    scale = float((t2 / (n * target_dev.shape[1])).sqrt().clamp_min(1e-9))
     return mean.float().cpu().numpy(), (1.0 / std).float().cpu().numpy(), scale
 
 
