@@ -59,8 +59,29 @@ public:
     {
         check(cmag_system_get_array(h_, array, data, (uint32_t)start, (uint32_t)count), h_);
     }
+    // several whole float4 arrays with one synchronisation (arrays[k] <-> data[k])
+    void setArrays(uint32_t count, const int32_t *arrays, const float *const *data)
+    {
+        check(cmag_system_set_arrays(h_, count, arrays, data), h_);
+    }
+    void getArrays(uint32_t count, const int32_t *arrays, float *const *data) const
+    {
+        check(cmag_system_get_arrays(h_, count, arrays, data), h_);
+    }
     void updateSteps(uint32_t steps) { check(cmag_system_update_n(h_, steps), h_); }
     void synchronize() { check(cmag_system_synchronize(h_), h_); }
+    // neighbour-loop choices (none changes a result bit beyond the lanes' summation order)
+    void autotune(int reps = 3) { check(cmag_system_autotune(h_, reps), h_); }
+    void setNeighborLists(bool enable) { check(cmag_system_set_neighbor_lists(h_, enable ? 1 : 0), h_); }
+    void setGroups(int densityLanes, int forceLanes) { check(cmag_system_set_groups(h_, densityLanes, forceLanes), h_); }
+    // dam breaks: kept wall densities (on by default; same bits either way)
+    void setWallCache(bool enable) { check(cmag_system_set_wall_cache(h_, enable ? 1 : 0), h_); }
+    bool wallCache() const
+    {
+        int32_t e = 0;
+        check(cmag_system_get_wall_cache(h_, &e), h_);
+        return e != 0;
+    }
     // max x, y, z of a fluid particle (device reduction)
     float3 fluidMax() const
     {
@@ -281,6 +302,7 @@ public:
     void setGraphs(bool enable, uint32_t stepsPerGraph = 1) { chk(cmag_batch_set_graphs(h_, enable ? 1 : 0, stepsPerGraph)); }
     void autotune(int reps = 3) { chk(cmag_batch_autotune(h_, reps)); }
     void set_group_lists(uint32_t group, bool enable) { chk(cmag_batch_set_group_lists(h_, group, enable ? 1 : 0)); }
+    void setWallCache(bool enable) { chk(cmag_batch_set_wall_cache(h_, enable ? 1 : 0)); }
     void synchronize() { chk(cmag_batch_synchronize(h_)); }
 
 private:
