@@ -338,14 +338,17 @@ def collect(pair, seeds, snapshots, every, min_shepard=0.5):
     return feat_dev[:row].contiguous(), target_dev[:row].contiguous()
 
 
-def collect_filtered(pair, seeds, snapshots, every, window, min_shepard=0.5):
+def collect_filtered(pair, seeds, snapshots, every, window, min_shepard=0.5, deadline=None, done=None):
     """Training rows with time-filtered targets: along the lockstep fine/coarse
     runs of each seed (no restarts), the target of a coarse fluid particle is its
     missed acceleration averaged over the `window` coarse steps that end at the
     sample (the acoustic part, which the two resolutions do not share, averages
     out; what the coarse method misses systematically stays), and its features
     are those at the sample.  `every` fine steps between samples (even, at least
-    2 window).  Returns device (features, targets)."""
+    2 window).  With a `deadline` (time.perf_counter() value) no seed starts after
+    it; `done` (a list) receives the seeds collected.  Returns device (features,
+    targets)."""
+    import time
     import torch
     if every % 2 or every < 2 * window:
         raise ValueError("`every` must be even and at least 2 * window")
@@ -355,6 +358,10 @@ def collect_filtered(pair, seeds, snapshots, every, window, min_shepard=0.5):
     target_dev = torch.empty((rows, NOUT), dtype=torch.float32, device="cuda")
     row = 0
     for seed in seeds:
+        if deadline is not None and time.perf_counter() > deadline:
+            break
+        if done is not None:
+            done.append(seed)
         pair.start(seed)
         for _ in range(snapshots):
             lead = every - 2 * window

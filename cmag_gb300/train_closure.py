@@ -1,7 +1,8 @@
 """Train the learned closure of the coarse 3-D dam break and save it.
 
     python -m cmag_gb300.train_closure [--seeds 20] [--window 10] [--t-train 1.0]
-        [--sample-every 0.025] [--steps 4000] [--out cmag_gb300/data/closure_dambreak3d.npz]
+        [--sample-every 0.025] [--steps 4000] [--time-budget S]
+        [--out cmag_gb300/data/closure_dambreak3d.npz]
 
 The fine run is the 64x128x64 dam break (dt 5e-5), the coarse run its 2x-coarser
 twin (32x64x32 fluid, dt 1e-4).  For each training seed (jitter seeds 2001, 2002,
@@ -60,8 +61,11 @@ def main():
     ap.add_argument("--sample-every", type=float, default=0.025)
     ap.add_argument("--steps", type=int, default=4000)
     ap.add_argument("--out", default=DEFAULT_OUT)
+    ap.add_argument("--time-budget", type=float, default=None,
+                    help="seconds of data collection after which no further seed starts")
     args = ap.parse_args()
-    run(args.seeds, args.window, args.t_train, args.sample_every, args.steps, args.out)
+    run(args.seeds, args.window, args.t_train, args.sample_every, args.steps, args.out,
+        time_budget=args.time_budget)
 
 
 def initial_params(seed=0):
@@ -80,7 +84,7 @@ def initial_params(seed=0):
 
 
 def run(seeds=20, window=10, t_train=1.0, sample_every=0.025, steps=4000, out=DEFAULT_OUT, valid_seed=998,
-        log=print):
+        log=print, time_budget=None):
     import torch
     pair = C.Pair()
     fine_dt = float(pair.pf.delta_time)
@@ -88,9 +92,12 @@ def run(seeds=20, window=10, t_train=1.0, sample_every=0.025, steps=4000, out=DE
     snaps = int(round(t_train / sample_every))
     train_seeds = list(range(2001, 2001 + seeds))
     t0 = time.perf_counter()
-    feat, tgt = C.collect_filtered(pair, train_seeds, snaps, every, window)
+    done = []
+    feat, tgt = C.collect_filtered(pair, train_seeds, snaps, every, window,
+                                   deadline=None if time_budget is None else t0 + time_budget, done=done)
+    train_seeds = done
     t_data = time.perf_counter() - t0
-    log("data: %d rows from %d seeds in %.1f s" % (feat.shape[0], seeds, t_data))
+    log("data: %d rows from %d seeds in %.1f s" % (feat.shape[0], len(train_seeds), t_data))
     c = C.Closure(initial_params(0))
     mean, inv, scale = C.normalization_from(feat, tgt)
     c.set_normalization(mean, inv, scale)
