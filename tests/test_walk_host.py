@@ -144,3 +144,18 @@ def test_harness_detects_a_missed_neighbour(walk_lib):
                               pos.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), pos.shape[0],
                               ctypes.byref(visited))
     assert bad > 0
+
+
+@pytest.mark.parametrize("grid,c", [((264, 245, 72), 3), ((16, 16, 4), 3), ((13, 11, 9), 3), ((5, 6, 7), 1),
+                                    ((5, 6, 7), 2), ((4, 4, 4), 3), ((9, 33, 10), 2)])
+def test_wall_cache_fluid_test_matches_brute_force(walk_lib, grid, c):
+    """The kept wall densities' test for fluid in a wall particle's cell box
+    (neighbor_walk.cuh: fluid_near) against every cell of the wrapped box: grids
+    that are and are not multiples of the 4-cell blocks, boxes wider than the
+    grid, cells outside the grid."""
+    walk_lib.wall_near_check.restype = ctypes.c_int64
+    walk_lib.wall_near_check.argtypes = [ctypes.POINTER(ctypes.c_uint32), ctypes.c_int, ctypes.c_uint32,
+                                         ctypes.c_uint64]
+    g = (ctypes.c_uint32 * 3)(*grid)
+    bad = walk_lib.wall_near_check(g, c, 4000, 1234 + c)
+    assert bad == 0, "%d of 4000 cell boxes judged wrongly" % bad

@@ -215,3 +215,53 @@ extern "C" int64_t walk_check(int system, int planar, int trim, int lanes, const
     if (system == CMAG_POISEUILLE) return by_shape<CMAG_POISEUILLE>(sc, lanes, visited);
     return by_shape<CMAG_PERISTALSIS>(sc, lanes, visited);
 }
+
+// The kept wall densities' fluid test (walk::fluid_near, the density side;
+// wall_cache_note stamps a fluid particle's block of its wrapped cell) against
+// brute force: for random cell-block stamps and random cells (inside the grid and
+// up to two grid periods outside), fluid_near must report exactly whether some
+// cell of the box g - c .. g + c, wrapped per axis, lies in a block stamped with
+// the current step's stamp.  Returns the number of disagreements.
+extern "C" int64_t wall_near_check(const uint32_t grid[3], int cell_count, uint32_t trials, uint64_t seed)
+{
+    DevParams p;
+    std::memset(&p, 0, sizeof p);
+    p.gx = grid[0];
+    p.gy = grid[1];
+    p.gz = grid[2];
+    p.cell_count = cell_count;
+    p.wc_nbx = (p.gx + 3u) / 4u;
+    p.wc_nby = (p.gy + 3u) / 4u;
+    p.wc_nbz = (p.gz + 3u) / 4u;
+    std::vector<uint32_t> marks((size_t)p.wc_nbx * p.wc_nby * p.wc_nbz), state(4, 0u);
+    const uint32_t stamp = 7u;
+    state[kWcStamp] = stamp;
+    p.wc_mark = marks.data();
+    p.wc_state = state.data();
+    uint64_t x = seed;
+    auto next = [&]() {  // splitmix64
+        x += 0x9e3779b97f4a7c15ull;
+        uint64_t z = x;
+        z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+        z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+        return z ^ (z >> 31);
+    };
+    auto residue = [](int v, uint32_t n) { const int m = v % (int)n; return (uint32_t)(m < 0 ? m + (int)n : m); };
+    int64_t bad = 0;
+    for (uint32_t t = 0; t < trials; ++t) {
+        if (t % 64 == 0)  // a few stamped blocks among stale ones
+            for (auto &m : marks) m = (next() % 97 == 0) ? stamp : (uint32_t)(next() % 7);
+        const int g[3] = {(int)(next() % (5 * p.gx)) - 2 * (int)p.gx, (int)(next() % (5 * p.gy)) - 2 * (int)p.gy,
+                          (int)(next() % (5 * p.gz)) - 2 * (int)p.gz};
+        bool want = false;
+        for (int dz = -cell_count; dz <= cell_count && !want; ++dz)
+            for (int dy = -cell_count; dy <= cell_count && !want; ++dy)
+                for (int dx = -cell_count; dx <= cell_count && !want; ++dx) {
+                    const uint32_t bx = residue(g[0] + dx, p.gx) >> 2, by = residue(g[1] + dy, p.gy) >> 2,
+                                   bz = residue(g[2] + dz, p.gz) >> 2;
+                    want = marks[((size_t)bz * p.wc_nby + by) * p.wc_nbx + bx] == stamp;
+                }
+        if (walk::fluid_near(p, make_int3(g[0], g[1], g[2])) != want) ++bad;
+    }
+    return bad;
+}
