@@ -663,13 +663,23 @@ int cmag_batch_create(const cmag_sph_params *params, const uint32_t *counts, uin
         step(dalloc(b, &b->scene_of, sizeof(uint16_t) * n));
         step(dalloc(b, &b->zexpect, sizeof(float2) * (size_t)scenes));
         step(dalloc(b, &b->zflags, sizeof(uint32_t) * (size_t)scenes));
-        if (b->wc_marks) {
-            step(dalloc(b, &b->wc_entry, f4));
-            step(dalloc(b, &b->wc_snap, f4));
-            step(dalloc(b, &b->wc_mark, sizeof(uint32_t) * b->wc_marks));
-            step(dalloc(b, &b->wc_state, 4 * sizeof(uint32_t)));
-            b->wc_on = true;
+    }
+    if (rc == CMAG_OK && b->wc_marks) {
+        // kept wall densities: an optimisation, so the batch is made without them
+        // when their memory cannot be had
+        void **bufs[4] = {(void **)&b->wc_entry, (void **)&b->wc_snap, (void **)&b->wc_mark, (void **)&b->wc_state};
+        const size_t sizes[4] = {f4, f4, sizeof(uint32_t) * b->wc_marks, 4 * sizeof(uint32_t)};
+        bool ok = true;
+        for (int k = 0; k < 4 && ok; ++k)
+            ok = cudaMalloc(bufs[k], sizes[k]) == cudaSuccess && cudaMemset(*bufs[k], 0, sizes[k]) == cudaSuccess;
+        if (!ok) {
+            (void)cudaGetLastError();
+            for (int k = 0; k < 4; ++k) {
+                if (*bufs[k]) cudaFree(*bufs[k]);
+                *bufs[k] = nullptr;
+            }
         }
+        b->wc_on = ok;
     }
     // the clears above ran on the legacy stream, which the batch's non-blocking
     // stream does not wait for
@@ -1336,7 +1346,7 @@ int cmag_batch_autotune(cmag_batch *b, int32_t reps)
 int cmag_batch_set_wall_cache(cmag_batch *b, int32_t enable)
 {
     if (!b) return bfail(nullptr, CMAG_ERR_INVALID, "null handle");
-    if (enable && !b->wc_entry) return bfail(b, CMAG_ERR_STATE, "the batch holds no dam-break scene");
+    if (enable && !b->wc_entry) return bfail(b, CMAG_ERR_STATE, "no kept wall densities here (no dam-break scene, or their memory could not be had)");
     if ((enable != 0) != b->wc_on) {
         b->wc_on = enable != 0;
         refresh_dev(b);

@@ -936,13 +936,24 @@ int cmag_system_create(const cmag_sph_params *params, uint32_t n, cmag_system **
     // 6 extent keys + pad (32 B), 4 doubles (32 B), 1 count (8 B)
     step(dalloc(s, &s->red, 128));
     step(dalloc(s, &s->zflag, kMaxArraysPerCall * sizeof(uint32_t)));
-    if (params->system == CMAG_DAMBREAK) {
+    if (rc == CMAG_OK && params->system == CMAG_DAMBREAK) {
+        // kept wall densities: an optimisation, so the instance is made without
+        // them when their memory cannot be had
         for (int a = 0; a < 3; ++a) s->wc_nb[a] = (params->grid_size[a] + 3u) / 4u;
-        step(dalloc(s, &s->wc_entry, f4));
-        step(dalloc(s, &s->wc_snap, f4));
-        step(dalloc(s, &s->wc_mark, sizeof(uint32_t) * (size_t)s->wc_nb[0] * s->wc_nb[1] * s->wc_nb[2]));
-        step(dalloc(s, &s->wc_state, 4 * sizeof(uint32_t)));
-        s->wc_on = true;
+        const size_t marks = sizeof(uint32_t) * (size_t)s->wc_nb[0] * s->wc_nb[1] * s->wc_nb[2];
+        void **bufs[4] = {(void **)&s->wc_entry, (void **)&s->wc_snap, (void **)&s->wc_mark, (void **)&s->wc_state};
+        const size_t sizes[4] = {f4, f4, marks, 4 * sizeof(uint32_t)};
+        bool ok = true;
+        for (int k = 0; k < 4 && ok; ++k)
+            ok = cudaMalloc(bufs[k], sizes[k]) == cudaSuccess && cudaMemset(*bufs[k], 0, sizes[k]) == cudaSuccess;
+        if (!ok) {
+            (void)cudaGetLastError();
+            for (int k = 0; k < 4; ++k) {
+                if (*bufs[k]) cudaFree(*bufs[k]);
+                *bufs[k] = nullptr;
+            }
+        }
+        s->wc_on = ok;
     }
     if (rc != CMAG_OK) {
         std::string msg = s->last_error;
@@ -1640,7 +1651,7 @@ int cmag_system_get_verlet(cmag_system *s, float *skin, uint32_t *rebuilds)
 int cmag_system_set_wall_cache(cmag_system *s, int32_t enable)
 {
     if (!s) return fail(nullptr, CMAG_ERR_INVALID, "null handle");
-    if (enable && !s->wc_entry) return fail(s, CMAG_ERR_STATE, "wall densities are kept for dam-break systems only");
+    if (enable && !s->wc_entry) return fail(s, CMAG_ERR_STATE, "no kept wall densities here (dam-break systems only; none when their memory could not be had)");
     if ((enable != 0) != s->wc_on) {
         s->wc_on = enable != 0;
         invalidate_graph(s);

@@ -327,8 +327,9 @@ int cmag_system_get_neighbor_lists(const cmag_system *s, int32_t *enabled, uint3
  * same non-fluid particles in the same order, so the reused value has the bits
  * the walk would give).  A non-fluid particle that moves or changes type, and any
  * change of parameters, lanes or lists, starts over.  On by default for DamBreak
- * (memory: num_particles x 32 bytes + 4 bytes per 4x4x4 cells); other families
- * have nothing to keep and refuse enable = 1 with CMAG_ERR_STATE. */
+ * (memory: num_particles x 32 bytes + 4 bytes per 4x4x4 cells; an instance whose
+ * creation could not have that memory is made without it); other families have
+ * nothing to keep.  enable = 1 without kept wall densities: CMAG_ERR_STATE. */
 int cmag_system_set_wall_cache(cmag_system *s, int32_t enable);
 int cmag_system_get_wall_cache(const cmag_system *s, int32_t *enabled);
 /* Neighbour lists kept over several steps.  No counterpart in the reference,
