@@ -330,13 +330,12 @@ int record_step(cmag_batch *b, int last, bool timed)
         b->events_used += 7;
     }
     auto mark = [&](int k) { if (ev) cudaEventRecord(ev[k], st); };
-    if (b->any_peristalsis) {
-        launch_phase_batch(b->dev, (uint32_t)b->sc.size(), b->phase, b->k_milli, st);
-        launch_configure_boundary(rep, v, b->pos, b->phase, st);
-    }
+    // Peristalsis scenes: this step's phase blocks (walls configured in the hash pass)
+    if (b->any_peristalsis) launch_phase_batch(b->dev, (uint32_t)b->sc.size(), b->phase, b->k_milli, st);
     mark(0);
     // keys = table slots: hash + counts + arrival ranks, offsets, counting sort
-    launch_hash(rep, v, b->pos, b->hash[0], b->cnt, b->idx[0], b->err, st);
+    launch_hash(rep, v, b->pos, b->hash[0], b->cnt, b->idx[0], b->err, st, nullptr,
+                b->any_peristalsis ? b->phase : nullptr);
     launch_cell_scan(b->cnt, b->off, b->table_total + 1, b->ws, st, b->wc_on ? b->wc_state : nullptr);
     mark(1);
     if (last >= CMAG_STAGE_SORT)

@@ -37,17 +37,26 @@ constexpr uint32_t kScanTile = kScanThreads * kScanItems;
 // in the table's last cell and reported as CMAG_DEVERR_RANGE.  rank[i] (when
 // given) is the count the particle's atomic increment found: its arrival order
 // among the particles of its cell.
+//
+// ph_all (one PhaseState per scene, or null): a Peristalsis wall particle is
+// first placed on its wall when the step configures the boundary (the
+// configureBoundaryD pass fused into the hash: the same arithmetic, one read of
+// the positions instead of two).
 template <bool BATCH>
 __global__ void __launch_bounds__(256)
-    k_hash(DevParams pv, BatchView bv, const float4 *__restrict__ pos, uint32_t *__restrict__ hash,
+    k_hash(DevParams pv, BatchView bv, float4 *__restrict__ pos, uint32_t *__restrict__ hash,
            uint32_t *__restrict__ cnt, uint32_t *__restrict__ rank, uint32_t *err,
-           float4 *__restrict__ snap)
+           float4 *__restrict__ snap, const PhaseState *__restrict__ ph_all)
 {
     pdl_entry();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= (BATCH ? bv.n_total : pv.n)) return;
     const DevParams &p = BATCH ? bv.scenes[bv.scene_of[i]] : pv;
-    const float4 q = pos[i];
+    float4 q = pos[i];
+    if (ph_all && p.system == CMAG_PERISTALSIS) {
+        const PhaseState *ph = ph_all + (BATCH ? bv.scene_of[i] : 0u);
+        if (ph->configure && configure_wall(p, ph->configure_height, q)) pos[i] = q;
+    }
     if (snap) snap[i] = q;  // positions the kept lists are built from
     const int3 g = grid_pos(p, q.x, q.y, q.z);
     const uint32_t hr = grid_hash(p, g.x, g.y, g.z);
@@ -282,14 +291,15 @@ __global__ void k_cell_view(const uint32_t *__restrict__ off, uint32_t scan_base
 
 }  // namespace
 
-void launch_hash(const DevParams &p, const BatchView &bv, const float4 *pos, uint32_t *hash,
-                 uint32_t *cnt, uint32_t *rank, uint32_t *err, cudaStream_t st, float4 *snap)
+void launch_hash(const DevParams &p, const BatchView &bv, float4 *pos, uint32_t *hash,
+                 uint32_t *cnt, uint32_t *rank, uint32_t *err, cudaStream_t st, float4 *snap,
+                 const PhaseState *ph)
 {
     const uint32_t n = bv.scenes ? bv.n_total : p.n;
     if (n == 0) return;
     const uint32_t blocks = (n + 255) / 256;
-    if (bv.scenes) launch_pdl(k_hash<true>, blocks, 256, 0, st, p, bv, pos, hash, cnt, rank, err, snap);
-    else launch_pdl(k_hash<false>, blocks, 256, 0, st, p, bv, pos, hash, cnt, rank, err, snap);
+    if (bv.scenes) launch_pdl(k_hash<true>, blocks, 256, 0, st, p, bv, pos, hash, cnt, rank, err, snap, ph);
+    else launch_pdl(k_hash<false>, blocks, 256, 0, st, p, bv, pos, hash, cnt, rank, err, snap, ph);
 }
 
 void launch_cell_sort(const uint32_t *hash, const uint32_t *rank, const uint32_t *off,

@@ -14,12 +14,6 @@ namespace cmag {
 
 namespace {
 
-// GetWave (PeristalsisKernel.cuh:59-62), wave_k = pi * waves / (fx * r)
-__device__ __forceinline__ float get_wave(const DevParams &p, float x, float t)
-{
-    return sinf(p.wave_k * ((x - p.ox) - p.wave_speed * t));
-}
-
 // Advance one boundary-configuration phase exactly as the host mirror does
 // (separately rounded adds and multiplies, no contraction).
 __device__ __forceinline__ void advance_phase(const DevParams &p, PhaseState *ph, float k_milli)
@@ -79,17 +73,9 @@ __global__ void __launch_bounds__(256)
     if (BATCH && p.system != CMAG_PERISTALSIS) return;
     const PhaseState *ph = ph_all + sc;
     if (!ph->configure) return;
-    const float wh = ph->configure_height;
     float4 q = pos[i];
-    if (q.w > 0.0f) {
-        q.y = -p.half_fluid_h + wh * get_wave(p, q.x, 0.0f) - p.r * (q.w - 1.0f);
-        pos[i] = q;
-    } else if (q.w < 0.0f) {
-        q.y = p.half_fluid_h - wh * get_wave(p, q.x, 0.0f) + p.r * (-q.w - 1.0f);
-        pos[i] = q;
-    } else {
-        return;
-    }
+    if (!configure_wall(p, ph->configure_height, q)) return;
+    pos[i] = q;
     if (xb) check_moved(p, q, xb[i], moved);
 }
 

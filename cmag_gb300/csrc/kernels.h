@@ -82,10 +82,12 @@ void launch_onesweep_pass(const uint32_t *kin, const uint32_t *vin, uint32_t *ko
 // ---- cells (cells.cu) --------------------------------------------------------
 // Hash every particle and count particles per cell.  rank (may be null): per
 // particle, its arrival order among the particles of its cell (0, 1, ...; not
-// deterministic).
-void launch_hash(const DevParams &p, const BatchView &bv, const float4 *pos, uint32_t *hash,
+// deterministic).  ph (Peristalsis phase blocks, may be null): first place the
+// wall particles on their walls where the step configures the boundary (the
+// work of launch_configure_boundary, fused).
+void launch_hash(const DevParams &p, const BatchView &bv, float4 *pos, uint32_t *hash,
                  uint32_t *cnt, uint32_t *rank, uint32_t *err, cudaStream_t st,
-                 float4 *snap = nullptr);
+                 float4 *snap = nullptr, const PhaseState *ph = nullptr);
 // Stable counting sort of the hashed particles by cell, from the dense offsets
 // (after launch_cell_scan): shash/idx = the hashes and original indices in the
 // order of a stable sort by hash (the radix sort's result exactly), and

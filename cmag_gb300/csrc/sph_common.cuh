@@ -124,6 +124,28 @@ struct PhaseState {
     float t;                  // time passed to the force/integrate kernels
 };
 
+// GetWave (PeristalsisKernel.cuh:59-62), wave_k = pi * waves / (fx * r)
+__device__ __forceinline__ float get_wave(const DevParams &p, float x, float t)
+{
+    return sinf(p.wave_k * ((x - p.ox) - p.wave_speed * t));
+}
+
+// configureBoundaryD (Peristalsis.Core/PeristalsisKernel.cu:144-171): a wall
+// particle (w > 0 bottom, w < 0 top; |w| its layer) placed on the wall of height
+// wh; false for a fluid particle (w = 0), which stays where it is.
+__device__ __forceinline__ bool configure_wall(const DevParams &p, float wh, float4 &q)
+{
+    if (q.w > 0.0f) {
+        q.y = -p.half_fluid_h + wh * get_wave(p, q.x, 0.0f) - p.r * (q.w - 1.0f);
+        return true;
+    }
+    if (q.w < 0.0f) {
+        q.y = p.half_fluid_h - wh * get_wave(p, q.x, 0.0f) + p.r * (-q.w - 1.0f);
+        return true;
+    }
+    return false;
+}
+
 // ---------------------------------------------------------------- hashing ---
 
 // calcGridPos: DamBreak divides by the cell size (fluid_kernel.cu:19-25); the

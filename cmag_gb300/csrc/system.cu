@@ -615,14 +615,13 @@ int record_step(cmag_system *s, int last, bool timed)
     }
     auto mark = [&](int k) { if (ev) cudaEventRecord(ev[k], st); };
 
-    if (p.system == CMAG_PERISTALSIS) {
-        launch_phase(d, s->phase, s->k_milli, st);
-        launch_configure_boundary(d, BatchView{}, s->pos, s->phase, st);
-    }
+    // Peristalsis: the phase block of this step (the walls are configured in the hash pass)
+    if (p.system == CMAG_PERISTALSIS) launch_phase(d, s->phase, s->k_milli, st);
     mark(0);
     // hash + per-cell counts (and each particle's arrival rank in its cell), dense
     // offsets, then the stable counting sort by cell
-    launch_hash(d, BatchView{}, s->pos, s->hash[0], s->cnt, s->idx[0], s->err, st);
+    launch_hash(d, BatchView{}, s->pos, s->hash[0], s->cnt, s->idx[0], s->err, st, nullptr,
+                p.system == CMAG_PERISTALSIS ? s->phase : nullptr);
     launch_cell_scan(s->cnt, s->off, s->scan_cells + 1, s->ws, st, d.wc_state);
     mark(1);
     if (last >= CMAG_STAGE_SORT)
