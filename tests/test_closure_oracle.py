@@ -40,3 +40,22 @@ def test_parameter_layout():
     assert C.NPARAMS == 16 * 64 + 64 + 2 * (64 * 64 + 64) + 3 * 64 + 3
     theta = np.arange(C.NPARAMS, dtype=np.float64)
     assert np.array_equal(C.pack(C.unpack(theta)), theta)
+
+
+def test_normalization_sums_chunk_by_chunk():
+    """The training set's normalisation (cmag_gb300.closure.normalization_from)
+    sums a chunk of rows at a time; any chunking gives torch's mean, unbiased
+    standard deviation and target RMS."""
+    torch = __import__("pytest").importorskip("torch")
+    from cmag_gb300 import closure as CL
+    g = torch.Generator().manual_seed(5)
+    feat = torch.randn(10007, 16, generator=g) * torch.linspace(0.1, 30.0, 16) + torch.linspace(-5.0, 5.0, 16)
+    tgt = torch.randn(10007, 3, generator=g) * 0.25
+    want_mean = feat.double().mean(0).numpy()
+    want_std = feat.double().std(0).numpy()
+    want_scale = float(tgt.double().pow(2).mean().sqrt())
+    for chunk in (1000, 4096, 1 << 24):
+        mean, inv, scale = CL.normalization_from(feat, tgt, chunk=chunk)
+        assert np.allclose(mean, want_mean, rtol=1e-6, atol=1e-6)
+        assert np.allclose(1.0 / inv, want_std, rtol=1e-5)
+        assert abs(scale - want_scale) <= 1e-6 * want_scale
